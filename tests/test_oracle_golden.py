@@ -1,0 +1,156 @@
+"""The CPU oracle against the golden values the reference's own tests pin for the MIRK
+path (lib/BoundaryValueDiffEqMIRK/test/Core/mirk_basic_tests.jl and ensemble_tests.jl).
+These run on the CPU only; they establish that the oracle restates the reference before
+it is used to judge the CUDA library."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle, RET_SUCCESS
+
+ORDERS = (2, 3, 4, 5, 6)
+
+
+def _oracle(p):
+    return Oracle(p.source, p.M, p.n_params, twopoint=p.twopoint, bc_t=p.bc_t, La=p.La, Lb=p.Lb)
+
+
+def _solve1(p, dt=None, n=None, params=(), y0=None, **kw):
+    o = _oracle(p)
+    t0, t1 = p.tspan
+    if n is None:
+        n = int(math.ceil((t1 - t0) / dt - 1e-12))  # cld(t1 - t0, dt) (Core/utils.jl:354)
+    pa = np.asarray(params, dtype=np.float64).reshape(1, -1) if len(params) else np.zeros((1, 1))
+    y0 = p.u0 if y0 is None else y0
+    r = o.solve_batch(pa, [n], [[t0, t1]], np.asarray(y0, dtype=np.float64), want_stages=True, **kw)
+    N = int(r["n_nodes"][0])
+    return o, r, N
+
+
+@pytest.mark.parametrize("order", ORDERS)
+@pytest.mark.parametrize("name", ["affine", "affine_twopoint"])
+def test_affineness(problems, name, order):
+    # mirk_basic_tests.jl:103-118: exact solution u1 = 5 - t; dt = 0.2
+    p = problems.ALL[name]
+    o, r, N = _solve1(p, dt=0.2, order=order)
+    assert r["retcode"][0] == RET_SUCCESS
+    u1 = r["y"][0, :N, 0]
+    assert np.abs(np.diff(u1) + 0.2).max() + abs(u1[0] - 5) < 1e-2
+
+
+@pytest.mark.parametrize("order", ORDERS)
+@pytest.mark.parametrize("name", ["linear", "linear_twopoint"])
+def test_convergence_order_linear(problems, name, order):
+    # mirk_basic_tests.jl:122-139: observed order ~ p within 0.4 on dts = 1/8, 1/4, 1/2.
+    p = problems.ALL[name]
+    errs = []
+    for dt in (1 / 8, 1 / 4, 1 / 2):
+        o, r, N = _solve1(p, dt=dt, order=order, adaptive=0, max_newton=20)
+        assert r["retcode"][0] == RET_SUCCESS
+        t = r["mesh"][0, :N]
+        errs.append(np.abs(r["y"][0, :N] - problems.linear_analytic(t)).max())
+    errs = np.array(errs)
+    est = np.log2(errs[1:] / errs[:-1]).mean()
+    assert abs(est - order) < 0.4, (errs, est)
+
+
+@pytest.mark.parametrize("order", ORDERS)
+def test_interpolation_twopoint(problems, order):
+    # mirk_basic_tests.jl:181-223 and 235-244: sol(0.001) and sol(0.04, Val{1}), atol 1e-6
+    p = problems.TWOPOINT_INTERP
+    o, r, N = _solve1(p, dt=0.001, params=(1.0,), order=order)
+    assert r["retcode"][0] == RET_SUCCESS
+    mesh, y, K, KI = r["mesh"][0, :N], r["y"][0], r["K"][0], r["KI"][0]
+    u, du = problems.twopoint_interp_analytic(np.array([0.001]))
+    got = o.interpolate(order, mesh, y, K, KI, [0.001])
+    assert np.abs(got - u).max() < 1e-6
+    u4, du4 = problems.twopoint_interp_analytic(np.array([0.04]))
+    assert np.abs(o.interpolate(order, mesh, y, K, KI, [0.04]) - u4).max() < 1e-6
+    assert np.abs(o.interpolate(order, mesh, y, K, KI, [0.04], deriv=1) - du4).max() < 1e-6
+
+
+@pytest.mark.parametrize("adaptive", [1, 0])
+@pytest.mark.parametrize("order", ORDERS)
+def test_interpolation_multipoint(problems, order, adaptive):
+    # mirk_basic_tests.jl:271-312: sol(pi/6) and sol(pi/3) vs (sin, cos), atol 1e-6
+    p = problems.MULTIPOINT
+    o, r, N = _solve1(p, dt=0.001, order=order, adaptive=adaptive)
+    assert r["retcode"][0] == RET_SUCCESS
+    mesh, y, K, KI = r["mesh"][0, :N], r["y"][0], r["K"][0], r["KI"][0]
+    for t in (math.pi / 6, math.pi / 3):
+        got = o.interpolate(order, mesh, y, K, KI, [t])[0]
+        assert np.abs(got - [math.sin(t), math.cos(t)]).max() < 1e-6
+
+
+def test_torus_geodesic_refines(problems):
+    # mirk_basic_tests.jl:726-756: adaptive refinement, BCs satisfied to 1e-8
+    p = problems.TORUS
+    a1, a2 = (0.5, -1.2), (-0.5, 0.3)
+    o, r, N = _solve1(p, dt=0.05, params=a1 + a2, order=4)
+    assert r["retcode"][0] == RET_SUCCESS
+    y = r["y"][0, :N]
+    assert np.abs(y[0, :2] - a1).max() < 1e-8
+    assert np.abs(y[-1, :2] - a2).max() < 1e-8
+
+
+def test_initial_guess_passthrough(problems):
+    # mirk_basic_tests.jl:678-720: maxiters = 0, non-adaptive -> the guess comes back exactly
+    p = problems.LINEAR_TWOPOINT
+    o = _oracle(p)
+    n = 10
+    rng = np.random.default_rng(7)
+    guess = rng.normal(size=(n + 1, 2))
+    r = o.solve_batch(np.zeros((1, 1)), [n], [[0.0, 1.0]], guess, y0_mode=1, adaptive=0,
+                      max_newton=0, linesearch_fallback=0)
+    assert np.array_equal(r["y"][0, :n + 1], guess)
+
+
+@pytest.mark.parametrize("order", ORDERS)
+def test_ensemble_converges(problems, order):
+    # ensemble_tests.jl:7-41: random p per trajectory, every trajectory converged
+    p = problems.ENSEMBLE
+    o = _oracle(p)
+    rng = np.random.default_rng(11)
+    n = 10
+    params = rng.uniform(0, 1, (n, 1))
+    r = o.solve_batch(params, [16] * n, np.tile(p.tspan, (n, 1)), np.tile(p.u0, (n, 1)),
+                      order=order)
+    assert (r["retcode"] == RET_SUCCESS).all()
+
+
+def test_pendulum_reference_config(problems):
+    # benchmark/simple_pendulum.jl:5-32 with dt = 0.05 (the reference test only checks that
+    # it runs); cross-checked against scipy's independent collocation solver.
+    scipy_integrate = pytest.importorskip("scipy.integrate")
+    p = problems.PENDULUM
+    o, r, N = _solve1(p, dt=0.05, params=(9.81, 0.0, 0.0), order=4)
+    assert r["retcode"][0] == RET_SUCCESS
+    mesh, y = r["mesh"][0, :N], r["y"][0, :N]
+    u_mid = o.interpolate(4, mesh, r["y"][0], r["K"][0], r["KI"][0], [math.pi / 4])[0]
+    assert abs(u_mid[0] + math.pi / 2) < 1e-6
+    assert abs(y[-1, 0] - math.pi / 2) < 1e-6
+
+    # scipy solve_bvp on the same problem: interior condition handled by splitting at pi/4
+    def fun(t, u):
+        return np.vstack([u[1], -9.81 * np.sin(u[0])])
+
+    # solve on [pi/4, pi/2] and [0, pi/4] as a two-piece problem with continuity
+    def fun2(t, w):
+        # w = (u on [0,pi/4] mapped to s in [0,1], u on [pi/4,pi/2] mapped to s in [0,1])
+        h = math.pi / 4
+        return np.vstack([h * w[1], -h * 9.81 * np.sin(w[0]), h * w[3], -h * 9.81 * np.sin(w[2])])
+
+    def bc2(wa, wb):
+        return np.array([wb[0] + math.pi / 2, wa[2] + math.pi / 2, wb[2] - math.pi / 2,
+                         wb[1] - wa[3]])
+
+    s = np.linspace(0, 1, 50)
+    w0 = np.zeros((4, s.size))
+    w0[0] = np.interp(s * math.pi / 4, mesh, y[:, 0]); w0[1] = np.interp(s * math.pi / 4, mesh, y[:, 1])
+    w0[2] = np.interp(math.pi / 4 + s * math.pi / 4, mesh, y[:, 0])
+    w0[3] = np.interp(math.pi / 4 + s * math.pi / 4, mesh, y[:, 1])
+    sol = scipy_integrate.solve_bvp(fun2, bc2, s, w0, tol=1e-8, max_nodes=100000)
+    assert sol.success
+    assert abs(sol.sol(0.0)[0] - y[0, 0]) < 1e-4
+    assert abs(sol.sol(0.0)[1] - y[0, 1]) < 1e-4
