@@ -1,2 +1,9 @@
-"""GB300-native batched MIRK boundary-value solver (host side)."""
+"""GB300-native batched MIRK boundary-value solver (host side).
+
+The compute path is libbvpgpu.so (include/bvpgpu.h): JIT-compiled sm_103a kernels for the
+MIRK collocation residual, the forward-mode Jacobian blocks, the structured block
+factorisation and the defect estimate, driven per instance by a persistent kernel.
+"""
 from . import problems  # noqa: F401
+from ._lib import build_library, load_library, LIB_PATH, EXPORTS  # noqa: F401
+from .solver import BatchSolver, BatchResult, BVPError, RET_SUCCESS, RET_FAILURE, RET_MAXITERS  # noqa: F401

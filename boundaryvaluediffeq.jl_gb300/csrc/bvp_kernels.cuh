@@ -1,0 +1,1367 @@
+// Batched adaptive MIRK solve on sm_103a: device code.
+//
+// NVRTC compiles this file once per (problem source, M, method, Jacobian precision)
+// after bvp_prelude.cuh and the user's problem source. Compile-time configuration:
+//   BVP_M          state dimension                 BVP_ORDER    MIRK order (2..6)
+//   BVP_TWOPOINT   1 for two-point BCs (bca, bcb)  BVP_NBC      BC evaluation points
+//   BVP_JT         Jacobian / factorisation scalar (float by default)
+//
+// One warp owns one BVP instance for its whole adaptive solve; a persistent grid of
+// warps pulls instances from an atomic work counter (largest meshes first). The warp's
+// lanes stride over mesh intervals for the per-interval work (residual, Jacobian blocks,
+// defect) and over block pairs for the cyclic-reduction factorisation.
+//
+// Reference functions restated here (paths relative to the reference project):
+//   Φ residual             lib/BoundaryValueDiffEqMIRK/src/collocation.jl:44-72
+//   residual layout        lib/BoundaryValueDiffEqMIRK/src/mirk.jl:471-534
+//   EvalSol BC access      lib/BoundaryValueDiffEqMIRK/src/interpolation.jl:214-242
+//   extra stages           lib/BoundaryValueDiffEqMIRK/src/interpolation.jl:337-372
+//   Jacobian blocks        lib/BoundaryValueDiffEqMIRK/src/mirk.jl:697-838 (exact block pattern)
+//   Newton driver          lib/BoundaryValueDiffEqCore/src/default_internal_solve.jl:31-45
+//   defect                 lib/BoundaryValueDiffEqMIRK/src/adaptivity.jl:416-461
+//   mesh selection         lib/BoundaryValueDiffEqMIRK/src/adaptivity.jl:23-75, 250-304
+//   solution transfer      lib/BoundaryValueDiffEqMIRK/src/adaptivity.jl:6-13 (mirk.jl:361-373)
+//   outer loop             lib/BoundaryValueDiffEqMIRK/src/mirk.jl:286-388
+#pragma once
+
+#ifndef BVP_JT
+#define BVP_JT float
+#endif
+#define BVP_JT_PTR BVP_JT
+#include "bvp_shared.h"
+#ifndef BVP_TWOPOINT
+#define BVP_TWOPOINT 0
+#endif
+#ifndef BVP_NBC
+#define BVP_NBC 2
+#endif
+#ifndef BVP_LA
+#define BVP_LA 0
+#endif
+
+#if BVP_TWOPOINT
+template <class T, class P> BVP_DEV void bvp_bc(T*, const T* const*, const P*) {}
+#else
+template <class T, class P> BVP_DEV void bvp_bca(T*, const T*, const P*) {}
+template <class T, class P> BVP_DEV void bvp_bcb(T*, const T*, const P*) {}
+#endif
+
+namespace bvp {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int M = BVP_M;
+constexpr int ORD = BVP_ORDER;
+constexpr int S = ORD - 1;
+constexpr int SS = (ORD == 2 || ORD == 3) ? 3 : (ORD == 4 ? 4 : (ORD == 5 ? 6 : 9));
+constexpr int NSX = SS - S;           // extra interpolant stages
+constexpr int NSXA = NSX > 0 ? NSX : 1;
+constexpr int D = 2 * M;              // tangent directions of one interval
+constexpr int NBC = BVP_NBC;
+constexpr int TWOPOINT = BVP_TWOPOINT;
+constexpr int LA = BVP_LA;
+using JT = BVP_JT;
+constexpr int EQW = 2 * M * M + M;    // reduced equation: A (MxM), B (MxM), g (M)
+constexpr int RECW = 3 * M * M + M;   // elimination record: U, X, Y (MxM), g (M)
+constexpr int NBCB = TWOPOINT ? 2 : 2 * NBC;   // BC Jacobian blocks (node, MxM)
+constexpr int KMAX = 2 + NBCB;                 // kept (separator) nodes
+constexpr int NDENSE = KMAX * M;
+
+enum : int { RET_SUCCESS = 0, RET_FAILURE = 1, RET_MAXITERS = 2 };
+
+// ---- MIRK tableaus (mirk_tableaus.jl:13-152), folded at compile time ------------------
+BVP_DEV constexpr double tab_c(int r) {
+    if (ORD == 2) return 0.5;
+    if (ORD == 3) return r == 0 ? 0.0 : 2.0 / 3.0;
+    if (ORD == 4) return r == 0 ? 0.0 : (r == 1 ? 1.0 : 0.5);
+    if (ORD == 5) return r == 0 ? 0.0 : (r == 1 ? 1.0 : (r == 2 ? 0.75 : 0.3));
+    return r == 0 ? 0.0 : (r == 1 ? 1.0 : (r == 2 ? 0.25 : (r == 3 ? 0.75 : 0.5)));
+}
+BVP_DEV constexpr double tab_v(int r) {
+    if (ORD == 2) return 0.5;
+    if (ORD == 3) return r == 0 ? 0.0 : 4.0 / 9.0;
+    if (ORD == 4) return r == 0 ? 0.0 : (r == 1 ? 1.0 : 0.5);
+    if (ORD == 5) return r == 0 ? 0.0 : (r == 1 ? 1.0 : (r == 2 ? 27.0 / 32.0 : 837.0 / 1250.0));
+    return r == 0 ? 0.0 : (r == 1 ? 1.0 : (r == 2 ? 5.0 / 32.0 : (r == 3 ? 27.0 / 32.0 : 0.5)));
+}
+BVP_DEV constexpr double tab_b(int r) {
+    if (ORD == 2) return 1.0;
+    if (ORD == 3) return r == 0 ? 0.25 : 0.75;
+    if (ORD == 4) return r == 2 ? 2.0 / 3.0 : 1.0 / 6.0;
+    if (ORD == 5) return r == 0 ? 5.0 / 54.0 : (r == 1 ? 1.0 / 14.0 : (r == 2 ? 32.0 / 81.0 : 250.0 / 567.0));
+    return r <= 1 ? 7.0 / 90.0 : (r <= 3 ? 16.0 / 45.0 : 2.0 / 15.0);
+}
+BVP_DEV constexpr double tab_x(int r, int j) {
+    if (ORD == 3) return (r == 1 && j == 0) ? 2.0 / 9.0 : 0.0;
+    if (ORD == 4) return r == 2 ? (j == 0 ? 0.125 : (j == 1 ? -0.125 : 0.0)) : 0.0;
+    if (ORD == 5) {
+        if (r == 2) return j == 0 ? 3.0 / 64.0 : (j == 1 ? -9.0 / 64.0 : 0.0);
+        if (r == 3) return j == 0 ? 21.0 / 1000.0 : (j == 1 ? 63.0 / 5000.0 : (j == 2 ? -252.0 / 625.0 : 0.0));
+        return 0.0;
+    }
+    if (ORD == 6) {
+        if (r == 2) return j == 0 ? 9.0 / 64.0 : (j == 1 ? -3.0 / 64.0 : 0.0);
+        if (r == 3) return j == 0 ? 3.0 / 64.0 : (j == 1 ? -9.0 / 64.0 : 0.0);
+        if (r == 4) return j == 0 ? -5.0 / 24.0 : (j == 1 ? 5.0 / 24.0 : (j == 2 ? 2.0 / 3.0 : (j == 3 ? -2.0 / 3.0 : 0.0)));
+        return 0.0;
+    }
+    return 0.0;
+}
+BVP_DEV constexpr double tab_cs(int r) {
+    if (ORD == 2) return r == 0 ? 0.0 : 1.0;
+    if (ORD == 3) return 1.0;
+    if (ORD == 4) return 0.75;
+    if (ORD == 5) return r == 0 ? 0.8 : 13.0 / 23.0;
+    return r == 0 ? 7.0 / 16.0 : (r == 1 ? 3.0 / 8.0 : (r == 2 ? 9.0 / 16.0 : 1.0 / 8.0));
+}
+BVP_DEV constexpr double tab_vs(int r) {
+    if (ORD == 4) return 27.0 / 32.0;
+    return tab_cs(r);
+}
+// x_star[extra r][stage j] (column-major indexing of the reference, interpolation.jl:308-309)
+BVP_DEV constexpr double tab_xs(int r, int j) {
+    if (ORD == 4) return j == 0 ? 3.0 / 64.0 : (j == 1 ? -9.0 / 64.0 : 0.0);
+    if (ORD == 5) {
+        if (r == 0) return j == 0 ? 14.0 / 1125.0 : (j == 1 ? -74.0 / 875.0 : (j == 2 ? -128.0 / 3375.0 : (j == 3 ? 104.0 / 945.0 : 0.0)));
+        return j == 0 ? 0.5 : (j == 1 ? 4508233.0 / 1958887.0 : (j == 2 ? 48720832.0 / 2518569.0 :
+               (j == 3 ? -27646420.0 / 17629983.0 : (j == 4 ? -11517095.0 / 559682.0 : 0.0))));
+    }
+    if (ORD == 6) {
+        if (r == 0) return j == 0 ? 1547.0 / 32768.0 : (j == 1 ? -1225.0 / 32768.0 : (j == 2 ? 749.0 / 4096.0 : (j == 3 ? -287.0 / 2048.0 : (j == 4 ? -861.0 / 16384.0 : 0.0))));
+        if (r == 1) return j == 0 ? 83.0 / 1536.0 : (j == 1 ? -13.0 / 384.0 : (j == 2 ? 283.0 / 1536.0 : (j == 3 ? -167.0 / 1536.0 : (j == 4 ? -49.0 / 512.0 : 0.0))));
+        if (r == 2) return j == 0 ? 1225.0 / 32768.0 : (j == 1 ? -1547.0 / 32768.0 : (j == 2 ? 287.0 / 2048.0 : (j == 3 ? -749.0 / 4096.0 : (j == 4 ? 861.0 / 16384.0 : 0.0))));
+        return j == 0 ? 233.0 / 3456.0 : (j == 1 ? -19.0 / 1152.0 : (j == 5 ? -5.0 / 72.0 : (j == 6 ? 7.0 / 72.0 : (j == 7 ? -17.0 / 216.0 : 0.0))));
+    }
+    return 0.0;
+}
+BVP_DEV constexpr double tau_star() {
+    return ORD == 2 ? 0.25 : (ORD == 3 ? 0.25 : (ORD == 4 ? 0.226 : (ORD == 5 ? 0.3 : 0.7156)));
+}
+
+// continuous-extension weights and derivatives (interpolation.jl:459-580)
+BVP_DEV void interp_weights(double t, double* w, double* wp) {
+    const double t2 = t * t, t3 = t2 * t, t4 = t3 * t, t5 = t4 * t, t6 = t5 * t;
+    if (ORD == 2) {
+        w[0] = 0; w[1] = t * (1 - t / 2); w[2] = t2 / 2;
+        wp[0] = 0; wp[1] = 1 - t; wp[2] = t;
+    } else if (ORD == 3) {
+        w[0] = t / 4.0 * (2.0 * t2 - 5.0 * t + 4.0);
+        w[1] = -3.0 / 4.0 * t2 * (2.0 * t - 3.0);
+        w[2] = t2 * (t - 1.0);
+        wp[0] = 3.0 / 2.0 * (t - 2.0 / 3.0) * (t - 1.0);
+        wp[1] = -9.0 / 2.0 * t * (t - 1.0);
+        wp[2] = 3.0 * t * (t - 2.0 / 3.0);
+    } else if (ORD == 4) {
+        const double tm1 = t - 1.0, t4m3 = t * 4.0 - 3.0, t2m1 = t * 2.0 - 1.0;
+        w[0] = -t * (2.0 * t - 3.0) * (2.0 * t2 - 3.0 * t + 2.0) / 6.0;
+        w[1] = t2 * (12.0 * t2 - 20.0 * t + 9.0) / 6.0;
+        w[2] = 2.0 * t2 * (6.0 * t2 - 14.0 * t + 9.0) / 3.0;
+        w[3] = -16.0 * t2 * tm1 * tm1 / 3.0;
+        wp[0] = -tm1 * t4m3 * t2m1 / 3.0;
+        wp[1] = t * t2m1 * t4m3;
+        wp[2] = 4.0 * t * t4m3 * tm1;
+        wp[3] = -32.0 * t * t2m1 * tm1 / 3.0;
+    } else if (ORD == 5) {
+        w[0] = t * (22464.0 - 83910.0 * t + 143041.0 * t2 - 113808.0 * t3 + 33256.0 * t4) / 22464.0;
+        w[1] = t2 * (-2418.0 + 12303.0 * t - 19512.0 * t2 + 10904.0 * t3) / 3360.0;
+        w[2] = -8.0 / 81.0 * t2 * (-78.0 + 209.0 * t - 204.0 * t2 + 8.0 * t3);
+        w[3] = -25.0 / 1134.0 * t2 * (-390.0 + 1045.0 * t - 1020.0 * t2 + 328.0 * t3);
+        w[4] = -25.0 / 5184.0 * t2 * (390.0 + 255.0 * t - 1680.0 * t2 + 2072.0 * t3);
+        w[5] = 279841.0 / 168480.0 * t2 * (-6.0 + 21.0 * t - 24.0 * t2 + 8.0 * t3);
+        wp[0] = 1.0 - 13985.0 / 1872.0 * t + 143041.0 / 7488.0 * t2 - 2371.0 / 117.0 * t3 + 20785.0 / 2808.0 * t4;
+        wp[1] = -403.0 / 280.0 * t + 12303.0 / 1120.0 * t2 - 813.0 / 35.0 * t3 + 1363.0 / 84.0 * t4;
+        wp[2] = 416.0 / 27.0 * t - 1672.0 / 27.0 * t2 + 2176.0 / 27.0 * t3 - 320.0 / 81.0 * t4;
+        wp[3] = 3250.0 / 189.0 * t - 26125.0 / 378.0 * t2 + 17000.0 / 189.0 * t3 - 20500.0 / 567.0 * t4;
+        wp[4] = -1625.0 / 432.0 * t - 2125.0 / 576.0 * t2 + 875.0 / 27.0 * t3 - 32375.0 / 648.0 * t4;
+        wp[5] = -279841.0 / 14040.0 * t + 1958887.0 / 18720.0 * t2 - 279841.0 / 1755.0 * t3 + 279841.0 / 4212.0 * t4;
+    } else {
+        w[0] = t - 28607.0 / 7434.0 * t2 - 166210.0 / 33453.0 * t3 + 334780.0 / 11151.0 * t4 -
+               1911296.0 / 55755.0 * t5 + 406528.0 / 33453.0 * t6;
+        w[1] = 777.0 / 590.0 * t2 - 2534158.0 / 234171.0 * t3 + 2088580.0 / 78057.0 * t4 -
+               10479104.0 / 390285.0 * t5 + 11328512.0 / 1170855.0 * t6;
+        w[2] = -1008.0 / 59.0 * t2 + 222176.0 / 1593.0 * t3 - 180032.0 / 531.0 * t4 +
+               876544.0 / 2655.0 * t5 - 180224.0 / 1593.0 * t6;
+        w[3] = w[2];
+        w[4] = -378.0 / 59.0 * t2 + 27772.0 / 531.0 * t3 - 22504.0 / 177.0 * t4 +
+               109568.0 / 885.0 * t5 - 22528.0 / 531.0 * t6;
+        w[5] = -95232.0 / 413.0 * t2 + 62384128.0 / 33453.0 * t3 - 49429504.0 / 11151.0 * t4 +
+               46759936.0 / 11151.0 * t5 - 46661632.0 / 33453.0 * t6;
+        w[6] = 896.0 / 5.0 * t2 - 4352.0 / 3.0 * t3 + 3456.0 * t4 - 16384.0 / 5.0 * t5 + 16384.0 / 15.0 * t6;
+        w[7] = 50176.0 / 531.0 * t2 - 179554304.0 / 234171.0 * t3 + 143363072.0 / 78057.0 * t4 -
+               136675328.0 / 78057.0 * t5 + 137363456.0 / 234171.0 * t6;
+        w[8] = 16384.0 / 441.0 * t3 - 16384.0 / 147.0 * t4 + 16384.0 / 147.0 * t5 - 16384.0 / 441.0 * t6;
+        wp[0] = 1 - 28607.0 / 3717.0 * t - 166210.0 / 11151.0 * t2 + 1339120.0 / 11151.0 * t3 -
+                1911296.0 / 11151.0 * t4 + 813056.0 / 11151.0 * t5;
+        wp[1] = 777.0 / 295.0 * t - 2534158.0 / 78057.0 * t2 + 8354320.0 / 78057.0 * t3 -
+                10479104.0 / 78057.0 * t4 + 22657024.0 / 390285.0 * t5;
+        wp[2] = -2016.0 / 59.0 * t + 222176.0 / 531.0 * t2 - 720128.0 / 531.0 * t3 +
+                876544.0 / 531.0 * t4 - 360448.0 / 531.0 * t5;
+        wp[3] = wp[2];
+        wp[4] = -756.0 / 59.0 * t + 27772.0 / 177.0 * t2 - 90016.0 / 177.0 * t3 +
+                109568.0 / 177.0 * t4 - 45056.0 / 177.0 * t5;
+        wp[5] = -190464.0 / 413.0 * t + 62384128.0 / 11151.0 * t2 - 197718016.0 / 11151.0 * t3 +
+                233799680.0 / 11151.0 * t4 - 93323264.0 / 11151.0 * t5;
+        wp[6] = 1792.0 / 5.0 * t - 4352.0 * t2 + 13824.0 * t3 - 16384.0 * t4 + 32768.0 / 5.0 * t5;
+        wp[7] = 100352.0 / 531.0 * t - 179554304.0 / 78057.0 * t2 + 573452288.0 / 78057.0 * t3 -
+                683376640.0 / 78057.0 * t4 + 274726912.0 / 78057.0 * t5;
+        wp[8] = 16384.0 / 147.0 * t2 - 65536.0 / 147.0 * t3 + 81920.0 / 147.0 * t4 - 32768.0 / 147.0 * t5;
+    }
+}
+
+// ---- launch arguments (shared with the host runtime) ------------------------------------
+using InstState = BvpInstState;
+using Args = BvpArgs;
+
+// per-instance scratch layout (doubles), the same formulas as bvp_make_layout()
+constexpr int SCR_BCRES = 0;                         // M
+constexpr int SCR_BCBLK = SCR_BCRES + M;             // NBCB x M x M
+constexpr int SCR_SEG = SCR_BCBLK + NBCB * M * M;    // (KMAX-1) x EQW
+constexpr int SCR_DENSE = SCR_SEG + (KMAX - 1) * EQW;  // NDENSE x NDENSE
+constexpr int SCR_RHS = SCR_DENSE + NDENSE * NDENSE;   // NDENSE
+constexpr int SCRW = SCR_RHS + NDENSE;
+// int scratch
+constexpr int ISCR_NK = 0;                 // kept count
+constexpr int ISCR_KEPT = 1;               // KMAX kept nodes
+constexpr int ISCR_NB = ISCR_KEPT + KMAX;  // number of BC blocks
+constexpr int ISCR_BNODE = ISCR_NB + 1;    // NBCB block nodes
+constexpr int ISCRW = ISCR_BNODE + NBCB;
+
+
+// ---- warp helpers ------------------------------------------------------------------------
+BVP_DEV int lane_id() { return threadIdx.x & 31; }
+BVP_DEV double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+BVP_DEV double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+BVP_DEV bool warp_any(bool b) { return __any_sync(FULL, b) != 0; }
+
+// lower_bound(mesh, t) - 1 clamped to [0, N-2]: the reference's interval()
+// (lib/BoundaryValueDiffEqCore/src/utils.jl:119-121)
+BVP_DEV int interval_of(const double* mesh, int N, double t) {
+    int lo = 0, hi = N;  // first index with mesh[idx] >= t
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (mesh[mid] < t) lo = mid + 1; else hi = mid;
+    }
+    int ii = lo - 1;
+    ii = ii < 0 ? 0 : ii;
+    ii = ii > N - 2 ? N - 2 : ii;
+    return ii;
+}
+
+// ---- per-instance view -----------------------------------------------------------------
+struct Inst {
+    int q, cap, N, cur;
+    long long nb;          // node offset
+    const double* p;
+    const JT* pj;
+    double* scr;
+    int* iscr;
+};
+
+BVP_DEV double* mesh_of(const Args& a, const Inst& I, int b) { return a.mesh + b * a.tot + I.nb; }
+BVP_DEV double* h_of(const Args& a, const Inst& I, int b) { return a.h + b * a.tot + I.nb; }
+BVP_DEV double* y_of(const Args& a, const Inst& I, int b) { return a.y + (b * a.tot + I.nb) * M; }
+
+// ---- Φ for one interval (collocation.jl:44-72) ------------------------------------------
+template <class T, class PT>
+BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, double ti, double hi_d) {
+    const PT hi = PT(hi_d);
+    T Y[M];
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) Y[m] = PT(1.0 - tab_v(r)) * yi[m] + PT(tab_v(r)) * yi1[m];
+#pragma unroll
+        for (int j = 0; j < r; ++j) {
+            if (tab_x(r, j) != 0.0) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) Y[m] = Y[m] + hi * (Ki[j * M + m] * PT(tab_x(r, j)));
+            }
+        }
+        bvp_f<T, PT>(&Ki[r * M], Y, p, PT(ti + tab_c(r) * hi_d));
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        T acc = Ki[m] * PT(tab_b(0));
+#pragma unroll
+        for (int r = 1; r < S; ++r) acc = acc + Ki[r * M + m] * PT(tab_b(r));
+        ri[m] = (yi1[m] - yi[m]) - hi * acc;
+    }
+}
+
+// extra interpolant stages of one interval (interpolation.jl:337-372)
+template <class T, class PT>
+BVP_DEV void interp_stages(const T* yi, const T* yi1, const T* Ki, T* KIi, const PT* p, double ti, double hi_d) {
+    const PT hi = PT(hi_d);
+    T Y[M];
+#pragma unroll
+    for (int r = 0; r < NSX; ++r) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            T acc = Ki[m] * PT(tab_xs(r, 0));
+#pragma unroll
+            for (int j = 1; j < S; ++j) acc = acc + Ki[j * M + m] * PT(tab_xs(r, j));
+#pragma unroll
+            for (int qq = 0; qq < r; ++qq) acc = acc + KIi[qq * M + m] * PT(tab_xs(r, S + qq));
+            Y[m] = acc * hi + PT(1.0 - tab_vs(r)) * yi[m] + PT(tab_vs(r)) * yi1[m];
+        }
+        bvp_f<T, PT>(&KIi[r * M], Y, p, PT(ti + tab_cs(r) * hi_d));
+    }
+}
+
+// z = y_i + h (Σ w_r K_r + Σ w_{s+q} KI_q)
+template <class T>
+BVP_DEV void sum_stages(const double* w, const T* yi, const T* Ki, const T* KIi, double hi, T* z) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        T acc = Ki[m] * w[0];
+#pragma unroll
+        for (int r = 1; r < S; ++r) acc = acc + Ki[r * M + m] * w[r];
+#pragma unroll
+        for (int qq = 0; qq < NSX; ++qq) acc = acc + KIi[qq * M + m] * w[S + qq];
+        z[m] = acc * hi + yi[m];
+    }
+}
+
+// EvalSol u(t) of the current iterate (interpolation.jl:214-242); lane-local.
+// Returns the node the reference attributes the BC Jacobian to; *interior set for
+// points strictly inside the mesh.
+BVP_DEV int eval_sol(const Args& a, const Inst& I, double t, double* z, bool* interior) {
+    const double* mesh = mesh_of(a, I, I.cur);
+    const double* h = h_of(a, I, I.cur);
+    const double* y = y_of(a, I, I.cur);
+    const int N = I.N;
+    if (t == mesh[0]) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) z[m] = y[m];
+        *interior = false; return 0;
+    }
+    if (t == mesh[N - 1]) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) z[m] = y[(N - 1) * M + m];
+        *interior = false; return N - 1;
+    }
+    const int ii = interval_of(mesh, N, t);
+    const double tau = (t - mesh[ii]) / h[ii];
+    double w[SS], wp[SS];
+    interp_weights(tau, w, wp);
+    double yi[M], yi1[M], Ki[S * M], KIi[NSXA * M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) { yi[m] = y[ii * M + m]; yi1[m] = y[(ii + 1) * M + m]; }
+    const double* Kg = a.K + (I.nb + ii) * (S * M);
+#pragma unroll
+    for (int k = 0; k < S * M; ++k) Ki[k] = Kg[k];
+    interp_stages<double, double>(yi, yi1, Ki, KIi, I.p, mesh[ii], h[ii]);
+    sum_stages<double>(w, yi, Ki, KIi, h[ii], z);
+    *interior = true;
+    return ii;
+}
+
+// ---- K1: residual and stages (warp). Returns ||F||_inf (+inf if non-finite). -----------
+BVP_DEV double residual(const Args& a, const Inst& I) {
+    const int lane = lane_id();
+    const double* mesh = mesh_of(a, I, I.cur);
+    const double* h = h_of(a, I, I.cur);
+    const double* y = y_of(a, I, I.cur);
+    double mx = 0.0;
+    bool bad = false;
+    for (int i = lane; i < I.N - 1; i += 32) {
+        double yi[M], yi1[M], Ki[S * M], ri[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) { yi[m] = y[i * M + m]; yi1[m] = y[(i + 1) * M + m]; }
+        phi_interval<double, double>(yi, yi1, Ki, ri, I.p, mesh[i], h[i]);
+        double* Kg = a.K + (I.nb + i) * (S * M);
+#pragma unroll
+        for (int k = 0; k < S * M; ++k) Kg[k] = Ki[k];
+        double* Fg = a.F + (I.nb + i) * M;
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            Fg[m] = ri[m];
+            bad |= !isfinite(ri[m]);
+            mx = fmax(mx, fabs(ri[m]));
+        }
+    }
+    __syncwarp();
+    if (lane == 0) {
+        double res[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) res[m] = 0.0;
+        if (TWOPOINT) {
+            double ra[M], rb[M];
+            bvp_bca<double, double>(ra, y, I.p);
+            bvp_bcb<double, double>(rb, y + (I.N - 1) * M, I.p);
+            for (int k = 0; k < LA; ++k) res[k] = ra[k];
+            for (int k = LA; k < M; ++k) res[k] = rb[k - LA];
+        } else {
+            double ua[NBC * M];
+            const double* ptrs[NBC];
+#pragma unroll
+            for (int k = 0; k < NBC; ++k) {
+                bool in;
+                eval_sol(a, I, a.bc_t[k], &ua[k * M], &in);
+                ptrs[k] = &ua[k * M];
+            }
+            bvp_bc<double, double>(res, ptrs, I.p);
+        }
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            I.scr[SCR_BCRES + m] = res[m];
+            bad |= !isfinite(res[m]);
+            mx = fmax(mx, fabs(res[m]));
+        }
+    }
+    __syncwarp();
+    mx = warp_max(mx);
+    bad = warp_any(bad);
+    return bad ? __longlong_as_double(0x7ff0000000000000LL) : mx;
+}
+
+// Σ F² over the full residual (for the line search)
+BVP_DEV double residual_sq(const Args& a, const Inst& I) {
+    const int lane = lane_id();
+    double s = 0.0;
+    for (int i = lane; i < I.N - 1; i += 32) {
+        const double* Fg = a.F + (I.nb + i) * M;
+#pragma unroll
+        for (int m = 0; m < M; ++m) s += Fg[m] * Fg[m];
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) s += I.scr[SCR_BCRES + m] * I.scr[SCR_BCRES + m];
+    }
+    return warp_sum(s);
+}
+
+// ---- K2: Jacobian blocks (warp) ------------------------------------------------------------
+// S_i = ∂r_i/∂y_i and R_i = ∂r_i/∂y_{i+1} by forward mode with 2M tangents in JT.
+BVP_DEV void add_bc_block(const Inst& I, int node, const double* G) {
+    int nb = I.iscr[ISCR_NB];
+    for (int k = 0; k < nb; ++k)
+        if (I.iscr[ISCR_BNODE + k] == node) {
+            for (int q = 0; q < M * M; ++q) I.scr[SCR_BCBLK + k * M * M + q] += G[q];
+            return;
+        }
+    I.iscr[ISCR_BNODE + nb] = node;
+    for (int q = 0; q < M * M; ++q) I.scr[SCR_BCBLK + nb * M * M + q] = G[q];
+    I.iscr[ISCR_NB] = nb + 1;
+}
+
+BVP_DEV void jacobian(const Args& a, const Inst& I) {
+    using DI = Dual<JT, D>;
+    using DU = Dual<JT, M>;
+    const int lane = lane_id();
+    const double* mesh = mesh_of(a, I, I.cur);
+    const double* h = h_of(a, I, I.cur);
+    const double* y = y_of(a, I, I.cur);
+    for (int i = lane; i < I.N - 1; i += 32) {
+        DI yi[M], yi1[M], Ki[S * M], ri[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            yi[m] = DI(JT(y[i * M + m])); yi[m].d[m] = JT(1);
+            yi1[m] = DI(JT(y[(i + 1) * M + m])); yi1[m].d[M + m] = JT(1);
+        }
+        phi_interval<DI, JT>(yi, yi1, Ki, ri, I.pj, mesh[i], h[i]);
+        JT* Sg = a.Sb + (I.nb + i) * (M * M);
+        JT* Rg = a.Rb + (I.nb + i) * (M * M);
+#pragma unroll
+        for (int r = 0; r < M; ++r)
+#pragma unroll
+            for (int c = 0; c < M; ++c) {
+                Sg[r * M + c] = ri[r].d[c];
+                Rg[r * M + c] = ri[r].d[M + c];
+            }
+    }
+    if (lane == 0) {
+        I.iscr[ISCR_NB] = 0;
+        double G[M * M];
+        if (TWOPOINT) {
+            DU ua[M], ra[M];
+            for (int m = 0; m < M; ++m) { ua[m] = DU(JT(y[m])); ua[m].d[m] = JT(1); }
+            bvp_bca<DU, JT>(ra, ua, I.pj);
+            for (int q = 0; q < M * M; ++q) G[q] = 0.0;
+            for (int r = 0; r < LA; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(ra[r].d[c]);
+            add_bc_block(I, 0, G);
+            for (int m = 0; m < M; ++m) { ua[m] = DU(JT(y[(I.N - 1) * M + m])); ua[m].d[m] = JT(1); }
+            bvp_bcb<DU, JT>(ra, ua, I.pj);
+            for (int q = 0; q < M * M; ++q) G[q] = 0.0;
+            for (int r = LA; r < M; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(ra[r - LA].d[c]);
+            add_bc_block(I, I.N - 1, G);
+        } else {
+            double uav[NBC * M];
+            int node[NBC];
+            bool inter[NBC];
+            for (int k = 0; k < NBC; ++k) {
+                bool in;
+                node[k] = eval_sol(a, I, a.bc_t[k], &uav[k * M], &in);
+                inter[k] = in;
+            }
+            for (int k = 0; k < NBC; ++k) {
+                DU ua[NBC * M];
+                const DU* ptrs[NBC];
+                for (int qq = 0; qq < NBC; ++qq) {
+                    for (int m = 0; m < M; ++m) {
+                        ua[qq * M + m] = DU(JT(uav[qq * M + m]));
+                        if (qq == k) ua[qq * M + m].d[m] = JT(1);
+                    }
+                    ptrs[qq] = &ua[qq * M];
+                }
+                DU res[M];
+                bvp_bc<DU, JT>(res, ptrs, I.pj);
+                for (int r = 0; r < M; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(res[r].d[c]);
+                if (!inter[k] || !a.bc_jac_exact) {
+                    // the interpolant's stages are held at their primal values: du(t)/dy = I
+                    // on the interval's left node (interpolation.jl:214-242, mirk.jl:565-572)
+                    add_bc_block(I, node[k], G);
+                } else {
+                    // exact: chain through the interval's stages and extra stages
+                    const int ii = node[k];
+                    const double tau = (a.bc_t[k] - mesh[ii]) / h[ii];
+                    double w[SS], wp[SS];
+                    interp_weights(tau, w, wp);
+                    DI yi[M], yi1[M], Ki[S * M], KIi[NSXA * M], ri[M], z[M];
+                    for (int m = 0; m < M; ++m) {
+                        yi[m] = DI(JT(y[ii * M + m])); yi[m].d[m] = JT(1);
+                        yi1[m] = DI(JT(y[(ii + 1) * M + m])); yi1[m].d[M + m] = JT(1);
+                    }
+                    phi_interval<DI, JT>(yi, yi1, Ki, ri, I.pj, mesh[ii], h[ii]);
+                    interp_stages<DI, JT>(yi, yi1, Ki, KIi, I.pj, mesh[ii], h[ii]);
+                    sum_stages<DI>(w, yi, Ki, KIi, h[ii], z);
+                    double JL[M * M], JR[M * M];
+                    for (int r = 0; r < M; ++r)
+                        for (int c = 0; c < M; ++c) {
+                            double sl = 0.0, sr = 0.0;
+                            for (int qq = 0; qq < M; ++qq) {
+                                sl += G[r * M + qq] * double(z[qq].d[c]);
+                                sr += G[r * M + qq] * double(z[qq].d[M + c]);
+                            }
+                            JL[r * M + c] = sl; JR[r * M + c] = sr;
+                        }
+                    add_bc_block(I, ii, JL);
+                    add_bc_block(I, ii + 1, JR);
+                }
+            }
+        }
+        // kept (separator) nodes: 0, N-1 and every node a BC row touches
+        int kept[KMAX];
+        int nk = 0;
+        kept[nk++] = 0;
+        kept[nk++] = I.N - 1;
+        const int nb = I.iscr[ISCR_NB];
+        for (int k = 0; k < nb; ++k) kept[nk++] = I.iscr[ISCR_BNODE + k];
+        // insertion sort + unique
+        for (int u = 1; u < nk; ++u) {
+            const int v = kept[u];
+            int w2 = u - 1;
+            while (w2 >= 0 && kept[w2] > v) { kept[w2 + 1] = kept[w2]; --w2; }
+            kept[w2 + 1] = v;
+        }
+        int nu = 0;
+        for (int u = 0; u < nk; ++u)
+            if (nu == 0 || kept[u] != kept[nu - 1]) kept[nu++] = kept[u];
+        I.iscr[ISCR_NK] = nu;
+        for (int u = 0; u < nu; ++u) I.iscr[ISCR_KEPT + u] = kept[u];
+    }
+    __syncwarp();
+}
+
+// ---- K3: structured factorisation + solve (warp) -----------------------------------------
+// Block cyclic reduction with partial pivoting over each segment between separator
+// nodes: pairs of neighbouring block rows eliminate their shared node (Gaussian
+// elimination with row pivoting on that node's 2M x M column block), halving the
+// segment at each level. The separator system is solved densely in FP64 and the
+// eliminated nodes are recovered level by level.
+BVP_DEV void load_eq0(const Args& a, const Inst& I, int i, JT* A, JT* B, JT* g) {
+    const JT* Sg = a.Sb + (I.nb + i) * (M * M);
+    const JT* Rg = a.Rb + (I.nb + i) * (M * M);
+    const double* Fg = a.F + (I.nb + i) * M;
+#pragma unroll
+    for (int q = 0; q < M * M; ++q) { A[q] = Sg[q]; B[q] = Rg[q]; }
+#pragma unroll
+    for (int m = 0; m < M; ++m) g[m] = JT(-Fg[m]);
+}
+BVP_DEV void load_eq(const JT* src, JT* A, JT* B, JT* g) {
+#pragma unroll
+    for (int q = 0; q < M * M; ++q) { A[q] = src[q]; B[q] = src[M * M + q]; }
+#pragma unroll
+    for (int m = 0; m < M; ++m) g[m] = src[2 * M * M + m];
+}
+BVP_DEV void store_eq(JT* dst, const JT* A, const JT* B, const JT* g) {
+#pragma unroll
+    for (int q = 0; q < M * M; ++q) { dst[q] = A[q]; dst[M * M + q] = B[q]; }
+#pragma unroll
+    for (int m = 0; m < M; ++m) dst[2 * M * M + m] = g[m];
+}
+
+// left: Al δ_lo + Bl δ_mid = gl;  right: Ar δ_mid + Br δ_hi = gr.
+// Eliminates δ_mid; writes the pivot rows (U δ_mid + X δ_lo + Y δ_hi = gu) to rec and
+// the reduced equation (An δ_lo + Bn δ_hi = gn). Returns false on a zero pivot.
+BVP_DEV bool eliminate_pair(const JT* Al, const JT* Bl, const JT* gl, const JT* Ar, const JT* Br,
+                            const JT* gr, JT* rec, JT* An, JT* Bn, JT* gn) {
+    constexpr int W = 3 * M + 1;
+    JT Wm[2 * M][W];
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+#pragma unroll
+        for (int c = 0; c < M; ++c) {
+            Wm[r][c] = Bl[r * M + c];     Wm[r][M + c] = Al[r * M + c];     Wm[r][2 * M + c] = JT(0);
+            Wm[M + r][c] = Ar[r * M + c]; Wm[M + r][M + c] = JT(0);         Wm[M + r][2 * M + c] = Br[r * M + c];
+        }
+        Wm[r][3 * M] = gl[r];
+        Wm[M + r][3 * M] = gr[r];
+    }
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+        int piv = k;
+        JT best = fabs(Wm[k][k]);
+#pragma unroll
+        for (int r = k + 1; r < 2 * M; ++r) {
+            const JT v = fabs(Wm[r][k]);
+            if (v > best) { best = v; piv = r; }
+        }
+        ok = ok && (best > JT(0)) && isfinite(best);
+#pragma unroll
+        for (int r = k + 1; r < 2 * M; ++r) {
+            if (r == piv) {
+#pragma unroll
+                for (int c = 0; c < W; ++c) { const JT t = Wm[k][c]; Wm[k][c] = Wm[r][c]; Wm[r][c] = t; }
+            }
+        }
+        const JT inv = JT(1) / Wm[k][k];
+#pragma unroll
+        for (int r = k + 1; r < 2 * M; ++r) {
+            const JT mlt = Wm[r][k] * inv;
+#pragma unroll
+            for (int c = k; c < W; ++c) Wm[r][c] -= mlt * Wm[k][c];
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+#pragma unroll
+        for (int c = 0; c < M; ++c) {
+            rec[r * M + c] = Wm[r][c];
+            rec[M * M + r * M + c] = Wm[r][M + c];
+            rec[2 * M * M + r * M + c] = Wm[r][2 * M + c];
+            An[r * M + c] = Wm[M + r][M + c];
+            Bn[r * M + c] = Wm[M + r][2 * M + c];
+        }
+        rec[3 * M * M + r] = Wm[r][3 * M];
+        gn[r] = Wm[M + r][3 * M];
+    }
+    return ok;
+}
+
+// reduce segment [na, nb]; its final relation A δ_na + B δ_nb = g goes to seg (FP64)
+BVP_DEV bool bcr_segment(const Args& a, const Inst& I, int na, int nbn, double* seg) {
+    const int lane = lane_id();
+    const int m = nbn - na;
+    JT A[M * M], B[M * M], g[M];
+    if (m == 1) {
+        if (lane == 0) {
+            load_eq0(a, I, na, A, B, g);
+            for (int q = 0; q < M * M; ++q) { seg[q] = double(A[q]); seg[M * M + q] = double(B[q]); }
+            for (int r = 0; r < M; ++r) seg[2 * M * M + r] = double(g[r]);
+        }
+        __syncwarp();
+        return true;
+    }
+    bool bad = false;
+    int ml = m, lvl = 0, buf = 0;
+    JT* eqb[2] = {a.eq + I.nb * EQW, a.eq + (a.tot + I.nb) * EQW};
+    while (ml > 1) {
+        const int np = ml >> 1;
+        for (int e = lane; e < np; e += 32) {
+            JT Al[M * M], Bl[M * M], gl[M], Ar[M * M], Br[M * M], gr[M];
+            if (lvl == 0) {
+                load_eq0(a, I, na + 2 * e, Al, Bl, gl);
+                load_eq0(a, I, na + 2 * e + 1, Ar, Br, gr);
+            } else {
+                load_eq(eqb[buf] + (2 * e) * EQW, Al, Bl, gl);
+                load_eq(eqb[buf] + (2 * e + 1) * EQW, Ar, Br, gr);
+            }
+            const int mid = na + ((2 * e + 1) << lvl);
+            JT* rg = a.rec + (I.nb + mid) * RECW;
+            const bool ok = eliminate_pair(Al, Bl, gl, Ar, Br, gr, rg, A, B, g);
+            bad |= !ok;
+            store_eq(eqb[buf ^ 1] + e * EQW, A, B, g);
+        }
+        if ((ml & 1) && lane == (np & 31)) {
+            if (lvl == 0) load_eq0(a, I, na + ml - 1, A, B, g);
+            else load_eq(eqb[buf] + (ml - 1) * EQW, A, B, g);
+            store_eq(eqb[buf ^ 1] + np * EQW, A, B, g);
+        }
+        __syncwarp();
+        buf ^= 1;
+        ml = (ml + 1) >> 1;
+        ++lvl;
+    }
+    if (lane == 0) {
+        load_eq(eqb[buf], A, B, g);
+        for (int q = 0; q < M * M; ++q) { seg[q] = double(A[q]); seg[M * M + q] = double(B[q]); }
+        for (int r = 0; r < M; ++r) seg[2 * M * M + r] = double(g[r]);
+    }
+    __syncwarp();
+    return !warp_any(bad);
+}
+
+BVP_DEV void bcr_backsub(const Args& a, const Inst& I, int na, int nbn) {
+    const int lane = lane_id();
+    const int m = nbn - na;
+    if (m <= 1) return;
+    int L = 0;
+    while ((1 << L) < m) ++L;
+    for (int lvl = L - 1; lvl >= 0; --lvl) {
+        const int ml = (m + (1 << lvl) - 1) >> lvl;
+        const int np = ml >> 1;
+        for (int e = lane; e < np; e += 32) {
+            const int lo = na + ((2 * e) << lvl);
+            const int mid = na + ((2 * e + 1) << lvl);
+            int hi = na + ((2 * e + 2) << lvl);
+            hi = hi > nbn ? nbn : hi;
+            const JT* rg = a.rec + (I.nb + mid) * RECW;
+            const JT* dlo = a.delta + (I.nb + lo) * M;
+            const JT* dhi = a.delta + (I.nb + hi) * M;
+            JT t[M];
+#pragma unroll
+            for (int r = 0; r < M; ++r) {
+                JT s = rg[3 * M * M + r];
+#pragma unroll
+                for (int c = 0; c < M; ++c)
+                    s -= rg[M * M + r * M + c] * dlo[c] + rg[2 * M * M + r * M + c] * dhi[c];
+                t[r] = s;
+            }
+            JT* dm = a.delta + (I.nb + mid) * M;
+#pragma unroll
+            for (int r = M - 1; r >= 0; --r) {
+                JT s = t[r];
+#pragma unroll
+                for (int c = r + 1; c < M; ++c) s -= rg[r * M + c] * t[c];
+                t[r] = s / rg[r * M + r];
+            }
+#pragma unroll
+            for (int r = 0; r < M; ++r) dm[r] = t[r];
+        }
+        __syncwarp();
+    }
+}
+
+// dense Gaussian elimination with partial pivoting (FP64), one lane
+BVP_DEV bool dense_solve(int n, double* A, double* b) {
+    for (int k = 0; k < n; ++k) {
+        int piv = k;
+        double best = fabs(A[k * n + k]);
+        for (int r = k + 1; r < n; ++r) {
+            const double v = fabs(A[r * n + k]);
+            if (v > best) { best = v; piv = r; }
+        }
+        if (!(best > 0.0) || !isfinite(best)) return false;
+        if (piv != k) {
+            for (int c = 0; c < n; ++c) { const double t = A[k * n + c]; A[k * n + c] = A[piv * n + c]; A[piv * n + c] = t; }
+            const double t = b[k]; b[k] = b[piv]; b[piv] = t;
+        }
+        const double inv = 1.0 / A[k * n + k];
+        for (int r = k + 1; r < n; ++r) {
+            const double mlt = A[r * n + k] * inv;
+            if (mlt == 0.0) continue;
+            for (int c = k + 1; c < n; ++c) A[r * n + c] -= mlt * A[k * n + c];
+            b[r] -= mlt * b[k];
+        }
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        double s = b[k];
+        for (int c = k + 1; c < n; ++c) s -= A[k * n + c] * b[c];
+        b[k] = s / A[k * n + k];
+    }
+    return true;
+}
+
+// Newton direction δ (in a.delta) for J δ = -F. Returns false if singular.
+BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
+    const int lane = lane_id();
+    const int nk = I.iscr[ISCR_NK];
+    bool ok = true;
+    for (int j = 0; j + 1 < nk; ++j)
+        ok = bcr_segment(a, I, I.iscr[ISCR_KEPT + j], I.iscr[ISCR_KEPT + j + 1], I.scr + SCR_SEG + j * EQW) && ok;
+    int dense_ok = 1;
+    if (lane == 0) {
+        const int n = nk * M;
+        double* G = I.scr + SCR_DENSE;
+        double* rhs = I.scr + SCR_RHS;
+        for (int q = 0; q < n * n; ++q) G[q] = 0.0;
+        for (int j = 0; j + 1 < nk; ++j) {
+            const double* seg = I.scr + SCR_SEG + j * EQW;
+            for (int r = 0; r < M; ++r) {
+                const int row = j * M + r;
+                for (int c = 0; c < M; ++c) {
+                    G[row * n + j * M + c] = seg[r * M + c];
+                    G[row * n + (j + 1) * M + c] = seg[M * M + r * M + c];
+                }
+                rhs[row] = seg[2 * M * M + r];
+            }
+        }
+        const int row0 = (nk - 1) * M;
+        const int nb = I.iscr[ISCR_NB];
+        for (int k = 0; k < nb; ++k) {
+            const int node = I.iscr[ISCR_BNODE + k];
+            int kj = 0;
+            while (I.iscr[ISCR_KEPT + kj] != node) ++kj;
+            for (int r = 0; r < M; ++r)
+                for (int c = 0; c < M; ++c) G[(row0 + r) * n + kj * M + c] += I.scr[SCR_BCBLK + k * M * M + r * M + c];
+        }
+        for (int r = 0; r < M; ++r) rhs[row0 + r] = -I.scr[SCR_BCRES + r];
+        dense_ok = dense_solve(n, G, rhs) ? 1 : 0;
+        for (int j = 0; j < nk; ++j) {
+            JT* d = a.delta + (I.nb + I.iscr[ISCR_KEPT + j]) * M;
+            for (int r = 0; r < M; ++r) d[r] = JT(rhs[j * M + r]);
+        }
+    }
+    dense_ok = __shfl_sync(FULL, dense_ok, 0);
+    __syncwarp();
+    ok = ok && dense_ok;
+    if (!ok) return false;
+    for (int j = 0; j + 1 < nk; ++j) bcr_backsub(a, I, I.iscr[ISCR_KEPT + j], I.iscr[ISCR_KEPT + j + 1]);
+    bool bad = false;
+    for (int k = lane; k < I.N * M; k += 32) bad |= !isfinite(a.delta[I.nb * M + k]);
+    return !warp_any(bad);
+}
+
+// ---- Newton (default_internal_solve.jl:31-45; ||F||_inf <= abstol, mirk.jl:51) ------------
+BVP_DEV void copy_y(double* dst, const double* src, int n) {
+    for (int k = lane_id(); k < n; k += 32) dst[k] = src[k];
+    __syncwarp();
+}
+
+BVP_DEV bool newton_attempt(const Args& a, Inst& I, bool linesearch, int& iters, double& nrm_out) {
+    const int lane = lane_id();
+    double* y = y_of(a, I, I.cur);
+    double* yb = a.ybase + I.nb * M;
+    const int nM = I.N * M;
+    iters = 0;
+    double nrm = residual(a, I);
+    nrm_out = nrm;
+    if (!isfinite(nrm)) return false;
+    if (nrm <= a.abstol) return true;
+    const double nrm0 = nrm;
+    double best = nrm;
+    int stall = 0;
+    for (int it = 0; it < a.max_newton; ++it) {
+        jacobian(a, I);
+        if (!linear_solve(a, I)) return false;
+        ++iters;
+        const JT* dl = a.delta + I.nb * M;
+        if (!linesearch) {
+            for (int k = lane; k < nM; k += 32) y[k] += double(dl[k]);
+            __syncwarp();
+            nrm = residual(a, I);
+        } else {
+            const double f0 = residual_sq(a, I);
+            copy_y(yb, y, nM);
+            double alpha = 1.0;
+            bool ok = false;
+            for (int ls = 0; ls < 20; ++ls) {
+                for (int k = lane; k < nM; k += 32) y[k] = yb[k] + alpha * double(dl[k]);
+                __syncwarp();
+                nrm = residual(a, I);
+                const double f1 = residual_sq(a, I);
+                if (isfinite(nrm) && f1 <= (1.0 - 2e-4 * alpha) * f0) { ok = true; break; }
+                alpha *= 0.5;
+            }
+            if (!ok) { nrm_out = nrm; return false; }
+        }
+        nrm_out = nrm;
+        if (!isfinite(nrm)) return false;
+        if (nrm <= a.abstol) return true;
+        if (nrm > a.divergence_factor * nrm0) return false;
+        if (nrm < best) { best = nrm; stall = 0; }
+        else if (++stall >= a.stall_steps) return false;
+    }
+    return false;
+}
+
+BVP_DEV bool newton(const Args& a, Inst& I, InstState& s) {
+    double* y = y_of(a, I, I.cur);
+    const int nM = I.N * M;
+    copy_y(a.ybak + I.nb * M, y, nM);
+    int it = 0;
+    double nrm;
+    bool ok = newton_attempt(a, I, false, it, nrm);
+    s.newton_iters += it;
+    if (!ok && a.linesearch) {
+        copy_y(y, a.ybak + I.nb * M, nM);
+        ok = newton_attempt(a, I, true, it, nrm);
+        s.newton_iters += it;
+        s.flags |= 1;
+    }
+    s.resid = nrm;
+    return ok;
+}
+
+// ---- K4: defect estimate (adaptivity.jl:416-461) -------------------------------------------
+BVP_DEV double defect(const Args& a, const Inst& I) {
+    const int lane = lane_id();
+    const double* mesh = mesh_of(a, I, I.cur);
+    const double* h = h_of(a, I, I.cur);
+    const double* y = y_of(a, I, I.cur);
+    double w1[SS], w1p[SS], w2[SS], w2p[SS];
+    interp_weights(tau_star(), w1, w1p);
+    interp_weights(1.0 - tau_star(), w2, w2p);
+    double dn = 0.0;
+    bool bad = false;
+    for (int i = lane; i < I.N - 1; i += 32) {
+        double yi[M], yi1[M], Ki[S * M], KIi[NSXA * M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) { yi[m] = y[i * M + m]; yi1[m] = y[(i + 1) * M + m]; }
+        const double* Kg = a.K + (I.nb + i) * (S * M);
+#pragma unroll
+        for (int k = 0; k < S * M; ++k) Ki[k] = Kg[k];
+        interp_stages<double, double>(yi, yi1, Ki, KIi, I.p, mesh[i], h[i]);
+        double* KIg = a.KI + (I.nb + i) * (NSXA * M);
+#pragma unroll
+        for (int k = 0; k < NSX * M; ++k) KIg[k] = KIi[k];
+        double est[2];
+#pragma unroll
+        for (int smp = 0; smp < 2; ++smp) {
+            const double* w = smp ? w2 : w1;
+            const double* wp = smp ? w2p : w1p;
+            double z[M], zp[M], fz[M];
+            sum_stages<double>(w, yi, Ki, KIi, h[i], z);
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                double acc = Ki[m] * wp[0];
+#pragma unroll
+                for (int r = 1; r < S; ++r) acc += Ki[r * M + m] * wp[r];
+#pragma unroll
+                for (int qq = 0; qq < NSX; ++qq) acc += KIi[qq * M + m] * wp[S + qq];
+                zp[m] = acc;
+            }
+            bvp_f<double, double>(fz, z, I.p, mesh[i] + (smp ? 1.0 - tau_star() : tau_star()) * h[i]);
+            double e = 0.0;
+#pragma unroll
+            for (int m = 0; m < M; ++m) e = fmax(e, fabs((zp[m] - fz[m]) / (fabs(fz[m]) + 1.0)));
+            est[smp] = e;
+        }
+        const double ei = est[0] > est[1] ? est[0] : est[1];
+        a.err[I.nb + i] = ei;
+        bad |= isnan(ei);
+        dn = fmax(dn, ei);
+    }
+    __syncwarp();
+    dn = warp_max(dn);
+    return warp_any(bad) ? __longlong_as_double(0x7ff0000000000000LL) : dn;
+}
+
+// ---- mesh selection (adaptivity.jl:23-75, 250-304) -------------------------------------------
+// half_mesh! of buffer src into buffer dst
+BVP_DEV void half_mesh(const Args& a, Inst& I, int src, int dst) {
+    const double* m0 = mesh_of(a, I, src);
+    const double* h0 = h_of(a, I, src);
+    double* m1 = mesh_of(a, I, dst);
+    double* h1 = h_of(a, I, dst);
+    const int n = I.N - 1;
+    for (int i = lane_id(); i <= n; i += 32) {
+        m1[2 * i] = m0[i];
+        if (i < n) {
+            m1[2 * i + 1] = (m0[i + 1] + m0[i]) / 2.0;
+            h1[2 * i] = h0[i] / 2.0;
+            h1[2 * i + 1] = h0[i] / 2.0;
+        }
+    }
+    __syncwarp();
+}
+
+BVP_DEV long round_even(double x) { return (long)rint(x); }
+
+// Returns 1 on success (new mesh in buffer cur^1, I.N updated), 0 on Failure.
+BVP_DEV int mesh_selector(const Args& a, Inst& I, int& newN) {
+    const int lane = lane_id();
+    const int n = I.N - 1;
+    const double* h0 = h_of(a, I, I.cur);
+    double* e = a.err + I.nb;
+    const double ex = 1.0 / (ORD + 1);
+    double r1 = -__longlong_as_double(0x7ff0000000000000LL), r2 = 0.0;
+    for (int i = lane; i < n; i += 32) {
+        const double sh = pow(e[i] / a.abstol, ex);
+        e[i] = sh;
+        r1 = fmax(r1, sh);
+    }
+    __syncwarp();
+    r1 = warp_max(r1);
+    // the reference sums sequentially; keep that order
+    if (lane == 0) for (int i = 0; i < n; ++i) r2 += e[i];
+    r2 = __shfl_sync(FULL, r2, 0);
+    const double r3 = r2 / (I.N - 1);
+    long n_pred = round_even(1.3 * r2 + 1);
+    const double n_ = 0.1 * n;
+    if (fabs(double(n_pred - n)) < n_) n_pred = round_even(n + n_);
+    const int dst = I.cur ^ 1;
+    if (r1 <= 1.0 * r3) {
+        if (2L * n > a.max_sub || 2 * n + 1 > I.cap) return 0;
+        half_mesh(a, I, I.cur, dst);
+        newN = 2 * n + 1;
+        return 1;
+    }
+    const long lb = I.N / 2, ub = 4L * (I.N - 1);
+    long Nsub = n_pred < lb ? lb : n_pred;
+    Nsub = Nsub > ub ? ub : Nsub;
+    if (Nsub > a.max_sub || Nsub + 1 > I.cap) return 0;
+    for (int i = lane; i < n; i += 32) e[i] /= h0[i];
+    __syncwarp();
+    const double* om = mesh_of(a, I, I.cur);
+    double* nm = mesh_of(a, I, dst);
+    double* nh = h_of(a, I, dst);
+    if (lane == 0) {
+        // redistribute! (adaptivity.jl:250-278), sequential as in the reference
+        double tot = 0.0;
+        for (int k = 0; k < n; ++k) tot += e[k] * h0[k];
+        const double zeta = tot / double(Nsub);
+        nm[0] = om[0];
+        double t = om[0], integral = 0.0;
+        int k = 0, i = 0;
+        long guard = 4L * (n + Nsub) + 64;  // each pass advances k or places a point
+        while (k < n && --guard > 0) {
+            const double next_piece = e[k] * (om[k + 1] - t);
+            const double int_next = integral + next_piece;
+            if (int_next > zeta) {
+                const double pt = (zeta - integral) / e[k] + t;
+                if (i + 1 < Nsub) nm[i + 1] = pt;
+                t = pt; ++i; integral = 0.0;
+            } else {
+                integral = int_next; t = om[k + 1]; ++k;
+            }
+        }
+        nm[Nsub] = om[n];
+    }
+    __syncwarp();
+    for (int q = lane; q < Nsub; q += 32) nh[q] = nm[q + 1] - nm[q];
+    __syncwarp();
+    newN = int(Nsub + 1);
+    return 1;
+}
+
+// New solution on mesh buffer cur^1 from the old interpolant (adaptivity.jl:6-13 as
+// called in mirk.jl:366-371). With transfer_inplace the reference's in-place update is
+// reproduced: node j reads y[i_old] after nodes < j were already overwritten.
+BVP_DEV void transfer(const Args& a, Inst& I, int newN) {
+    const int lane = lane_id();
+    const int src = I.cur, dst = I.cur ^ 1;
+    const double* om = mesh_of(a, I, src);
+    const double* oh = h_of(a, I, src);
+    const double* nm = mesh_of(a, I, dst);
+    const double* oy = y_of(a, I, src);
+    double* ny = y_of(a, I, dst);
+    double* inc = a.inc + I.nb * M;
+    int* io = a.iold + I.nb;
+    for (int j = lane; j < newN; j += 32) {
+        const double t = nm[j];
+        const int i = interval_of(om, I.N, t);
+        const double dt = oh[i];
+        const double tau = (t - om[i]) / dt;
+        double w[SS], wp[SS];
+        interp_weights(tau, w, wp);
+        const double* Kg = a.K + (I.nb + i) * (S * M);
+        const double* KIg = a.KI + (I.nb + i) * (NSXA * M);
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            double acc = Kg[m] * w[0];
+#pragma unroll
+            for (int r = 1; r < S; ++r) acc += Kg[r * M + m] * w[r];
+#pragma unroll
+            for (int qq = 0; qq < NSX; ++qq) acc += KIg[qq * M + m] * w[S + qq];
+            if (a.transfer_inplace) inc[j * M + m] = acc * dt;
+            else ny[j * M + m] = acc * dt + oy[i * M + m];
+        }
+        io[j] = i;
+    }
+    __syncwarp();
+    if (a.transfer_inplace && lane == 0) {
+        for (int j = 0; j < newN; ++j) {
+            const int i = io[j];
+            const double* base = (i < j) ? ny + i * M : oy + i * M;
+#pragma unroll
+            for (int m = 0; m < M; ++m) ny[j * M + m] = inc[j * M + m] + base[m];
+        }
+    }
+    __syncwarp();
+}
+
+// ---- one instance, whole adaptive solve (solve!, mirk.jl:286-388) -----------------------------
+BVP_DEV void init_instance(const Args& a, Inst& I) {
+    const int lane = lane_id();
+    const int n = a.n_init[I.q];
+    const double t0 = a.tspans[2 * I.q], t1 = a.tspans[2 * I.q + 1];
+    double* mesh = mesh_of(a, I, 0);
+    double* h = h_of(a, I, 0);
+    double* y = y_of(a, I, 0);
+    const double hh = (t1 - t0) / n;   // range(t0; stop = t1, length = n + 1) (Core/utils.jl:694-700)
+    for (int i = lane; i <= n; i += 32) mesh[i] = (i == n) ? t1 : fma(double(i), hh, t0);
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) h[i] = mesh[i + 1] - mesh[i];
+    if (a.y0_mode == 0) {
+        const double* src = a.y0 + I.q * M;
+        for (int k = lane; k < (n + 1) * M; k += 32) y[k] = src[k % M];
+    } else {
+        const double* src = a.y0 + a.y0_off[I.q] * M;
+        for (int k = lane; k < (n + 1) * M; k += 32) y[k] = src[k];
+    }
+    __syncwarp();
+    I.N = n + 1;
+    I.cur = 0;
+}
+
+BVP_DEV void finalize_stages(const Args& a, Inst& I) {
+    residual(a, I);
+    const double* mesh = mesh_of(a, I, I.cur);
+    const double* h = h_of(a, I, I.cur);
+    const double* y = y_of(a, I, I.cur);
+    for (int i = lane_id(); i < I.N - 1; i += 32) {
+        double yi[M], yi1[M], Ki[S * M], KIi[NSXA * M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) { yi[m] = y[i * M + m]; yi1[m] = y[(i + 1) * M + m]; }
+        const double* Kg = a.K + (I.nb + i) * (S * M);
+#pragma unroll
+        for (int k = 0; k < S * M; ++k) Ki[k] = Kg[k];
+        interp_stages<double, double>(yi, yi1, Ki, KIi, I.p, mesh[i], h[i]);
+        double* KIg = a.KI + (I.nb + i) * (NSXA * M);
+#pragma unroll
+        for (int k = 0; k < NSX * M; ++k) KIg[k] = KIi[k];
+    }
+    __syncwarp();
+}
+
+BVP_DEV void solve_instance(const Args& a, Inst& I) {
+    InstState s;
+    s.retcode = RET_FAILURE; s.newton_iters = 0; s.rounds = 0; s.flags = 0;
+    s.defect = __longlong_as_double(0x7ff8000000000000LL);
+    s.resid = s.defect;
+    init_instance(a, I);
+    int info_ok = 1;
+    bool maxed = false;
+    while (true) {
+        ++s.rounds;
+        double error_norm = 2 * a.abstol;
+        const bool nl_ok = newton(a, I, s);
+        if (!a.adaptive) { s.retcode = nl_ok ? RET_SUCCESS : RET_FAILURE; info_ok = nl_ok; break; }
+        bool ok = nl_ok;
+        if (ok) {
+            error_norm = defect(a, I);
+            s.defect = error_norm;
+            ok = !(error_norm > a.defect_threshold) && !isnan(error_norm);
+        }
+        if (ok) {
+            if (error_norm > a.abstol) {
+                int newN = 0;
+                info_ok = mesh_selector(a, I, newN);
+                if (info_ok) {
+                    transfer(a, I, newN);
+                    I.cur ^= 1;
+                    I.N = newN;
+                }
+            } else {
+                info_ok = 1;
+            }
+        } else {
+            if (2L * (I.N - 1) > a.max_sub || 2 * (I.N - 1) + 1 > I.cap) {
+                info_ok = 0;
+                if (2 * (I.N - 1) + 1 > I.cap) s.flags |= 2;
+            } else {
+                half_mesh(a, I, I.cur, I.cur ^ 1);
+                I.cur ^= 1;
+                I.N = 2 * (I.N - 1) + 1;
+                double* y = y_of(a, I, I.cur);
+                for (int k = lane_id(); k < I.N * M; k += 32) y[k] = 0.0;
+                __syncwarp();
+                info_ok = 1;
+            }
+        }
+        if (!(info_ok && error_norm > a.abstol)) break;
+        if (s.rounds >= a.max_rounds) { maxed = true; break; }
+    }
+    if (a.adaptive) s.retcode = maxed ? RET_MAXITERS : (info_ok ? RET_SUCCESS : RET_FAILURE);
+    if (a.want_stages) finalize_stages(a, I);
+    // results live in buffer 0
+    if (I.cur == 1) {
+        double* m0 = mesh_of(a, I, 0); const double* m1 = mesh_of(a, I, 1);
+        double* h0 = h_of(a, I, 0); const double* h1 = h_of(a, I, 1);
+        double* y0 = y_of(a, I, 0); const double* y1 = y_of(a, I, 1);
+        for (int k = lane_id(); k < I.N; k += 32) { m0[k] = m1[k]; if (k < I.N - 1) h0[k] = h1[k]; }
+        for (int k = lane_id(); k < I.N * M; k += 32) y0[k] = y1[k];
+        __syncwarp();
+        I.cur = 0;
+    }
+    s.N = I.N;
+    s.cur = 0;
+    if (lane_id() == 0) a.st[I.q] = s;
+    __syncwarp();
+}
+
+BVP_DEV Inst make_inst(const Args& a, int q) {
+    Inst I;
+    I.q = q;
+    I.nb = a.node_off[q];
+    I.cap = a.cap[q];
+    I.p = a.params + (long long)q * a.n_params;
+    I.pj = a.params_j + (long long)q * a.n_params;
+    I.scr = a.scr + (long long)q * SCRW;
+    I.iscr = a.iscr + (long long)q * ISCRW;
+    I.N = 0;
+    I.cur = 0;
+    return I;
+}
+
+}  // namespace bvp
+
+// ---- kernels ---------------------------------------------------------------------------------
+// Persistent fused solve: each warp repeatedly takes the next instance from the work
+// counter and runs its complete adaptive solve.
+extern "C" __global__ void __launch_bounds__(128) bvp_solve_fused(const bvp::Args a) {
+    const int lane = bvp::lane_id();
+    while (true) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(a.work_counter, 1);
+        k = __shfl_sync(bvp::FULL, k, 0);
+        if (k >= a.n_inst) break;
+        bvp::Inst I = bvp::make_inst(a, a.order[k]);
+        bvp::solve_instance(a, I);
+    }
+}
+
+// Stage kernels on caller-provided (mesh, y) in buffer 0 with N = st[q].N. Used by the
+// per-kernel parity tests; stage: 0 residual (F, K, BC residual), 1 Jacobian blocks,
+// 2 Newton direction (residual + Jacobian + factor/solve), 3 defect (residual + defect).
+extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, int stage, double* out_norm) {
+    const int lane = bvp::lane_id();
+    while (true) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(a.work_counter, 1);
+        k = __shfl_sync(bvp::FULL, k, 0);
+        if (k >= a.n_inst) break;
+        bvp::Inst I = bvp::make_inst(a, a.order[k]);
+        I.N = a.st[I.q].N;
+        I.cur = 0;
+        double v = bvp::residual(a, I);
+        if (stage >= 1 && stage <= 2) bvp::jacobian(a, I);
+        if (stage == 2) v = bvp::linear_solve(a, I) ? 0.0 : 1.0;
+        if (stage == 3) v = bvp::defect(a, I);
+        if (lane == 0) out_norm[I.q] = v;
+        __syncwarp();
+    }
+}
+
+// Copy the results of every instance (buffer 0) into packed host-bound arrays.
+extern "C" __global__ void bvp_pack(const bvp::Args a, const long long* out_off, double* mesh_out,
+                                    double* y_out, int want_stages, double* K_out, double* KI_out) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = bvp::lane_id();
+    if (warp >= a.n_inst) return;
+    const int q = warp;
+    const long long nb = a.node_off[q];
+    const int N = a.st[q].N;
+    const long long o = out_off[q];
+    for (int k = lane; k < N; k += 32) mesh_out[o + k] = a.mesh[nb + k];
+    for (int k = lane; k < N * bvp::M; k += 32) y_out[o * bvp::M + k] = a.y[nb * bvp::M + k];
+    if (want_stages) {
+        // stages are per interval; packed at the instance's node offset (N-1 used)
+        for (int k = lane; k < (N - 1) * bvp::S * bvp::M; k += 32)
+            K_out[o * bvp::S * bvp::M + k] = a.K[nb * bvp::S * bvp::M + k];
+        for (int k = lane; k < (N - 1) * bvp::NSXA * bvp::M; k += 32)
+            KI_out[o * bvp::NSXA * bvp::M + k] = a.KI[nb * bvp::NSXA * bvp::M + k];
+    }
+}
+
+// Device-side layout constants, checked against the host's at handle creation.
+extern "C" __global__ void bvp_layout_probe(int* out) {
+    out[0] = bvp::SCRW;
+    out[1] = bvp::ISCRW;
+    out[2] = bvp::EQW;
+    out[3] = bvp::RECW;
+    out[4] = int(sizeof(BvpArgs));
+    out[5] = int(sizeof(BvpInstState));
+    out[6] = bvp::NSXA;
+    out[7] = bvp::S;
+}
+
+// Parameters in the Jacobian precision.
+extern "C" __global__ void bvp_convert_params(const double* p, bvp::JT* pj, long long n) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        pj[k] = bvp::JT(p[k]);
+}
+
+// One block: node capacities (max(n, max_sub) + 1), their exclusive prefix sum (arena
+// offsets), and the work order, costliest (largest initial mesh) first.
+extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_init, int max_sub, int* cap,
+                                                            long long* node_off, int* order, int* counter) {
+    constexpr int NB = 4096;
+    __shared__ int hist[NB];
+    __shared__ long long wsum[32];
+    __shared__ long long carry;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int k = tid; k < NB; k += blockDim.x) hist[k] = 0;
+    if (tid == 0) { carry = 0; *counter = 0; }
+    __syncthreads();
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int q = base + tid;
+        long long c = 0;
+        if (q < n) {
+            const int ni = n_init[q];
+            c = (ni > max_sub ? ni : max_sub) + 1;
+            cap[q] = int(c);
+        }
+        long long v = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long t = __shfl_up_sync(bvp::FULL, v, o);
+            if (lane >= o) v += t;
+        }
+        if (lane == 31) wsum[warp] = v;
+        __syncthreads();
+        if (warp == 0) {
+            long long w = (lane < int(blockDim.x >> 5)) ? wsum[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long t = __shfl_up_sync(bvp::FULL, w, o);
+                if (lane >= o) w += t;
+            }
+            wsum[lane] = w;
+        }
+        __syncthreads();
+        const long long excl = carry + (warp > 0 ? wsum[warp - 1] : 0) + v - c;
+        if (q < n) node_off[q] = excl;
+        __syncthreads();
+        if (tid == 0) carry += wsum[31];
+        __syncthreads();
+    }
+    for (int q = tid; q < n; q += blockDim.x) {
+        const int key = n_init[q] < NB - 1 ? n_init[q] : NB - 1;
+        atomicAdd(&hist[NB - 1 - key], 1);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int PER = NB / 32;
+        int s = 0;
+        for (int k = 0; k < PER; ++k) s += hist[lane * PER + k];
+        int incl = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(bvp::FULL, incl, o);
+            if (lane >= o) incl += t;
+        }
+        int run = incl - s;
+        for (int k = 0; k < PER; ++k) {
+            const int hv = hist[lane * PER + k];
+            hist[lane * PER + k] = run;
+            run += hv;
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < n; q += blockDim.x) {
+        const int key = n_init[q] < NB - 1 ? n_init[q] : NB - 1;
+        const int pos = atomicAdd(&hist[NB - 1 - key], 1);
+        order[pos] = q;
+    }
+}

@@ -1,0 +1,104 @@
+// Structures shared by the host runtime and the JIT-compiled device code: the kernel
+// argument block, the per-instance state record, and the scratch layout formulas.
+// Both sides include this file so the launch ABI cannot drift. The device build defines
+// BVP_JT_PTR as the Jacobian scalar type; the host sees those arrays as void*.
+#pragma once
+
+#ifndef BVP_JT_PTR
+#define BVP_JT_PTR void
+#endif
+
+#ifdef __CUDACC_RTC__
+typedef long long bvp_i64;
+#else
+#include <cstdint>
+typedef long long bvp_i64;
+#endif
+
+struct BvpInstState {
+    int N;              // current mesh points
+    int cur;            // active ping-pong buffer
+    int retcode;        // 0 success, 1 failure, 2 max rounds
+    int newton_iters;
+    int rounds;
+    int flags;          // bit0: line-search fallback used, bit1: capacity guard hit
+    double defect;
+    double resid;
+};
+
+struct BvpArgs {
+    int n_inst, n_params;
+    int adaptive, max_sub, max_newton, max_rounds, stall_steps;
+    int transfer_inplace, bc_jac_exact, linesearch, want_stages, y0_mode;
+    double abstol, defect_threshold, divergence_factor;
+    double bc_t[16];
+    bvp_i64 tot;                   // total node capacity (sum over instances)
+    const int* order;              // work order (instance ids, costliest first)
+    int* work_counter;
+    const double* params;          // n_inst x n_params
+    const BVP_JT_PTR* params_j;    // same, in the Jacobian precision
+    const int* n_init;             // initial interval counts
+    const double* tspans;          // n_inst x 2
+    const double* y0;              // y0_mode 0: n_inst x M; 1: packed per-node guesses
+    const bvp_i64* y0_off;         // y0_mode 1: per-instance offsets (in M-vectors)
+    const bvp_i64* node_off;       // per-instance node offset into the arena
+    const int* cap;                // per-instance node capacity
+    double* mesh;                  // [2][tot]
+    double* h;                     // [2][tot]
+    double* y;                     // [2][tot][M]
+    double* ybak;                  // [tot][M]
+    double* ybase;                 // [tot][M]
+    double* K;                     // [tot][S][M]
+    double* KI;                    // [tot][NSXA][M]
+    double* F;                     // [tot][M]  collocation residual of interval i
+    double* err;                   // [tot]
+    double* inc;                   // [tot][M]
+    int* iold;                     // [tot]
+    BVP_JT_PTR* Sb;                // [tot][M][M]
+    BVP_JT_PTR* Rb;                // [tot][M][M]
+    BVP_JT_PTR* rec;               // [tot][RECW]
+    BVP_JT_PTR* eq;                // [2][tot][EQW]
+    BVP_JT_PTR* delta;             // [tot][M]
+    double* scr;                   // per-instance scratch, SCRW doubles each
+    int* iscr;                     // per-instance int scratch, ISCRW ints each
+    BvpInstState* st;
+};
+
+// Scratch layout as a function of (M, order, BC evaluation points, two-point).
+struct BvpLayout {
+    int M, S, SS, NSX, NSXA, EQW, RECW, NBCB, KMAX, NDENSE;
+    int SCR_BCRES, SCR_BCBLK, SCR_SEG, SCR_DENSE, SCR_RHS, SCRW;
+    int ISCR_NK, ISCR_KEPT, ISCR_NB, ISCR_BNODE, ISCRW;
+};
+
+#ifdef __CUDACC_RTC__
+#define BVP_LAYOUT_FN __host__ __device__ inline
+#else
+#define BVP_LAYOUT_FN inline
+#endif
+
+BVP_LAYOUT_FN BvpLayout bvp_make_layout(int M, int order, int nbc, int twopoint) {
+    BvpLayout L;
+    L.M = M;
+    L.S = order - 1;
+    L.SS = (order == 2 || order == 3) ? 3 : (order == 4 ? 4 : (order == 5 ? 6 : 9));
+    L.NSX = L.SS - L.S;
+    L.NSXA = L.NSX > 0 ? L.NSX : 1;
+    L.EQW = 2 * M * M + M;
+    L.RECW = 3 * M * M + M;
+    L.NBCB = twopoint ? 2 : 2 * nbc;
+    L.KMAX = 2 + L.NBCB;
+    L.NDENSE = L.KMAX * M;
+    L.SCR_BCRES = 0;
+    L.SCR_BCBLK = L.SCR_BCRES + M;
+    L.SCR_SEG = L.SCR_BCBLK + L.NBCB * M * M;
+    L.SCR_DENSE = L.SCR_SEG + (L.KMAX - 1) * L.EQW;
+    L.SCR_RHS = L.SCR_DENSE + L.NDENSE * L.NDENSE;
+    L.SCRW = L.SCR_RHS + L.NDENSE;
+    L.ISCR_NK = 0;
+    L.ISCR_KEPT = 1;
+    L.ISCR_NB = L.ISCR_KEPT + L.KMAX;
+    L.ISCR_BNODE = L.ISCR_NB + 1;
+    L.ISCRW = L.ISCR_BNODE + L.NBCB;
+    return L;
+}

@@ -1,0 +1,694 @@
+// Host runtime of libbvpgpu.so: the C ABI declared in include/bvpgpu.h.
+//
+// bvp_create JIT-compiles the device code (bvp_prelude.cuh + the user's problem source +
+// bvp_kernels.cuh) with NVRTC for sm_103a, caches the cubin on disk, and loads it with
+// the runtime's library API. bvp_solve_batch stages the inputs through pinned memory,
+// launches the prep and the persistent fused solve kernels on the handle's stream, and
+// brings the per-instance results and the packed solutions back.
+//
+// The host side of the reference path this replaces is SciMLBase.__init / solve! of
+// lib/BoundaryValueDiffEqMIRK/src/mirk.jl:49-332 (setup, outer loop orchestration) and
+// the EnsembleProblem loop over trajectories.
+#include "bvpgpu.h"
+
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bvp_shared.h"
+#include "bvp_embedded.inc"  // kEmbedCount, kEmbedNames[], kEmbedSources[], kEmbedHash
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct HostBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct bvp_handle_s {
+    bvp_problem_desc desc{};
+    bvp_options opt{};
+    std::string source;
+    std::string err;
+    BvpLayout L{};
+    int js = 4;  // sizeof Jacobian scalar
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t k_fused = nullptr, k_stage = nullptr, k_pack = nullptr, k_probe = nullptr,
+                 k_convert = nullptr, k_prep = nullptr;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    // device arrays
+    DevBuf d_mesh, d_h, d_y, d_ybak, d_ybase, d_K, d_KI, d_F, d_err, d_inc, d_iold, d_Sb, d_Rb,
+        d_rec, d_eq, d_delta, d_scr, d_iscr, d_st, d_order, d_cap, d_node_off, d_counter,
+        d_params, d_params_j, d_n_init, d_tspans, d_y0, d_y0_off, d_out_off, d_out_mesh,
+        d_out_y, d_out_K, d_out_KI, d_norm;
+    // pinned host staging
+    HostBuf h_in, h_st, h_off, h_mesh, h_y, h_K, h_KI;
+    // last batch
+    int last_n = 0;
+    long long last_tot = 0;
+    bool have_results = false;
+    bool pending_device = false;
+    int pending_n = 0;
+    double timing_ms[2] = {0, 0};
+    std::vector<BvpInstState> st;
+    std::vector<int64_t> offsets;
+};
+
+namespace {
+
+bvp_status fail(bvp_handle* h, bvp_status s, const std::string& msg) {
+    if (h) h->err = msg;
+    return s;
+}
+
+#define CU(call)                                                                             \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(h, BVP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+bool ensure_dev(DevBuf& b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return true;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    if (cudaMalloc(&b.p, bytes) != cudaSuccess) { b.p = nullptr; return false; }
+    b.bytes = bytes;
+    return true;
+}
+
+bool ensure_host(HostBuf& b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return true;
+    if (b.p) cudaFreeHost(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    if (cudaMallocHost(&b.p, bytes) != cudaSuccess) { b.p = nullptr; return false; }
+    b.bytes = bytes;
+    return true;
+}
+
+uint64_t fnv1a(const void* data, size_t n, uint64_t h = 1469598103934665603ull) {
+    const unsigned char* p = static_cast<const unsigned char*>(data);
+    for (size_t i = 0; i < n; ++i) { h ^= p[i]; h *= 1099511628211ull; }
+    return h;
+}
+
+std::string lib_dir() {
+    Dl_info info;
+    if (dladdr(reinterpret_cast<void*>(&bvp_default_options), &info) && info.dli_fname) {
+        std::string p(info.dli_fname);
+        const size_t k = p.rfind('/');
+        if (k != std::string::npos) return p.substr(0, k);
+    }
+    return ".";
+}
+
+std::string cache_dir() {
+    const char* env = std::getenv("BVPGPU_CACHE_DIR");
+    std::string d = env && *env ? std::string(env) : lib_dir() + "/jit_cache";
+    mkdir(d.c_str(), 0755);
+    return d;
+}
+
+bool read_file(const std::string& path, std::vector<char>& out) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) return false;
+    std::fseek(f, 0, SEEK_END);
+    const long n = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    out.resize(n > 0 ? size_t(n) : 0);
+    const size_t got = n > 0 ? std::fread(out.data(), 1, size_t(n), f) : 0;
+    std::fclose(f);
+    return n > 0 && got == size_t(n);
+}
+
+void write_file_atomic(const std::string& path, const std::vector<char>& data) {
+    const std::string tmp = path + ".tmp" + std::to_string(long(getpid()));
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return;
+    std::fwrite(data.data(), 1, data.size(), f);
+    std::fclose(f);
+    std::rename(tmp.c_str(), path.c_str());
+}
+
+}  // namespace
+
+extern "C" {
+
+void bvp_default_options(bvp_options* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->order = 4;
+    o->adaptive = 1;
+    o->max_subintervals = 3000;
+    o->max_newton = 100;
+    o->max_rounds = 64;
+    o->transfer_inplace = 1;
+    o->bc_jac_exact = 0;
+    o->linesearch_fallback = 1;
+    o->stall_steps = 32;
+    o->jac_precision = 32;
+    o->want_stages = 0;
+    o->abstol = 1e-6;
+    o->defect_threshold = 0.1;
+    o->divergence_factor = 1e3;
+}
+
+const char* bvp_last_error(bvp_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+void* bvp_stream(bvp_handle* h) { return h ? static_cast<void*>(h->stream) : nullptr; }
+
+static bvp_status compile_and_load(bvp_handle* h) {
+    const bvp_problem_desc& d = h->desc;
+    const bvp_options& o = h->opt;
+    std::vector<std::string> opts = {
+        "--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true",
+        "-DBVP_M=" + std::to_string(d.M), "-DBVP_ORDER=" + std::to_string(o.order),
+        "-DBVP_TWOPOINT=" + std::to_string(d.twopoint),
+        "-DBVP_NBC=" + std::to_string(d.twopoint ? 2 : d.n_bc_pts),
+        "-DBVP_LA=" + std::to_string(d.twopoint ? d.La : 0),
+        std::string("-DBVP_JT=") + (o.jac_precision == 64 ? "double" : "float"),
+    };
+    const std::string src = std::string("#include \"bvp_prelude.cuh\"\n#line 1 \"problem_source\"\n") +
+                            h->source + "\n#include \"bvp_kernels.cuh\"\n";
+    uint64_t key = fnv1a(kEmbedHash, std::strlen(kEmbedHash));
+    key = fnv1a(src.data(), src.size(), key);
+    for (auto& s : opts) key = fnv1a(s.data(), s.size() + 1, key);
+    char name[64];
+    std::snprintf(name, sizeof(name), "/bvp_%016llx.cubin", (unsigned long long)key);
+    const std::string path = cache_dir() + name;
+    std::vector<char> cubin;
+    if (!read_file(path, cubin)) {
+        nvrtcProgram prog;
+        if (nvrtcCreateProgram(&prog, src.c_str(), "bvp_problem.cu", kEmbedCount, kEmbedSources,
+                               kEmbedNames) != NVRTC_SUCCESS)
+            return fail(h, BVP_ERR_COMPILE, "nvrtcCreateProgram failed");
+        std::vector<const char*> cop;
+        for (auto& s : opts) cop.push_back(s.c_str());
+        const nvrtcResult rc = nvrtcCompileProgram(prog, int(cop.size()), cop.data());
+        size_t logn = 0;
+        nvrtcGetProgramLogSize(prog, &logn);
+        std::string log(logn, '\0');
+        if (logn) nvrtcGetProgramLog(prog, &log[0]);
+        if (rc != NVRTC_SUCCESS) {
+            nvrtcDestroyProgram(&prog);
+            return fail(h, BVP_ERR_COMPILE, "NVRTC: " + std::string(nvrtcGetErrorString(rc)) + "\n" + log);
+        }
+        size_t n = 0;
+        nvrtcGetCUBINSize(prog, &n);
+        cubin.resize(n);
+        nvrtcGetCUBIN(prog, cubin.data());
+        nvrtcDestroyProgram(&prog);
+        write_file_atomic(path, cubin);
+    }
+    CU(cudaLibraryLoadData(&h->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+    CU(cudaLibraryGetKernel(&h->k_fused, h->lib, "bvp_solve_fused"));
+    CU(cudaLibraryGetKernel(&h->k_stage, h->lib, "bvp_stage"));
+    CU(cudaLibraryGetKernel(&h->k_pack, h->lib, "bvp_pack"));
+    CU(cudaLibraryGetKernel(&h->k_probe, h->lib, "bvp_layout_probe"));
+    CU(cudaLibraryGetKernel(&h->k_convert, h->lib, "bvp_convert_params"));
+    CU(cudaLibraryGetKernel(&h->k_prep, h->lib, "bvp_prep"));
+    return BVP_OK;
+}
+
+bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bvp_options* opt,
+                      bvp_handle** out) {
+    bvp_handle* h = nullptr;
+    if (!desc || !source || !out) return BVP_ERR_INVALID;
+    *out = nullptr;
+    h = new bvp_handle_s();
+    h->desc = *desc;
+    if (opt) h->opt = *opt; else bvp_default_options(&h->opt);
+    h->source = source;
+    const bvp_problem_desc& d = h->desc;
+    const bvp_options& o = h->opt;
+    std::string why;
+    if (d.M < 1 || d.M > 8) why = "M must be in 1..8";
+    else if (d.n_params < 0) why = "n_params must be >= 0";
+    else if (!d.twopoint && (d.n_bc_pts < 1 || d.n_bc_pts > 16)) why = "n_bc_pts must be in 1..16";
+    else if (d.twopoint && (d.La < 0 || d.Lb < 0 || d.La + d.Lb != d.M)) why = "La + Lb must equal M";
+    else if (o.order < 2 || o.order > 6) why = "order must be 2..6";
+    else if (!(o.abstol > 0)) why = "abstol must be > 0";
+    else if (o.max_subintervals < 1) why = "max_subintervals must be >= 1";
+    else if (o.jac_precision != 32 && o.jac_precision != 64) why = "jac_precision must be 32 or 64";
+    if (!why.empty()) { delete h; return BVP_ERR_INVALID; }
+    h->L = bvp_make_layout(d.M, o.order, d.twopoint ? 2 : d.n_bc_pts, d.twopoint);
+    h->js = o.jac_precision == 64 ? 8 : 4;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaEventCreate(&h->ev[k]);
+    if (e != cudaSuccess) {
+        h->err = std::string("CUDA init: ") + cudaGetErrorString(e);
+        *out = h;
+        return BVP_ERR_CUDA;
+    }
+    bvp_status s = compile_and_load(h);
+    *out = h;
+    if (s != BVP_OK) return s;
+    // check that host and device agree on the launch ABI
+    DevBuf probe;
+    if (!ensure_dev(probe, 16 * sizeof(int))) return fail(h, BVP_ERR_NOMEM, "probe alloc");
+    int* pp = static_cast<int*>(probe.p);
+    void* args[] = {&pp};
+    CU(cudaLaunchKernel((const void*)h->k_probe, dim3(1), dim3(1), args, 0, h->stream));
+    int got[16] = {0};
+    CU(cudaMemcpyAsync(got, probe.p, sizeof(got), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
+    cudaFree(probe.p);
+    const BvpLayout& L = h->L;
+    if (got[0] != L.SCRW || got[1] != L.ISCRW || got[2] != L.EQW || got[3] != L.RECW ||
+        got[4] != int(sizeof(BvpArgs)) || got[5] != int(sizeof(BvpInstState)) ||
+        got[6] != L.NSXA || got[7] != L.S)
+        return fail(h, BVP_ERR_STATE, "host/device layout mismatch");
+    return BVP_OK;
+}
+
+static bvp_status ensure_arena(bvp_handle* h, long long tot, int n, long long y0_vals) {
+    const BvpLayout& L = h->L;
+    const int M = L.M, js = h->js;
+    const size_t T = size_t(tot);
+    bool ok = ensure_dev(h->d_mesh, 2 * T * 8) && ensure_dev(h->d_h, 2 * T * 8) &&
+              ensure_dev(h->d_y, 2 * T * M * 8) && ensure_dev(h->d_ybak, T * M * 8) &&
+              ensure_dev(h->d_ybase, T * M * 8) && ensure_dev(h->d_K, T * L.S * M * 8) &&
+              ensure_dev(h->d_KI, T * L.NSXA * M * 8) && ensure_dev(h->d_F, T * M * 8) &&
+              ensure_dev(h->d_err, T * 8) && ensure_dev(h->d_inc, T * M * 8) &&
+              ensure_dev(h->d_iold, T * 4) && ensure_dev(h->d_Sb, T * M * M * js) &&
+              ensure_dev(h->d_Rb, T * M * M * js) && ensure_dev(h->d_rec, T * L.RECW * js) &&
+              ensure_dev(h->d_eq, 2 * T * L.EQW * js) && ensure_dev(h->d_delta, T * M * js) &&
+              ensure_dev(h->d_scr, size_t(n) * L.SCRW * 8) && ensure_dev(h->d_iscr, size_t(n) * L.ISCRW * 4) &&
+              ensure_dev(h->d_st, size_t(n) * sizeof(BvpInstState)) && ensure_dev(h->d_order, size_t(n) * 4) &&
+              ensure_dev(h->d_cap, size_t(n) * 4) && ensure_dev(h->d_node_off, size_t(n) * 8) &&
+              ensure_dev(h->d_counter, 16) &&
+              ensure_dev(h->d_params, size_t(n) * std::max(1, h->desc.n_params) * 8) &&
+              ensure_dev(h->d_params_j, size_t(n) * std::max(1, h->desc.n_params) * js) &&
+              ensure_dev(h->d_n_init, size_t(n) * 4) && ensure_dev(h->d_tspans, size_t(n) * 16) &&
+              ensure_dev(h->d_y0, size_t(std::max<long long>(y0_vals, 1)) * 8) &&
+              ensure_dev(h->d_y0_off, size_t(n) * 8) && ensure_dev(h->d_out_off, size_t(n + 1) * 8) &&
+              ensure_dev(h->d_norm, size_t(n) * 8);
+    if (!ok) return fail(h, BVP_ERR_NOMEM, "device allocation failed");
+    return BVP_OK;
+}
+
+static void fill_args(bvp_handle* h, BvpArgs& a, int n, long long tot, int y0_mode, const double* d_params,
+                      const int* d_n_init, const double* d_tspans, const double* d_y0, const long long* d_y0_off) {
+    const bvp_options& o = h->opt;
+    std::memset(&a, 0, sizeof(a));
+    a.n_inst = n;
+    a.n_params = h->desc.n_params;
+    a.adaptive = o.adaptive;
+    a.max_sub = o.max_subintervals;
+    a.max_newton = o.max_newton;
+    a.max_rounds = o.max_rounds;
+    a.stall_steps = o.stall_steps;
+    a.transfer_inplace = o.transfer_inplace;
+    a.bc_jac_exact = o.bc_jac_exact;
+    a.linesearch = o.linesearch_fallback;
+    a.want_stages = o.want_stages;
+    a.y0_mode = y0_mode;
+    a.abstol = o.abstol;
+    a.defect_threshold = o.defect_threshold;
+    a.divergence_factor = o.divergence_factor;
+    for (int k = 0; k < 16; ++k) a.bc_t[k] = h->desc.bc_t[k];
+    a.tot = tot;
+    a.order = static_cast<const int*>(h->d_order.p);
+    a.work_counter = static_cast<int*>(h->d_counter.p);
+    a.params = d_params;
+    a.params_j = h->d_params_j.p;
+    a.n_init = d_n_init;
+    a.tspans = d_tspans;
+    a.y0 = d_y0;
+    a.y0_off = d_y0_off;
+    a.node_off = static_cast<const bvp_i64*>(h->d_node_off.p);
+    a.cap = static_cast<const int*>(h->d_cap.p);
+    a.mesh = static_cast<double*>(h->d_mesh.p);
+    a.h = static_cast<double*>(h->d_h.p);
+    a.y = static_cast<double*>(h->d_y.p);
+    a.ybak = static_cast<double*>(h->d_ybak.p);
+    a.ybase = static_cast<double*>(h->d_ybase.p);
+    a.K = static_cast<double*>(h->d_K.p);
+    a.KI = static_cast<double*>(h->d_KI.p);
+    a.F = static_cast<double*>(h->d_F.p);
+    a.err = static_cast<double*>(h->d_err.p);
+    a.inc = static_cast<double*>(h->d_inc.p);
+    a.iold = static_cast<int*>(h->d_iold.p);
+    a.Sb = h->d_Sb.p;
+    a.Rb = h->d_Rb.p;
+    a.rec = h->d_rec.p;
+    a.eq = h->d_eq.p;
+    a.delta = h->d_delta.p;
+    a.scr = static_cast<double*>(h->d_scr.p);
+    a.iscr = static_cast<int*>(h->d_iscr.p);
+    a.st = static_cast<BvpInstState*>(h->d_st.p);
+}
+
+static int fused_grid(bvp_handle* h, int n) {
+    const int warps_per_block = 4;
+    const int want = (n + warps_per_block - 1) / warps_per_block;
+    const int cap = std::max(1, h->sm_count) * 16;
+    return std::max(1, std::min(want, cap));
+}
+
+// Launches prep + conversion + fused solve on the handle's stream.
+static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode, const double* d_params,
+                               const int* d_n_init, const double* d_tspans, const double* d_y0,
+                               const long long* d_y0_off) {
+    BvpArgs a;
+    fill_args(h, a, n, tot, y0_mode, d_params, d_n_init, d_tspans, d_y0, d_y0_off);
+    CU(cudaEventRecord(h->ev[0], h->stream));
+    {
+        long long np = (long long)n * h->desc.n_params;
+        const double* src = d_params;
+        void* dst = h->d_params_j.p;
+        void* args[] = {&src, &dst, &np};
+        const int blocks = int(std::min<long long>((np + 255) / 256 + 1, 4096));
+        CU(cudaLaunchKernel((const void*)h->k_convert, dim3(blocks), dim3(256), args, 0, h->stream));
+    }
+    {
+        int nn = n, ms = h->opt.max_subintervals;
+        const int* ni = d_n_init;
+        int* cap = static_cast<int*>(h->d_cap.p);
+        bvp_i64* off = static_cast<bvp_i64*>(h->d_node_off.p);
+        int* ord = static_cast<int*>(h->d_order.p);
+        int* ctr = static_cast<int*>(h->d_counter.p);
+        void* args[] = {&nn, &ni, &ms, &cap, &off, &ord, &ctr};
+        CU(cudaLaunchKernel((const void*)h->k_prep, dim3(1), dim3(1024), args, 0, h->stream));
+    }
+    CU(cudaEventRecord(h->ev[1], h->stream));
+    {
+        void* args[] = {&a};
+        CU(cudaLaunchKernel((const void*)h->k_fused, dim3(fused_grid(h, n)), dim3(128), args, 0, h->stream));
+    }
+    CU(cudaEventRecord(h->ev[2], h->stream));
+    h->last_n = n;
+    h->last_tot = tot;
+    return BVP_OK;
+}
+
+// Brings per-instance state and packed solutions of the last solve to the host.
+static bvp_status finish(bvp_handle* h, bvp_results* out) {
+    const int n = h->last_n;
+    const int M = h->L.M;
+    if (!ensure_host(h->h_st, size_t(n) * sizeof(BvpInstState)))
+        return fail(h, BVP_ERR_NOMEM, "pinned allocation failed");
+    CU(cudaMemcpyAsync(h->h_st.p, h->d_st.p, size_t(n) * sizeof(BvpInstState), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
+    float ms0 = 0, ms1 = 0;
+    cudaEventElapsedTime(&ms0, h->ev[0], h->ev[2]);
+    cudaEventElapsedTime(&ms1, h->ev[1], h->ev[2]);
+    h->timing_ms[0] = ms0;
+    h->timing_ms[1] = ms1;
+    const BvpInstState* st = static_cast<const BvpInstState*>(h->h_st.p);
+    h->st.assign(st, st + n);
+    if (!ensure_host(h->h_off, size_t(n + 1) * 8)) return fail(h, BVP_ERR_NOMEM, "pinned allocation failed");
+    int64_t* off = static_cast<int64_t*>(h->h_off.p);
+    off[0] = 0;
+    for (int q = 0; q < n; ++q) off[q + 1] = off[q] + st[q].N;
+    const long long tot_out = off[n];
+    h->offsets.assign(off, off + n + 1);
+    const bool stages = h->opt.want_stages != 0;
+    if (!ensure_dev(h->d_out_mesh, size_t(tot_out) * 8) || !ensure_dev(h->d_out_y, size_t(tot_out) * M * 8) ||
+        !ensure_host(h->h_mesh, size_t(tot_out) * 8) || !ensure_host(h->h_y, size_t(tot_out) * M * 8))
+        return fail(h, BVP_ERR_NOMEM, "output allocation failed");
+    if (stages && (!ensure_dev(h->d_out_K, size_t(tot_out) * h->L.S * M * 8) ||
+                   !ensure_dev(h->d_out_KI, size_t(tot_out) * h->L.NSXA * M * 8) ||
+                   !ensure_host(h->h_K, size_t(tot_out) * h->L.S * M * 8) ||
+                   !ensure_host(h->h_KI, size_t(tot_out) * h->L.NSXA * M * 8)))
+        return fail(h, BVP_ERR_NOMEM, "output allocation failed");
+    CU(cudaMemcpyAsync(h->d_out_off.p, off, size_t(n + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+    {
+        BvpArgs a;
+        fill_args(h, a, n, h->last_tot, 0, static_cast<const double*>(h->d_params.p), nullptr, nullptr, nullptr, nullptr);
+        const long long* oo = static_cast<const long long*>(h->d_out_off.p);
+        double* om = static_cast<double*>(h->d_out_mesh.p);
+        double* oy = static_cast<double*>(h->d_out_y.p);
+        int ws = stages ? 1 : 0;
+        double* oK = static_cast<double*>(h->d_out_K.p);
+        double* oKI = static_cast<double*>(h->d_out_KI.p);
+        void* args[] = {&a, &oo, &om, &oy, &ws, &oK, &oKI};
+        const int blocks = (n * 32 + 255) / 256;
+        CU(cudaLaunchKernel((const void*)h->k_pack, dim3(std::max(1, blocks)), dim3(256), args, 0, h->stream));
+    }
+    CU(cudaMemcpyAsync(h->h_mesh.p, h->d_out_mesh.p, size_t(tot_out) * 8, cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaMemcpyAsync(h->h_y.p, h->d_out_y.p, size_t(tot_out) * M * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (stages) {
+        CU(cudaMemcpyAsync(h->h_K.p, h->d_out_K.p, size_t(tot_out) * h->L.S * M * 8, cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaMemcpyAsync(h->h_KI.p, h->d_out_KI.p, size_t(tot_out) * h->L.NSXA * M * 8, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CU(cudaStreamSynchronize(h->stream));
+    if (out) {
+        for (int q = 0; q < n; ++q) {
+            if (out->retcode) out->retcode[q] = st[q].retcode;
+            if (out->n_nodes) out->n_nodes[q] = st[q].N;
+            if (out->newton_iters) out->newton_iters[q] = st[q].newton_iters;
+            if (out->rounds) out->rounds[q] = st[q].rounds;
+            if (out->defect) out->defect[q] = st[q].defect;
+            if (out->resid) out->resid[q] = st[q].resid;
+        }
+    }
+    h->have_results = true;
+    h->pending_device = false;
+    return BVP_OK;
+}
+
+bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const int32_t* n_intervals,
+                           const double* tspans, int32_t y0_mode, const double* y0, bvp_results* out) {
+    if (!h) return BVP_ERR_INVALID;
+    if (n < 1 || !n_intervals || !tspans || !y0 || (h->desc.n_params > 0 && !params) ||
+        (y0_mode != 0 && y0_mode != 1))
+        return fail(h, BVP_ERR_INVALID, "invalid arguments");
+    const int M = h->L.M;
+    long long tot = 0, y0_vals = 0;
+    for (int q = 0; q < n; ++q) {
+        const int ni = n_intervals[q];
+        if (ni < 1) return fail(h, BVP_ERR_INVALID, "n_intervals must be >= 1");
+        if (!(tspans[2 * q + 1] > tspans[2 * q])) return fail(h, BVP_ERR_INVALID, "tspan must satisfy t0 < t1");
+        tot += std::max(ni, h->opt.max_subintervals) + 1;
+        y0_vals += (y0_mode == 1) ? (long long)(ni + 1) * M : M;
+    }
+    bvp_status s = ensure_arena(h, tot, n, y0_vals);
+    if (s != BVP_OK) return s;
+    const int P = h->desc.n_params;
+    const size_t b_params = size_t(n) * P * 8, b_ni = size_t(n) * 4, b_ts = size_t(n) * 16,
+                 b_y0 = size_t(y0_vals) * 8, b_off = size_t(n) * 8;
+    if (!ensure_host(h->h_in, b_params + b_ni + b_ts + b_y0 + b_off + 64))
+        return fail(h, BVP_ERR_NOMEM, "pinned allocation failed");
+    char* hp = static_cast<char*>(h->h_in.p);
+    // the staging copy is part of the host -> device path
+    std::memcpy(hp, params, b_params);
+    std::memcpy(hp + b_params, n_intervals, b_ni);
+    std::memcpy(hp + b_params + b_ni, tspans, b_ts);
+    std::memcpy(hp + b_params + b_ni + b_ts, y0, b_y0);
+    int64_t* yoff = reinterpret_cast<int64_t*>(hp + b_params + b_ni + b_ts + b_y0);
+    if (y0_mode == 1) {
+        long long acc = 0;
+        for (int q = 0; q < n; ++q) { yoff[q] = acc; acc += n_intervals[q] + 1; }
+    }
+    if (b_params) CU(cudaMemcpyAsync(h->d_params.p, hp, b_params, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_n_init.p, hp + b_params, b_ni, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_tspans.p, hp + b_params + b_ni, b_ts, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_y0.p, hp + b_params + b_ni + b_ts, b_y0, cudaMemcpyHostToDevice, h->stream));
+    if (y0_mode == 1) CU(cudaMemcpyAsync(h->d_y0_off.p, yoff, b_off, cudaMemcpyHostToDevice, h->stream));
+    s = launch_solve(h, n, tot, y0_mode, static_cast<const double*>(h->d_params.p),
+                     static_cast<const int*>(h->d_n_init.p), static_cast<const double*>(h->d_tspans.p),
+                     static_cast<const double*>(h->d_y0.p), static_cast<const long long*>(h->d_y0_off.p));
+    if (s != BVP_OK) return s;
+    return finish(h, out);
+}
+
+bvp_status bvp_solve_batch_device(bvp_handle* h, int32_t n, const double* d_params, const int32_t* d_n_intervals,
+                                  const double* d_tspans, int32_t y0_mode, const double* d_y0,
+                                  const int64_t* d_y0_off, int32_t max_intervals) {
+    if (!h) return BVP_ERR_INVALID;
+    if (n < 1 || !d_n_intervals || !d_tspans || !d_y0 || max_intervals < 1 || (y0_mode == 1 && !d_y0_off))
+        return fail(h, BVP_ERR_INVALID, "invalid arguments");
+    const long long tot = (long long)n * (std::max<int>(max_intervals, h->opt.max_subintervals) + 1);
+    bvp_status s = ensure_arena(h, tot, n, 1);
+    if (s != BVP_OK) return s;
+    const double* dp = d_params ? d_params : static_cast<const double*>(h->d_params.p);
+    s = launch_solve(h, n, tot, y0_mode, dp, d_n_intervals, d_tspans, d_y0,
+                     reinterpret_cast<const long long*>(d_y0_off));
+    if (s != BVP_OK) return s;
+    h->pending_device = true;
+    h->have_results = false;
+    return BVP_OK;
+}
+
+bvp_status bvp_fetch_results(bvp_handle* h, bvp_results* out) {
+    if (!h) return BVP_ERR_INVALID;
+    if (!h->pending_device && !h->have_results) return fail(h, BVP_ERR_STATE, "no solve to fetch");
+    if (h->have_results && !h->pending_device) {
+        if (out) {
+            for (int q = 0; q < h->last_n; ++q) {
+                const BvpInstState& st = h->st[q];
+                if (out->retcode) out->retcode[q] = st.retcode;
+                if (out->n_nodes) out->n_nodes[q] = st.N;
+                if (out->newton_iters) out->newton_iters[q] = st.newton_iters;
+                if (out->rounds) out->rounds[q] = st.rounds;
+                if (out->defect) out->defect[q] = st.defect;
+                if (out->resid) out->resid[q] = st.resid;
+            }
+        }
+        return BVP_OK;
+    }
+    return finish(h, out);
+}
+
+bvp_status bvp_last_timing(bvp_handle* h, double* ms2) {
+    if (!h || !ms2) return BVP_ERR_INVALID;
+    if (h->pending_device) {
+        CU(cudaStreamSynchronize(h->stream));
+        float ms0 = 0, ms1 = 0;
+        cudaEventElapsedTime(&ms0, h->ev[0], h->ev[2]);
+        cudaEventElapsedTime(&ms1, h->ev[1], h->ev[2]);
+        h->timing_ms[0] = ms0;
+        h->timing_ms[1] = ms1;
+    }
+    ms2[0] = h->timing_ms[0];
+    ms2[1] = h->timing_ms[1];
+    return BVP_OK;
+}
+
+bvp_status bvp_get_solution(bvp_handle* h, int32_t inst, double* mesh, double* y, int32_t cap, int32_t* n_nodes) {
+    if (!h) return BVP_ERR_INVALID;
+    if (!h->have_results) return fail(h, BVP_ERR_STATE, "no results");
+    if (inst < 0 || inst >= h->last_n) return fail(h, BVP_ERR_INVALID, "instance out of range");
+    const int64_t o = h->offsets[inst];
+    const int N = int(h->offsets[inst + 1] - o);
+    if (n_nodes) *n_nodes = N;
+    if (cap < N) return fail(h, BVP_ERR_INVALID, "capacity too small");
+    const int M = h->L.M;
+    if (mesh) std::memcpy(mesh, static_cast<const double*>(h->h_mesh.p) + o, size_t(N) * 8);
+    if (y) std::memcpy(y, static_cast<const double*>(h->h_y.p) + o * M, size_t(N) * M * 8);
+    return BVP_OK;
+}
+
+bvp_status bvp_get_packed(bvp_handle* h, const int64_t** offsets, const double** mesh, const double** y,
+                          const double** K, const double** KI) {
+    if (!h) return BVP_ERR_INVALID;
+    if (!h->have_results) return fail(h, BVP_ERR_STATE, "no results");
+    if (offsets) *offsets = h->offsets.data();
+    if (mesh) *mesh = static_cast<const double*>(h->h_mesh.p);
+    if (y) *y = static_cast<const double*>(h->h_y.p);
+    if (K) *K = h->opt.want_stages ? static_cast<const double*>(h->h_K.p) : nullptr;
+    if (KI) *KI = h->opt.want_stages ? static_cast<const double*>(h->h_KI.p) : nullptr;
+    return BVP_OK;
+}
+
+bvp_status bvp_eval_stage(bvp_handle* h, int32_t stage, int32_t n, const double* params, const int32_t* n_nodes,
+                          const double* mesh, const double* y, double* norm, double* F, double* bc_res,
+                          double* K, double* S, double* R, double* delta, double* err) {
+    if (!h) return BVP_ERR_INVALID;
+    if (stage < 0 || stage > 3 || n < 1 || !n_nodes || !mesh || !y || (h->desc.n_params > 0 && !params))
+        return fail(h, BVP_ERR_INVALID, "invalid arguments");
+    const BvpLayout& L = h->L;
+    const int M = L.M, P = h->desc.n_params, js = h->js;
+    std::vector<long long> off(n + 1, 0);
+    std::vector<int> cap(n), order(n);
+    for (int q = 0; q < n; ++q) {
+        if (n_nodes[q] < 2) return fail(h, BVP_ERR_INVALID, "n_nodes must be >= 2");
+        cap[q] = n_nodes[q];
+        off[q + 1] = off[q] + n_nodes[q];
+        order[q] = q;
+    }
+    const long long tot = off[n];
+    bvp_status s = ensure_arena(h, tot, n, 1);
+    if (s != BVP_OK) return s;
+    std::vector<double> hh(size_t(tot), 0.0);
+    std::vector<BvpInstState> st(n);
+    for (int q = 0; q < n; ++q) {
+        for (int i = 0; i + 1 < n_nodes[q]; ++i) hh[off[q] + i] = mesh[off[q] + i + 1] - mesh[off[q] + i];
+        std::memset(&st[q], 0, sizeof(BvpInstState));
+        st[q].N = n_nodes[q];
+    }
+    CU(cudaMemcpyAsync(h->d_mesh.p, mesh, size_t(tot) * 8, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_h.p, hh.data(), size_t(tot) * 8, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_y.p, y, size_t(tot) * M * 8, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_node_off.p, off.data(), size_t(n) * 8, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_cap.p, cap.data(), size_t(n) * 4, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_order.p, order.data(), size_t(n) * 4, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_st.p, st.data(), size_t(n) * sizeof(BvpInstState), cudaMemcpyHostToDevice, h->stream));
+    if (P > 0) CU(cudaMemcpyAsync(h->d_params.p, params, size_t(n) * P * 8, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemsetAsync(h->d_counter.p, 0, 16, h->stream));
+    {
+        long long np = (long long)n * P;
+        const double* src = static_cast<const double*>(h->d_params.p);
+        void* dst = h->d_params_j.p;
+        void* args[] = {&src, &dst, &np};
+        CU(cudaLaunchKernel((const void*)h->k_convert, dim3(64), dim3(256), args, 0, h->stream));
+    }
+    BvpArgs a;
+    fill_args(h, a, n, tot, 0, static_cast<const double*>(h->d_params.p), nullptr, nullptr, nullptr, nullptr);
+    double* dn = static_cast<double*>(h->d_norm.p);
+    int stg = stage;
+    void* args[] = {&a, &stg, &dn};
+    CU(cudaLaunchKernel((const void*)h->k_stage, dim3(fused_grid(h, n)), dim3(128), args, 0, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
+    if (norm) CU(cudaMemcpy(norm, dn, size_t(n) * 8, cudaMemcpyDeviceToHost));
+    if (F) CU(cudaMemcpy(F, h->d_F.p, size_t(tot) * M * 8, cudaMemcpyDeviceToHost));
+    if (K) CU(cudaMemcpy(K, h->d_K.p, size_t(tot) * L.S * M * 8, cudaMemcpyDeviceToHost));
+    if (err) CU(cudaMemcpy(err, h->d_err.p, size_t(tot) * 8, cudaMemcpyDeviceToHost));
+    if (bc_res) {
+        std::vector<double> scr(size_t(n) * L.SCRW);
+        CU(cudaMemcpy(scr.data(), h->d_scr.p, scr.size() * 8, cudaMemcpyDeviceToHost));
+        for (int q = 0; q < n; ++q)
+            for (int m = 0; m < M; ++m) bc_res[q * M + m] = scr[size_t(q) * L.SCRW + L.SCR_BCRES + m];
+    }
+    auto fetch_jt = [&](const DevBuf& b, double* dst, size_t count) -> bvp_status {
+        if (js == 8) {
+            CU(cudaMemcpy(dst, b.p, count * 8, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> tmp(count);
+            CU(cudaMemcpy(tmp.data(), b.p, count * 4, cudaMemcpyDeviceToHost));
+            for (size_t k = 0; k < count; ++k) dst[k] = tmp[k];
+        }
+        return BVP_OK;
+    };
+    if (S && (s = fetch_jt(h->d_Sb, S, size_t(tot) * M * M)) != BVP_OK) return s;
+    if (R && (s = fetch_jt(h->d_Rb, R, size_t(tot) * M * M)) != BVP_OK) return s;
+    if (delta && (s = fetch_jt(h->d_delta, delta, size_t(tot) * M)) != BVP_OK) return s;
+    return BVP_OK;
+}
+
+void bvp_destroy(bvp_handle* h) {
+    if (!h) return;
+    DevBuf* devs[] = {&h->d_mesh, &h->d_h, &h->d_y, &h->d_ybak, &h->d_ybase, &h->d_K, &h->d_KI, &h->d_F,
+                      &h->d_err, &h->d_inc, &h->d_iold, &h->d_Sb, &h->d_Rb, &h->d_rec, &h->d_eq,
+                      &h->d_delta, &h->d_scr, &h->d_iscr, &h->d_st, &h->d_order, &h->d_cap,
+                      &h->d_node_off, &h->d_counter, &h->d_params, &h->d_params_j, &h->d_n_init,
+                      &h->d_tspans, &h->d_y0, &h->d_y0_off, &h->d_out_off, &h->d_out_mesh,
+                      &h->d_out_y, &h->d_out_K, &h->d_out_KI, &h->d_norm};
+    for (DevBuf* b : devs)
+        if (b->p) cudaFree(b->p);
+    HostBuf* hosts[] = {&h->h_in, &h->h_st, &h->h_off, &h->h_mesh, &h->h_y, &h->h_K, &h->h_KI};
+    for (HostBuf* b : hosts)
+        if (b->p) cudaFreeHost(b->p);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->lib) cudaLibraryUnload(h->lib);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+}  // extern "C"

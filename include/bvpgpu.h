@@ -1,0 +1,156 @@
+/* bvpgpu.h — C ABI of the GB300 batched MIRK boundary-value solver (libbvpgpu.so).
+ *
+ * Plain C types only: pointers, sizes and enums. The library owns all device memory,
+ * the JIT-compiled kernels and the CUDA stream; the caller owns every host buffer it
+ * passes in. One handle per host thread; calls on a handle are stream-ordered and
+ * return after their results are on the host (except bvp_solve_batch_device).
+ *
+ * Each entry point names the reference interface it stands in for (paths relative to
+ * the SciML/BoundaryValueDiffEq.jl project).
+ */
+#ifndef BVPGPU_H
+#define BVPGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    BVP_OK = 0,
+    BVP_ERR_INVALID = 1,   /* bad argument: the reference raises ArgumentError (e.g. dt <= 0, Core/src/utils.jl:354) */
+    BVP_ERR_COMPILE = 2,   /* the problem source did not compile (NVRTC log in bvp_last_error) */
+    BVP_ERR_CUDA = 3,      /* a CUDA runtime call failed */
+    BVP_ERR_NOMEM = 4,     /* device or pinned host allocation failed */
+    BVP_ERR_STATE = 5      /* no results available yet / handle misuse */
+} bvp_status;
+
+/* Per-instance return codes, the reference's ReturnCode values of solve! (mirk.jl:293-331). */
+typedef enum {
+    BVP_RET_SUCCESS = 0,
+    BVP_RET_FAILURE = 1,   /* Newton failed beyond the mesh cap, or mesh selection exceeded max_subintervals */
+    BVP_RET_MAXITERS = 2   /* outer (mesh) round cap reached */
+} bvp_retcode;
+
+/* Problem description (the shape part of a BVProblem / TwoPointBVProblem).
+ * Standard problems evaluate the BC on u(bc_t[k]) as the reference's EvalSol does
+ * (lib/BoundaryValueDiffEqMIRK/src/interpolation.jl:214-242); two-point problems give La
+ * residuals at t0 and Lb at t1 (lib/BoundaryValueDiffEqCore/src/utils.jl:157-181). */
+typedef struct {
+    int32_t M;            /* state dimension (1..8 on the warp-per-instance kernels) */
+    int32_t n_params;     /* parameters per instance */
+    int32_t twopoint;     /* 0 standard, 1 two-point */
+    int32_t n_bc_pts;     /* standard: number of evaluation times (1..16) */
+    int32_t La, Lb;       /* two-point: residual counts, La + Lb == M */
+    double bc_t[16];      /* standard: evaluation times */
+} bvp_problem_desc;
+
+/* Solver options; defaults (bvp_default_options) are the reference's:
+ * abstol 1e-6, adaptive, DefectControl(defect_threshold = 0.1), max_num_subintervals 3000
+ * (lib/BoundaryValueDiffEqMIRK/src/mirk.jl:49-53, algorithms.jl:55-61,
+ *  lib/BoundaryValueDiffEqCore/src/calc_errors.jl:54-60). */
+typedef struct {
+    int32_t order;                /* MIRK order: 2, 3, 4, 5 or 6 */
+    int32_t adaptive;             /* 1: defect-controlled mesh refinement */
+    int32_t max_subintervals;     /* mesh cap (reference default 3000) */
+    int32_t max_newton;           /* Newton iterations per attempt */
+    int32_t max_rounds;           /* cap on outer mesh rounds (the reference has none) */
+    int32_t transfer_inplace;     /* 1: the reference's in-place solution transfer (default) */
+    int32_t bc_jac_exact;         /* 0: the reference's BC Jacobian (stages held fixed), 1: exact */
+    int32_t linesearch_fallback;  /* 1: retry a failed Newton with backtracking */
+    int32_t stall_steps;          /* Newton stops after this many non-improving steps */
+    int32_t jac_precision;        /* 32: FP32 Jacobian blocks and factorisation, 64: FP64 */
+    int32_t want_stages;          /* 1: keep K and the interpolant stages for dense output */
+    int32_t reserved;
+    double abstol;
+    double defect_threshold;
+    double divergence_factor;     /* Newton stops when ||F|| exceeds this times its start */
+} bvp_options;
+
+/* Per-instance outputs of a batch (caller-owned arrays of n_inst entries; any may be NULL). */
+typedef struct {
+    int32_t* retcode;
+    int32_t* n_nodes;       /* final mesh points */
+    int32_t* newton_iters;  /* Newton iterations over all rounds */
+    int32_t* rounds;        /* outer mesh rounds */
+    double* defect;         /* last defect norm */
+    double* resid;          /* last ||F||_inf */
+} bvp_results;
+
+typedef struct bvp_handle_s bvp_handle;
+
+/* Defaults of MIRKn() + __init kwargs (algorithms.jl:55-61, mirk.jl:49-53). */
+void bvp_default_options(bvp_options* opt);
+
+/* Setup: replaces SciMLBase.__init(prob::BVProblem, alg::AbstractMIRK; ...)
+ * (lib/BoundaryValueDiffEqMIRK/src/mirk.jl:49-265). The problem source (f and bc as
+ * BVP_F / BVP_BC or BVP_BCA + BVP_BCB bodies) is JIT-compiled once for sm_103a. */
+bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bvp_options* opt,
+                      bvp_handle** out);
+
+/* Batched solve: replaces SciMLBase.solve!(cache::MIRKCache) (mirk.jl:286-332) applied to
+ * every trajectory of an EnsembleProblem (test/Core/ensemble_tests.jl:20-38).
+ *   params      n_inst x n_params (row-major)
+ *   n_intervals initial uniform mesh sizes, cld(t1 - t0, dt) (Core/src/utils.jl:349-363)
+ *   tspans      n_inst x 2 (t0 < t1)
+ *   y0_mode 0:  y0 is n_inst x M, copied to every mesh point (Core/src/utils.jl:766-769)
+ *   y0_mode 1:  y0 holds (n_intervals[i]+1) x M guesses per instance, packed in order
+ *               (the vector-of-arrays initial guess, Core/src/utils.jl:750-765)
+ * Results stay in the handle until the next solve (bvp_get_solution / bvp_get_packed). */
+bvp_status bvp_solve_batch(bvp_handle* h, int32_t n_inst, const double* params,
+                           const int32_t* n_intervals, const double* tspans, int32_t y0_mode,
+                           const double* y0, bvp_results* out);
+
+/* Same solve with inputs already in device memory (device pointers; y0_off is the
+ * per-instance offset, in M-vectors, for y0_mode 1, else NULL). max_intervals bounds
+ * n_intervals. Runs on the handle's stream and returns without synchronising; results
+ * stay on the device (read them with bvp_fetch_results). */
+bvp_status bvp_solve_batch_device(bvp_handle* h, int32_t n_inst, const double* d_params,
+                                  const int32_t* d_n_intervals, const double* d_tspans,
+                                  int32_t y0_mode, const double* d_y0, const int64_t* d_y0_off,
+                                  int32_t max_intervals);
+
+/* Synchronise and bring the results of the last solve to the host. */
+bvp_status bvp_fetch_results(bvp_handle* h, bvp_results* out);
+
+/* Final mesh and solution of instance `inst` of the last batch: the ODESolution the
+ * reference builds (mirk.jl:324-331; Core/src/utils.jl:798-805). cap is the capacity of
+ * mesh (points) and y (points x M). */
+bvp_status bvp_get_solution(bvp_handle* h, int32_t inst, double* mesh, double* y, int32_t cap,
+                            int32_t* n_nodes);
+
+/* Pointers to the packed results of the last batch (valid until the next solve):
+ * instance i occupies points offsets[i] .. offsets[i+1]-1 of mesh / y (x M); with
+ * want_stages, K (s x M per interval) and KI (extra stages x M per interval) use the same
+ * offsets (interval i of instance q at offsets[q] + i). */
+bvp_status bvp_get_packed(bvp_handle* h, const int64_t** offsets, const double** mesh,
+                          const double** y, const double** K, const double** KI);
+
+/* One kernel stage on caller-given meshes and solutions (packed as bvp_get_packed):
+ * stage 0 residual (__mirk_loss!, mirk.jl:471-494), 1 Jacobian blocks
+ * (__mirk_mpoint_jacobian!, mirk.jl:824-838), 2 Newton direction (the linear solve of
+ * NewtonRaphson), 3 defect (error_estimate!, adaptivity.jl:416-461). Outputs (any may be
+ * NULL, packed by node offsets): norm (n_inst), F (collocation residual per interval,
+ * x M), bc_res (n_inst x M), K (per interval, s x M), S and R (per interval, M x M),
+ * delta (per point, x M), err (per interval). */
+bvp_status bvp_eval_stage(bvp_handle* h, int32_t stage, int32_t n_inst, const double* params,
+                          const int32_t* n_nodes, const double* mesh, const double* y,
+                          double* norm, double* F, double* bc_res, double* K, double* S,
+                          double* R, double* delta, double* err);
+
+/* Device time of the last solve's kernels in milliseconds (CUDA events on the handle's
+ * stream): [0] whole solve, [1] fused solve kernel. */
+bvp_status bvp_last_timing(bvp_handle* h, double* ms2);
+
+/* The handle's CUDA stream (cudaStream_t as void*). */
+void* bvp_stream(bvp_handle* h);
+
+const char* bvp_last_error(bvp_handle* h);
+void bvp_destroy(bvp_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BVPGPU_H */
