@@ -21,7 +21,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD = os.path.join(PKG_DIR, "_build")
 INCLUDE = os.path.join(os.path.dirname(PKG_DIR), "include")
 LIB_PATH = os.path.join(BUILD, "libbvpgpu.so")
-EMBED = ("bvp_prelude.cuh", "bvp_kernels.cuh", "bvp_shared.h")
+EMBED = ("bvp_prelude.cuh", "bvp_kernels.cuh", "bvp_shared.h", "bvp_tableau.cuh")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
@@ -143,7 +143,7 @@ class Options(C.Structure):
                 ("max_newton", C.c_int32), ("max_rounds", C.c_int32), ("transfer_inplace", C.c_int32),
                 ("bc_jac_exact", C.c_int32), ("linesearch_fallback", C.c_int32),
                 ("stall_steps", C.c_int32), ("jac_precision", C.c_int32), ("want_stages", C.c_int32),
-                ("reserved", C.c_int32), ("abstol", C.c_double), ("defect_threshold", C.c_double),
+                ("fp32_phase", C.c_int32), ("abstol", C.c_double), ("defect_threshold", C.c_double),
                 ("divergence_factor", C.c_double)]
 
 

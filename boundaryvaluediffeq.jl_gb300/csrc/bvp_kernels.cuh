@@ -8,8 +8,13 @@
 //
 // One warp owns one BVP instance for its whole adaptive solve; a persistent grid of
 // warps pulls instances from an atomic work counter (largest meshes first). The warp's
-// lanes stride over mesh intervals for the per-interval work (residual, Jacobian blocks,
-// defect) and over block pairs for the cyclic-reduction factorisation.
+// lanes split the mesh intervals for the per-interval work (residual, Jacobian blocks,
+// defect) and the block pairs of each cyclic-reduction level.
+//
+// Precision: the residual that decides Newton convergence, the defect, the mesh selection
+// and the solution transfer are FP64. The Jacobian blocks and the factorisation run in
+// BVP_JT. With JT = float the first Newton iterations also use an FP32 residual (GB300's
+// FP32 pipe is far wider than its FP64 pipe); convergence is always decided in FP64.
 //
 // Reference functions restated here (paths relative to the reference project):
 //   Φ residual             lib/BoundaryValueDiffEqMIRK/src/collocation.jl:44-72
@@ -38,6 +43,7 @@
 #ifndef BVP_LA
 #define BVP_LA 0
 #endif
+#include "bvp_tableau.cuh"
 
 #if BVP_TWOPOINT
 template <class T, class P> BVP_DEV void bvp_bc(T*, const T* const*, const P*) {}
@@ -50,16 +56,13 @@ namespace bvp {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int M = BVP_M;
-constexpr int ORD = BVP_ORDER;
-constexpr int S = ORD - 1;
-constexpr int SS = (ORD == 2 || ORD == 3) ? 3 : (ORD == 4 ? 4 : (ORD == 5 ? 6 : 9));
-constexpr int NSX = SS - S;           // extra interpolant stages
-constexpr int NSXA = NSX > 0 ? NSX : 1;
 constexpr int D = 2 * M;              // tangent directions of one interval
 constexpr int NBC = BVP_NBC;
 constexpr int TWOPOINT = BVP_TWOPOINT;
+constexpr int NBCP = TWOPOINT ? 2 : NBC;  // BC evaluation points
 constexpr int LA = BVP_LA;
 using JT = BVP_JT;
+constexpr bool F32_PHASE_OK = sizeof(JT) == 4;
 constexpr int EQW = 2 * M * M + M;    // reduced equation: A (MxM), B (MxM), g (M)
 constexpr int RECW = 3 * M * M + M;   // elimination record: U, X, Y (MxM), g (M)
 constexpr int NBCB = TWOPOINT ? 2 : 2 * NBC;   // BC Jacobian blocks (node, MxM)
@@ -68,163 +71,26 @@ constexpr int NDENSE = KMAX * M;
 
 enum : int { RET_SUCCESS = 0, RET_FAILURE = 1, RET_MAXITERS = 2 };
 
-// ---- MIRK tableaus (mirk_tableaus.jl:13-152), folded at compile time ------------------
-BVP_DEV constexpr double tab_c(int r) {
-    if (ORD == 2) return 0.5;
-    if (ORD == 3) return r == 0 ? 0.0 : 2.0 / 3.0;
-    if (ORD == 4) return r == 0 ? 0.0 : (r == 1 ? 1.0 : 0.5);
-    if (ORD == 5) return r == 0 ? 0.0 : (r == 1 ? 1.0 : (r == 2 ? 0.75 : 0.3));
-    return r == 0 ? 0.0 : (r == 1 ? 1.0 : (r == 2 ? 0.25 : (r == 3 ? 0.75 : 0.5)));
-}
-BVP_DEV constexpr double tab_v(int r) {
-    if (ORD == 2) return 0.5;
-    if (ORD == 3) return r == 0 ? 0.0 : 4.0 / 9.0;
-    if (ORD == 4) return r == 0 ? 0.0 : (r == 1 ? 1.0 : 0.5);
-    if (ORD == 5) return r == 0 ? 0.0 : (r == 1 ? 1.0 : (r == 2 ? 27.0 / 32.0 : 837.0 / 1250.0));
-    return r == 0 ? 0.0 : (r == 1 ? 1.0 : (r == 2 ? 5.0 / 32.0 : (r == 3 ? 27.0 / 32.0 : 0.5)));
-}
-BVP_DEV constexpr double tab_b(int r) {
-    if (ORD == 2) return 1.0;
-    if (ORD == 3) return r == 0 ? 0.25 : 0.75;
-    if (ORD == 4) return r == 2 ? 2.0 / 3.0 : 1.0 / 6.0;
-    if (ORD == 5) return r == 0 ? 5.0 / 54.0 : (r == 1 ? 1.0 / 14.0 : (r == 2 ? 32.0 / 81.0 : 250.0 / 567.0));
-    return r <= 1 ? 7.0 / 90.0 : (r <= 3 ? 16.0 / 45.0 : 2.0 / 15.0);
-}
-BVP_DEV constexpr double tab_x(int r, int j) {
-    if (ORD == 3) return (r == 1 && j == 0) ? 2.0 / 9.0 : 0.0;
-    if (ORD == 4) return r == 2 ? (j == 0 ? 0.125 : (j == 1 ? -0.125 : 0.0)) : 0.0;
-    if (ORD == 5) {
-        if (r == 2) return j == 0 ? 3.0 / 64.0 : (j == 1 ? -9.0 / 64.0 : 0.0);
-        if (r == 3) return j == 0 ? 21.0 / 1000.0 : (j == 1 ? 63.0 / 5000.0 : (j == 2 ? -252.0 / 625.0 : 0.0));
-        return 0.0;
-    }
-    if (ORD == 6) {
-        if (r == 2) return j == 0 ? 9.0 / 64.0 : (j == 1 ? -3.0 / 64.0 : 0.0);
-        if (r == 3) return j == 0 ? 3.0 / 64.0 : (j == 1 ? -9.0 / 64.0 : 0.0);
-        if (r == 4) return j == 0 ? -5.0 / 24.0 : (j == 1 ? 5.0 / 24.0 : (j == 2 ? 2.0 / 3.0 : (j == 3 ? -2.0 / 3.0 : 0.0)));
-        return 0.0;
-    }
-    return 0.0;
-}
-BVP_DEV constexpr double tab_cs(int r) {
-    if (ORD == 2) return r == 0 ? 0.0 : 1.0;
-    if (ORD == 3) return 1.0;
-    if (ORD == 4) return 0.75;
-    if (ORD == 5) return r == 0 ? 0.8 : 13.0 / 23.0;
-    return r == 0 ? 7.0 / 16.0 : (r == 1 ? 3.0 / 8.0 : (r == 2 ? 9.0 / 16.0 : 1.0 / 8.0));
-}
-BVP_DEV constexpr double tab_vs(int r) {
-    if (ORD == 4) return 27.0 / 32.0;
-    return tab_cs(r);
-}
-// x_star[extra r][stage j] (column-major indexing of the reference, interpolation.jl:308-309)
-BVP_DEV constexpr double tab_xs(int r, int j) {
-    if (ORD == 4) return j == 0 ? 3.0 / 64.0 : (j == 1 ? -9.0 / 64.0 : 0.0);
-    if (ORD == 5) {
-        if (r == 0) return j == 0 ? 14.0 / 1125.0 : (j == 1 ? -74.0 / 875.0 : (j == 2 ? -128.0 / 3375.0 : (j == 3 ? 104.0 / 945.0 : 0.0)));
-        return j == 0 ? 0.5 : (j == 1 ? 4508233.0 / 1958887.0 : (j == 2 ? 48720832.0 / 2518569.0 :
-               (j == 3 ? -27646420.0 / 17629983.0 : (j == 4 ? -11517095.0 / 559682.0 : 0.0))));
-    }
-    if (ORD == 6) {
-        if (r == 0) return j == 0 ? 1547.0 / 32768.0 : (j == 1 ? -1225.0 / 32768.0 : (j == 2 ? 749.0 / 4096.0 : (j == 3 ? -287.0 / 2048.0 : (j == 4 ? -861.0 / 16384.0 : 0.0))));
-        if (r == 1) return j == 0 ? 83.0 / 1536.0 : (j == 1 ? -13.0 / 384.0 : (j == 2 ? 283.0 / 1536.0 : (j == 3 ? -167.0 / 1536.0 : (j == 4 ? -49.0 / 512.0 : 0.0))));
-        if (r == 2) return j == 0 ? 1225.0 / 32768.0 : (j == 1 ? -1547.0 / 32768.0 : (j == 2 ? 287.0 / 2048.0 : (j == 3 ? -749.0 / 4096.0 : (j == 4 ? 861.0 / 16384.0 : 0.0))));
-        return j == 0 ? 233.0 / 3456.0 : (j == 1 ? -19.0 / 1152.0 : (j == 5 ? -5.0 / 72.0 : (j == 6 ? 7.0 / 72.0 : (j == 7 ? -17.0 / 216.0 : 0.0))));
-    }
-    return 0.0;
-}
-BVP_DEV constexpr double tau_star() {
-    return ORD == 2 ? 0.25 : (ORD == 3 ? 0.25 : (ORD == 4 ? 0.226 : (ORD == 5 ? 0.3 : 0.7156)));
-}
-
-// continuous-extension weights and derivatives (interpolation.jl:459-580)
-BVP_DEV void interp_weights(double t, double* w, double* wp) {
-    const double t2 = t * t, t3 = t2 * t, t4 = t3 * t, t5 = t4 * t, t6 = t5 * t;
-    if (ORD == 2) {
-        w[0] = 0; w[1] = t * (1 - t / 2); w[2] = t2 / 2;
-        wp[0] = 0; wp[1] = 1 - t; wp[2] = t;
-    } else if (ORD == 3) {
-        w[0] = t / 4.0 * (2.0 * t2 - 5.0 * t + 4.0);
-        w[1] = -3.0 / 4.0 * t2 * (2.0 * t - 3.0);
-        w[2] = t2 * (t - 1.0);
-        wp[0] = 3.0 / 2.0 * (t - 2.0 / 3.0) * (t - 1.0);
-        wp[1] = -9.0 / 2.0 * t * (t - 1.0);
-        wp[2] = 3.0 * t * (t - 2.0 / 3.0);
-    } else if (ORD == 4) {
-        const double tm1 = t - 1.0, t4m3 = t * 4.0 - 3.0, t2m1 = t * 2.0 - 1.0;
-        w[0] = -t * (2.0 * t - 3.0) * (2.0 * t2 - 3.0 * t + 2.0) / 6.0;
-        w[1] = t2 * (12.0 * t2 - 20.0 * t + 9.0) / 6.0;
-        w[2] = 2.0 * t2 * (6.0 * t2 - 14.0 * t + 9.0) / 3.0;
-        w[3] = -16.0 * t2 * tm1 * tm1 / 3.0;
-        wp[0] = -tm1 * t4m3 * t2m1 / 3.0;
-        wp[1] = t * t2m1 * t4m3;
-        wp[2] = 4.0 * t * t4m3 * tm1;
-        wp[3] = -32.0 * t * t2m1 * tm1 / 3.0;
-    } else if (ORD == 5) {
-        w[0] = t * (22464.0 - 83910.0 * t + 143041.0 * t2 - 113808.0 * t3 + 33256.0 * t4) / 22464.0;
-        w[1] = t2 * (-2418.0 + 12303.0 * t - 19512.0 * t2 + 10904.0 * t3) / 3360.0;
-        w[2] = -8.0 / 81.0 * t2 * (-78.0 + 209.0 * t - 204.0 * t2 + 8.0 * t3);
-        w[3] = -25.0 / 1134.0 * t2 * (-390.0 + 1045.0 * t - 1020.0 * t2 + 328.0 * t3);
-        w[4] = -25.0 / 5184.0 * t2 * (390.0 + 255.0 * t - 1680.0 * t2 + 2072.0 * t3);
-        w[5] = 279841.0 / 168480.0 * t2 * (-6.0 + 21.0 * t - 24.0 * t2 + 8.0 * t3);
-        wp[0] = 1.0 - 13985.0 / 1872.0 * t + 143041.0 / 7488.0 * t2 - 2371.0 / 117.0 * t3 + 20785.0 / 2808.0 * t4;
-        wp[1] = -403.0 / 280.0 * t + 12303.0 / 1120.0 * t2 - 813.0 / 35.0 * t3 + 1363.0 / 84.0 * t4;
-        wp[2] = 416.0 / 27.0 * t - 1672.0 / 27.0 * t2 + 2176.0 / 27.0 * t3 - 320.0 / 81.0 * t4;
-        wp[3] = 3250.0 / 189.0 * t - 26125.0 / 378.0 * t2 + 17000.0 / 189.0 * t3 - 20500.0 / 567.0 * t4;
-        wp[4] = -1625.0 / 432.0 * t - 2125.0 / 576.0 * t2 + 875.0 / 27.0 * t3 - 32375.0 / 648.0 * t4;
-        wp[5] = -279841.0 / 14040.0 * t + 1958887.0 / 18720.0 * t2 - 279841.0 / 1755.0 * t3 + 279841.0 / 4212.0 * t4;
-    } else {
-        w[0] = t - 28607.0 / 7434.0 * t2 - 166210.0 / 33453.0 * t3 + 334780.0 / 11151.0 * t4 -
-               1911296.0 / 55755.0 * t5 + 406528.0 / 33453.0 * t6;
-        w[1] = 777.0 / 590.0 * t2 - 2534158.0 / 234171.0 * t3 + 2088580.0 / 78057.0 * t4 -
-               10479104.0 / 390285.0 * t5 + 11328512.0 / 1170855.0 * t6;
-        w[2] = -1008.0 / 59.0 * t2 + 222176.0 / 1593.0 * t3 - 180032.0 / 531.0 * t4 +
-               876544.0 / 2655.0 * t5 - 180224.0 / 1593.0 * t6;
-        w[3] = w[2];
-        w[4] = -378.0 / 59.0 * t2 + 27772.0 / 531.0 * t3 - 22504.0 / 177.0 * t4 +
-               109568.0 / 885.0 * t5 - 22528.0 / 531.0 * t6;
-        w[5] = -95232.0 / 413.0 * t2 + 62384128.0 / 33453.0 * t3 - 49429504.0 / 11151.0 * t4 +
-               46759936.0 / 11151.0 * t5 - 46661632.0 / 33453.0 * t6;
-        w[6] = 896.0 / 5.0 * t2 - 4352.0 / 3.0 * t3 + 3456.0 * t4 - 16384.0 / 5.0 * t5 + 16384.0 / 15.0 * t6;
-        w[7] = 50176.0 / 531.0 * t2 - 179554304.0 / 234171.0 * t3 + 143363072.0 / 78057.0 * t4 -
-               136675328.0 / 78057.0 * t5 + 137363456.0 / 234171.0 * t6;
-        w[8] = 16384.0 / 441.0 * t3 - 16384.0 / 147.0 * t4 + 16384.0 / 147.0 * t5 - 16384.0 / 441.0 * t6;
-        wp[0] = 1 - 28607.0 / 3717.0 * t - 166210.0 / 11151.0 * t2 + 1339120.0 / 11151.0 * t3 -
-                1911296.0 / 11151.0 * t4 + 813056.0 / 11151.0 * t5;
-        wp[1] = 777.0 / 295.0 * t - 2534158.0 / 78057.0 * t2 + 8354320.0 / 78057.0 * t3 -
-                10479104.0 / 78057.0 * t4 + 22657024.0 / 390285.0 * t5;
-        wp[2] = -2016.0 / 59.0 * t + 222176.0 / 531.0 * t2 - 720128.0 / 531.0 * t3 +
-                876544.0 / 531.0 * t4 - 360448.0 / 531.0 * t5;
-        wp[3] = wp[2];
-        wp[4] = -756.0 / 59.0 * t + 27772.0 / 177.0 * t2 - 90016.0 / 177.0 * t3 +
-                109568.0 / 177.0 * t4 - 45056.0 / 177.0 * t5;
-        wp[5] = -190464.0 / 413.0 * t + 62384128.0 / 11151.0 * t2 - 197718016.0 / 11151.0 * t3 +
-                233799680.0 / 11151.0 * t4 - 93323264.0 / 11151.0 * t5;
-        wp[6] = 1792.0 / 5.0 * t - 4352.0 * t2 + 13824.0 * t3 - 16384.0 * t4 + 32768.0 / 5.0 * t5;
-        wp[7] = 100352.0 / 531.0 * t - 179554304.0 / 78057.0 * t2 + 573452288.0 / 78057.0 * t3 -
-                683376640.0 / 78057.0 * t4 + 274726912.0 / 78057.0 * t5;
-        wp[8] = 16384.0 / 147.0 * t2 - 65536.0 / 147.0 * t3 + 81920.0 / 147.0 * t4 - 32768.0 / 147.0 * t5;
-    }
-}
-
 // ---- launch arguments (shared with the host runtime) ------------------------------------
 using InstState = BvpInstState;
 using Args = BvpArgs;
 
 // per-instance scratch layout (doubles), the same formulas as bvp_make_layout()
-constexpr int SCR_BCRES = 0;                         // M
-constexpr int SCR_BCBLK = SCR_BCRES + M;             // NBCB x M x M
-constexpr int SCR_SEG = SCR_BCBLK + NBCB * M * M;    // (KMAX-1) x EQW
-constexpr int SCR_DENSE = SCR_SEG + (KMAX - 1) * EQW;  // NDENSE x NDENSE
-constexpr int SCR_RHS = SCR_DENSE + NDENSE * NDENSE;   // NDENSE
-constexpr int SCRW = SCR_RHS + NDENSE;
+constexpr int SCR_BCRES = 0;                           // M        BC residual (FP64)
+constexpr int SCR_BCBLK = SCR_BCRES + M;               // NBCB x M x M  BC Jacobian blocks
+constexpr int SCR_SEG = SCR_BCBLK + NBCB * M * M;      // (KMAX-1) x EQW segment relations (JT)
+constexpr int SCR_DENSE = SCR_SEG + (KMAX - 1) * EQW;  // NDENSE x NDENSE separator system (JT)
+constexpr int SCR_RHS = SCR_DENSE + NDENSE * NDENSE;   // NDENSE (JT)
+constexpr int SCR_UA = SCR_RHS + NDENSE;               // NBCP x M  u at the BC points (FP64)
+constexpr int SCRW = SCR_UA + NBCP * M;
 // int scratch
-constexpr int ISCR_NK = 0;                 // kept count
-constexpr int ISCR_KEPT = 1;               // KMAX kept nodes
-constexpr int ISCR_NB = ISCR_KEPT + KMAX;  // number of BC blocks
-constexpr int ISCR_BNODE = ISCR_NB + 1;    // NBCB block nodes
-constexpr int ISCRW = ISCR_BNODE + NBCB;
-
+constexpr int ISCR_NK = 0;                   // kept count
+constexpr int ISCR_KEPT = 1;                 // KMAX kept nodes
+constexpr int ISCR_NB = ISCR_KEPT + KMAX;    // number of BC blocks
+constexpr int ISCR_BNODE = ISCR_NB + 1;      // NBCB block nodes
+constexpr int ISCR_UNODE = ISCR_BNODE + NBCB;  // NBCP: node each BC point maps to
+constexpr int ISCR_UIN = ISCR_UNODE + NBCP;    // NBCP: 1 if the point is interior
+constexpr int ISCRW = ISCR_UIN + NBCP;
 
 // ---- warp helpers ------------------------------------------------------------------------
 BVP_DEV int lane_id() { return threadIdx.x & 31; }
@@ -239,6 +105,7 @@ BVP_DEV double warp_sum(double v) {
     return v;
 }
 BVP_DEV bool warp_any(bool b) { return __any_sync(FULL, b) != 0; }
+BVP_DEV double dinf() { return __longlong_as_double(0x7ff0000000000000LL); }
 
 // lower_bound(mesh, t) - 1 clamped to [0, N-2]: the reference's interval()
 // (lib/BoundaryValueDiffEqCore/src/utils.jl:119-121)
@@ -267,14 +134,45 @@ struct Inst {
 BVP_DEV double* mesh_of(const Args& a, const Inst& I, int b) { return a.mesh + b * a.tot + I.nb; }
 BVP_DEV double* h_of(const Args& a, const Inst& I, int b) { return a.h + b * a.tot + I.nb; }
 BVP_DEV double* y_of(const Args& a, const Inst& I, int b) { return a.y + (b * a.tot + I.nb) * M; }
+BVP_DEV JT* yj_of(const Args& a, const Inst& I) { return a.yj + I.nb * M; }
+
+// parameters and iterate in the residual's precision R (R = float only when JT = float)
+template <class R> BVP_DEV const R* params_as(const Inst& I) {
+    if constexpr (sizeof(R) == 8) return reinterpret_cast<const R*>(I.p);
+    else return reinterpret_cast<const R*>(I.pj);
+}
+template <class R> BVP_DEV R y_at(const Args& a, const Inst& I, int k) {
+    if constexpr (sizeof(R) == 8) return y_of(a, I, I.cur)[k];
+    else return R(yj_of(a, I)[k]);
+}
+
+// MIRK4/5/6 put their first two stages on the mesh nodes (c = v = 0 and c = v = 1, no x
+// terms): K_1 of interval i is f(y_i, t_i) and K_2 is f(y_{i+1}, t_{i+1}), which is K_1 of
+// interval i+1. The residual evaluates each node once and shares it between neighbours
+// (the reference evaluates it twice, collocation.jl:60-66).
+constexpr bool NODE_SHARE = S >= 2 && ORD >= 4;
 
 // ---- Φ for one interval (collocation.jl:44-72) ------------------------------------------
+// With `node` non-null and NODE_SHARE, stage 0 is taken from node[] (f at the left node)
+// and stage 1 is evaluated at the right node with t = t_{i+1} and written back to node[].
 template <class T, class PT>
-BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, double ti, double hi_d) {
+BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, double ti, double hi_d,
+                          T* node = nullptr, double ti1 = 0.0) {
     const PT hi = PT(hi_d);
     T Y[M];
 #pragma unroll
     for (int r = 0; r < S; ++r) {
+        if (NODE_SHARE && r == 0 && node) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) Ki[m] = node[m];
+            continue;
+        }
+        if (NODE_SHARE && r == 1 && node) {
+            bvp_f<T, PT>(&Ki[M], yi1, p, PT(ti1));
+#pragma unroll
+            for (int m = 0; m < M; ++m) node[m] = Ki[M + m];
+            continue;
+        }
 #pragma unroll
         for (int m = 0; m < M; ++m) Y[m] = PT(1.0 - tab_v(r)) * yi[m] + PT(tab_v(r)) * yi1[m];
 #pragma unroll
@@ -316,8 +214,8 @@ BVP_DEV void interp_stages(const T* yi, const T* yi1, const T* Ki, T* KIi, const
 }
 
 // z = y_i + h (Σ w_r K_r + Σ w_{s+q} KI_q)
-template <class T>
-BVP_DEV void sum_stages(const double* w, const T* yi, const T* Ki, const T* KIi, double hi, T* z) {
+template <class T, class W>
+BVP_DEV void sum_stages(const W* w, const T* yi, const T* Ki, const T* KIi, W hi, T* z) {
 #pragma unroll
     for (int m = 0; m < M; ++m) {
         T acc = Ki[m] * w[0];
@@ -329,100 +227,140 @@ BVP_DEV void sum_stages(const double* w, const T* yi, const T* Ki, const T* KIi,
     }
 }
 
-// EvalSol u(t) of the current iterate (interpolation.jl:214-242); lane-local.
-// Returns the node the reference attributes the BC Jacobian to; *interior set for
-// points strictly inside the mesh.
-BVP_DEV int eval_sol(const Args& a, const Inst& I, double t, double* z, bool* interior) {
+// EvalSol u(t) of the current iterate in precision R (interpolation.jl:214-242); one lane.
+// Returns the node the reference attributes the BC Jacobian to (the exact endpoint, else
+// the interval's left node); *interior is set for points strictly inside the mesh.
+// With R = double the interval's stages come from K (written by the FP64 residual);
+// with R = float they are recomputed.
+template <class R>
+BVP_DEV int eval_sol(const Args& a, const Inst& I, double t, R* z, bool* interior) {
     const double* mesh = mesh_of(a, I, I.cur);
     const double* h = h_of(a, I, I.cur);
-    const double* y = y_of(a, I, I.cur);
     const int N = I.N;
     if (t == mesh[0]) {
 #pragma unroll
-        for (int m = 0; m < M; ++m) z[m] = y[m];
+        for (int m = 0; m < M; ++m) z[m] = y_at<R>(a, I, m);
         *interior = false; return 0;
     }
     if (t == mesh[N - 1]) {
 #pragma unroll
-        for (int m = 0; m < M; ++m) z[m] = y[(N - 1) * M + m];
+        for (int m = 0; m < M; ++m) z[m] = y_at<R>(a, I, (N - 1) * M + m);
         *interior = false; return N - 1;
     }
     const int ii = interval_of(mesh, N, t);
-    const double tau = (t - mesh[ii]) / h[ii];
-    double w[SS], wp[SS];
-    interp_weights(tau, w, wp);
-    double yi[M], yi1[M], Ki[S * M], KIi[NSXA * M];
+    const R tau = R((t - mesh[ii]) / h[ii]);
+    R w[SS], wp[SS];
+    interp_weights<R>(tau, w, wp);
+    R yi[M], yi1[M], Ki[S * M], KIi[NSXA * M], ri[M];
 #pragma unroll
-    for (int m = 0; m < M; ++m) { yi[m] = y[ii * M + m]; yi1[m] = y[(ii + 1) * M + m]; }
-    const double* Kg = a.K + (I.nb + ii) * (S * M);
+    for (int m = 0; m < M; ++m) { yi[m] = y_at<R>(a, I, ii * M + m); yi1[m] = y_at<R>(a, I, (ii + 1) * M + m); }
+    const R* pr = params_as<R>(I);
+    if constexpr (sizeof(R) == 8) {
+        const double* Kg = a.K + (I.nb + ii) * (S * M);
 #pragma unroll
-    for (int k = 0; k < S * M; ++k) Ki[k] = Kg[k];
-    interp_stages<double, double>(yi, yi1, Ki, KIi, I.p, mesh[ii], h[ii]);
-    sum_stages<double>(w, yi, Ki, KIi, h[ii], z);
+        for (int k = 0; k < S * M; ++k) Ki[k] = Kg[k];
+    } else {
+        phi_interval<R, R>(yi, yi1, Ki, ri, pr, mesh[ii], h[ii]);
+    }
+    interp_stages<R, R>(yi, yi1, Ki, KIi, pr, mesh[ii], h[ii]);
+    sum_stages<R, R>(w, yi, Ki, KIi, R(h[ii]), z);
     *interior = true;
     return ii;
 }
 
 // ---- K1: residual and stages (warp). Returns ||F||_inf (+inf if non-finite). -----------
+// R is the precision of the stage evaluations and the residual assembly: double for the
+// Newton residual that decides convergence (writes K and F in FP64), float for the early
+// Newton iterations of the mixed-precision path (writes only the FP32 right-hand side).
+// Each lane owns a contiguous block of intervals so node stages pass between neighbours
+// in registers. Lane 0 then evaluates the BCs and caches u at the BC points.
+template <class R = double>
 BVP_DEV double residual(const Args& a, const Inst& I) {
     const int lane = lane_id();
     const double* mesh = mesh_of(a, I, I.cur);
     const double* h = h_of(a, I, I.cur);
-    const double* y = y_of(a, I, I.cur);
+    const R* pr = params_as<R>(I);
     double mx = 0.0;
+    R mxr = R(0);
     bool bad = false;
-    for (int i = lane; i < I.N - 1; i += 32) {
-        double yi[M], yi1[M], Ki[S * M], ri[M];
+    const int nI = I.N - 1;
+    const int per = (nI + 31) >> 5;
+    const int i0 = lane * per;
+    const int i1 = min(i0 + per, nI);
+    R node[M];
+    if (NODE_SHARE && i0 < i1) {
+        R y0v[M];
 #pragma unroll
-        for (int m = 0; m < M; ++m) { yi[m] = y[i * M + m]; yi1[m] = y[(i + 1) * M + m]; }
-        phi_interval<double, double>(yi, yi1, Ki, ri, I.p, mesh[i], h[i]);
-        double* Kg = a.K + (I.nb + i) * (S * M);
+        for (int m = 0; m < M; ++m) y0v[m] = y_at<R>(a, I, i0 * M + m);
+        bvp_f<R, R>(node, y0v, pr, R(mesh[i0]));
+    }
+    for (int i = i0; i < i1; ++i) {
+        R yi[M], yi1[M], Ki[S * M], ri[M];
 #pragma unroll
-        for (int k = 0; k < S * M; ++k) Kg[k] = Ki[k];
-        double* Fg = a.F + (I.nb + i) * M;
+        for (int m = 0; m < M; ++m) { yi[m] = y_at<R>(a, I, i * M + m); yi1[m] = y_at<R>(a, I, (i + 1) * M + m); }
+        phi_interval<R, R>(yi, yi1, Ki, ri, pr, mesh[i], h[i], NODE_SHARE ? node : nullptr, mesh[i + 1]);
+        JT* Fj = a.Fj + (I.nb + i) * M;
+        if constexpr (sizeof(R) == 8) {
+            double* Kg = a.K + (I.nb + i) * (S * M);
+#pragma unroll
+            for (int k = 0; k < S * M; ++k) Kg[k] = Ki[k];
+            double* Fg = a.F + (I.nb + i) * M;
+#pragma unroll
+            for (int m = 0; m < M; ++m) Fg[m] = ri[m];
+        }
 #pragma unroll
         for (int m = 0; m < M; ++m) {
-            Fg[m] = ri[m];
+            Fj[m] = JT(ri[m]);
             bad |= !isfinite(ri[m]);
-            mx = fmax(mx, fabs(ri[m]));
+            mxr = fmax(mxr, fabs(ri[m]));
         }
     }
+    mx = double(mxr);
     __syncwarp();
     if (lane == 0) {
-        double res[M];
+        R res[M];
 #pragma unroll
-        for (int m = 0; m < M; ++m) res[m] = 0.0;
+        for (int m = 0; m < M; ++m) res[m] = R(0);
+        double* ua_c = I.scr + SCR_UA;
         if (TWOPOINT) {
-            double ra[M], rb[M];
-            bvp_bca<double, double>(ra, y, I.p);
-            bvp_bcb<double, double>(rb, y + (I.N - 1) * M, I.p);
+            R ya[M], yb[M], ra[M], rb[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) { ya[m] = y_at<R>(a, I, m); yb[m] = y_at<R>(a, I, (I.N - 1) * M + m); }
+            bvp_bca<R, R>(ra, ya, pr);
+            bvp_bcb<R, R>(rb, yb, pr);
             for (int k = 0; k < LA; ++k) res[k] = ra[k];
             for (int k = LA; k < M; ++k) res[k] = rb[k - LA];
+            for (int m = 0; m < M; ++m) { ua_c[m] = double(ya[m]); ua_c[M + m] = double(yb[m]); }
+            I.iscr[ISCR_UNODE] = 0; I.iscr[ISCR_UNODE + 1] = I.N - 1;
+            I.iscr[ISCR_UIN] = 0; I.iscr[ISCR_UIN + 1] = 0;
         } else {
-            double ua[NBC * M];
-            const double* ptrs[NBC];
+            R ua[NBC * M];
+            const R* ptrs[NBC];
 #pragma unroll
             for (int k = 0; k < NBC; ++k) {
                 bool in;
-                eval_sol(a, I, a.bc_t[k], &ua[k * M], &in);
+                const int nd = eval_sol<R>(a, I, a.bc_t[k], &ua[k * M], &in);
                 ptrs[k] = &ua[k * M];
+                I.iscr[ISCR_UNODE + k] = nd;
+                I.iscr[ISCR_UIN + k] = in ? 1 : 0;
             }
-            bvp_bc<double, double>(res, ptrs, I.p);
+            bvp_bc<R, R>(res, ptrs, pr);
+            for (int k = 0; k < NBC * M; ++k) ua_c[k] = double(ua[k]);
         }
 #pragma unroll
         for (int m = 0; m < M; ++m) {
-            I.scr[SCR_BCRES + m] = res[m];
+            I.scr[SCR_BCRES + m] = double(res[m]);
             bad |= !isfinite(res[m]);
-            mx = fmax(mx, fabs(res[m]));
+            mx = fmax(mx, fabs(double(res[m])));
         }
     }
     __syncwarp();
     mx = warp_max(mx);
     bad = warp_any(bad);
-    return bad ? __longlong_as_double(0x7ff0000000000000LL) : mx;
+    return bad ? dinf() : mx;
 }
 
-// Σ F² over the full residual (for the line search)
+// Σ F² over the full FP64 residual (for the line search)
 BVP_DEV double residual_sq(const Args& a, const Inst& I) {
     const int lane = lane_id();
     double s = 0.0;
@@ -439,7 +377,8 @@ BVP_DEV double residual_sq(const Args& a, const Inst& I) {
 }
 
 // ---- K2: Jacobian blocks (warp) ------------------------------------------------------------
-// S_i = ∂r_i/∂y_i and R_i = ∂r_i/∂y_{i+1} by forward mode with 2M tangents in JT.
+// S_i = ∂r_i/∂y_i and R_i = ∂r_i/∂y_{i+1} by forward mode with 2M tangents in JT, from the
+// JT copy of the iterate. BC rows use u at the BC points cached by the last residual.
 BVP_DEV void add_bc_block(const Inst& I, int node, const double* G) {
     int nb = I.iscr[ISCR_NB];
     for (int k = 0; k < nb; ++k)
@@ -458,13 +397,13 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
     const int lane = lane_id();
     const double* mesh = mesh_of(a, I, I.cur);
     const double* h = h_of(a, I, I.cur);
-    const double* y = y_of(a, I, I.cur);
+    const JT* yj = yj_of(a, I);
     for (int i = lane; i < I.N - 1; i += 32) {
         DI yi[M], yi1[M], Ki[S * M], ri[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) {
-            yi[m] = DI(JT(y[i * M + m])); yi[m].d[m] = JT(1);
-            yi1[m] = DI(JT(y[(i + 1) * M + m])); yi1[m].d[M + m] = JT(1);
+            yi[m] = DI(yj[i * M + m]); yi[m].d[m] = JT(1);
+            yi1[m] = DI(yj[(i + 1) * M + m]); yi1[m].d[M + m] = JT(1);
         }
         phi_interval<DI, JT>(yi, yi1, Ki, ri, I.pj, mesh[i], h[i]);
         JT* Sg = a.Sb + (I.nb + i) * (M * M);
@@ -480,33 +419,26 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
     if (lane == 0) {
         I.iscr[ISCR_NB] = 0;
         double G[M * M];
+        const double* ua_c = I.scr + SCR_UA;
         if (TWOPOINT) {
             DU ua[M], ra[M];
-            for (int m = 0; m < M; ++m) { ua[m] = DU(JT(y[m])); ua[m].d[m] = JT(1); }
+            for (int m = 0; m < M; ++m) { ua[m] = DU(JT(ua_c[m])); ua[m].d[m] = JT(1); }
             bvp_bca<DU, JT>(ra, ua, I.pj);
             for (int q = 0; q < M * M; ++q) G[q] = 0.0;
             for (int r = 0; r < LA; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(ra[r].d[c]);
             add_bc_block(I, 0, G);
-            for (int m = 0; m < M; ++m) { ua[m] = DU(JT(y[(I.N - 1) * M + m])); ua[m].d[m] = JT(1); }
+            for (int m = 0; m < M; ++m) { ua[m] = DU(JT(ua_c[M + m])); ua[m].d[m] = JT(1); }
             bvp_bcb<DU, JT>(ra, ua, I.pj);
             for (int q = 0; q < M * M; ++q) G[q] = 0.0;
             for (int r = LA; r < M; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(ra[r - LA].d[c]);
             add_bc_block(I, I.N - 1, G);
         } else {
-            double uav[NBC * M];
-            int node[NBC];
-            bool inter[NBC];
-            for (int k = 0; k < NBC; ++k) {
-                bool in;
-                node[k] = eval_sol(a, I, a.bc_t[k], &uav[k * M], &in);
-                inter[k] = in;
-            }
             for (int k = 0; k < NBC; ++k) {
                 DU ua[NBC * M];
                 const DU* ptrs[NBC];
                 for (int qq = 0; qq < NBC; ++qq) {
                     for (int m = 0; m < M; ++m) {
-                        ua[qq * M + m] = DU(JT(uav[qq * M + m]));
+                        ua[qq * M + m] = DU(JT(ua_c[qq * M + m]));
                         if (qq == k) ua[qq * M + m].d[m] = JT(1);
                     }
                     ptrs[qq] = &ua[qq * M];
@@ -514,24 +446,25 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
                 DU res[M];
                 bvp_bc<DU, JT>(res, ptrs, I.pj);
                 for (int r = 0; r < M; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(res[r].d[c]);
-                if (!inter[k] || !a.bc_jac_exact) {
+                const int node = I.iscr[ISCR_UNODE + k];
+                if (!I.iscr[ISCR_UIN + k] || !a.bc_jac_exact) {
                     // the interpolant's stages are held at their primal values: du(t)/dy = I
                     // on the interval's left node (interpolation.jl:214-242, mirk.jl:565-572)
-                    add_bc_block(I, node[k], G);
+                    add_bc_block(I, node, G);
                 } else {
                     // exact: chain through the interval's stages and extra stages
-                    const int ii = node[k];
-                    const double tau = (a.bc_t[k] - mesh[ii]) / h[ii];
-                    double w[SS], wp[SS];
-                    interp_weights(tau, w, wp);
+                    const int ii = node;
+                    const JT tau = JT((a.bc_t[k] - mesh[ii]) / h[ii]);
+                    JT w[SS], wp[SS];
+                    interp_weights<JT>(tau, w, wp);
                     DI yi[M], yi1[M], Ki[S * M], KIi[NSXA * M], ri[M], z[M];
                     for (int m = 0; m < M; ++m) {
-                        yi[m] = DI(JT(y[ii * M + m])); yi[m].d[m] = JT(1);
-                        yi1[m] = DI(JT(y[(ii + 1) * M + m])); yi1[m].d[M + m] = JT(1);
+                        yi[m] = DI(yj[ii * M + m]); yi[m].d[m] = JT(1);
+                        yi1[m] = DI(yj[(ii + 1) * M + m]); yi1[m].d[M + m] = JT(1);
                     }
                     phi_interval<DI, JT>(yi, yi1, Ki, ri, I.pj, mesh[ii], h[ii]);
                     interp_stages<DI, JT>(yi, yi1, Ki, KIi, I.pj, mesh[ii], h[ii]);
-                    sum_stages<DI>(w, yi, Ki, KIi, h[ii], z);
+                    sum_stages<DI, JT>(w, yi, Ki, KIi, JT(h[ii]), z);
                     double JL[M * M], JR[M * M];
                     for (int r = 0; r < M; ++r)
                         for (int c = 0; c < M; ++c) {
@@ -554,7 +487,6 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
         kept[nk++] = I.N - 1;
         const int nb = I.iscr[ISCR_NB];
         for (int k = 0; k < nb; ++k) kept[nk++] = I.iscr[ISCR_BNODE + k];
-        // insertion sort + unique
         for (int u = 1; u < nk; ++u) {
             const int v = kept[u];
             int w2 = u - 1;
@@ -574,16 +506,16 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
 // Block cyclic reduction with partial pivoting over each segment between separator
 // nodes: pairs of neighbouring block rows eliminate their shared node (Gaussian
 // elimination with row pivoting on that node's 2M x M column block), halving the
-// segment at each level. The separator system is solved densely in FP64 and the
-// eliminated nodes are recovered level by level.
+// segment at each level. The separator system is solved densely and the eliminated nodes
+// are recovered level by level.
 BVP_DEV void load_eq0(const Args& a, const Inst& I, int i, JT* A, JT* B, JT* g) {
     const JT* Sg = a.Sb + (I.nb + i) * (M * M);
     const JT* Rg = a.Rb + (I.nb + i) * (M * M);
-    const double* Fg = a.F + (I.nb + i) * M;
+    const JT* Fg = a.Fj + (I.nb + i) * M;
 #pragma unroll
     for (int q = 0; q < M * M; ++q) { A[q] = Sg[q]; B[q] = Rg[q]; }
 #pragma unroll
-    for (int m = 0; m < M; ++m) g[m] = JT(-Fg[m]);
+    for (int m = 0; m < M; ++m) g[m] = -Fg[m];
 }
 BVP_DEV void load_eq(const JT* src, JT* A, JT* B, JT* g) {
 #pragma unroll
@@ -657,16 +589,17 @@ BVP_DEV bool eliminate_pair(const JT* Al, const JT* Bl, const JT* gl, const JT* 
     return ok;
 }
 
-// reduce segment [na, nb]; its final relation A δ_na + B δ_nb = g goes to seg (FP64)
-BVP_DEV bool bcr_segment(const Args& a, const Inst& I, int na, int nbn, double* seg) {
+BVP_DEV JT* seg_of(const Inst& I, int j) { return reinterpret_cast<JT*>(I.scr + SCR_SEG) + j * EQW; }
+
+// reduce segment [na, nb]; its final relation A δ_na + B δ_nb = g goes to seg_of(j)
+BVP_DEV bool bcr_segment(const Args& a, const Inst& I, int na, int nbn, JT* seg) {
     const int lane = lane_id();
     const int m = nbn - na;
     JT A[M * M], B[M * M], g[M];
     if (m == 1) {
         if (lane == 0) {
             load_eq0(a, I, na, A, B, g);
-            for (int q = 0; q < M * M; ++q) { seg[q] = double(A[q]); seg[M * M + q] = double(B[q]); }
-            for (int r = 0; r < M; ++r) seg[2 * M * M + r] = double(g[r]);
+            store_eq(seg, A, B, g);
         }
         __syncwarp();
         return true;
@@ -703,8 +636,7 @@ BVP_DEV bool bcr_segment(const Args& a, const Inst& I, int na, int nbn, double* 
     }
     if (lane == 0) {
         load_eq(eqb[buf], A, B, g);
-        for (int q = 0; q < M * M; ++q) { seg[q] = double(A[q]); seg[M * M + q] = double(B[q]); }
-        for (int r = 0; r < M; ++r) seg[2 * M * M + r] = double(g[r]);
+        store_eq(seg, A, B, g);
     }
     __syncwarp();
     return !warp_any(bad);
@@ -751,30 +683,31 @@ BVP_DEV void bcr_backsub(const Args& a, const Inst& I, int na, int nbn) {
     }
 }
 
-// dense Gaussian elimination with partial pivoting (FP64), one lane
-BVP_DEV bool dense_solve(int n, double* A, double* b) {
+// dense Gaussian elimination with partial pivoting, one lane
+template <class R>
+BVP_DEV bool dense_solve(int n, R* A, R* b) {
     for (int k = 0; k < n; ++k) {
         int piv = k;
-        double best = fabs(A[k * n + k]);
+        R best = fabs(A[k * n + k]);
         for (int r = k + 1; r < n; ++r) {
-            const double v = fabs(A[r * n + k]);
+            const R v = fabs(A[r * n + k]);
             if (v > best) { best = v; piv = r; }
         }
-        if (!(best > 0.0) || !isfinite(best)) return false;
+        if (!(best > R(0)) || !isfinite(best)) return false;
         if (piv != k) {
-            for (int c = 0; c < n; ++c) { const double t = A[k * n + c]; A[k * n + c] = A[piv * n + c]; A[piv * n + c] = t; }
-            const double t = b[k]; b[k] = b[piv]; b[piv] = t;
+            for (int c = 0; c < n; ++c) { const R t = A[k * n + c]; A[k * n + c] = A[piv * n + c]; A[piv * n + c] = t; }
+            const R t = b[k]; b[k] = b[piv]; b[piv] = t;
         }
-        const double inv = 1.0 / A[k * n + k];
+        const R inv = R(1) / A[k * n + k];
         for (int r = k + 1; r < n; ++r) {
-            const double mlt = A[r * n + k] * inv;
-            if (mlt == 0.0) continue;
+            const R mlt = A[r * n + k] * inv;
+            if (mlt == R(0)) continue;
             for (int c = k + 1; c < n; ++c) A[r * n + c] -= mlt * A[k * n + c];
             b[r] -= mlt * b[k];
         }
     }
     for (int k = n - 1; k >= 0; --k) {
-        double s = b[k];
+        R s = b[k];
         for (int c = k + 1; c < n; ++c) s -= A[k * n + c] * b[c];
         b[k] = s / A[k * n + k];
     }
@@ -787,15 +720,15 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     const int nk = I.iscr[ISCR_NK];
     bool ok = true;
     for (int j = 0; j + 1 < nk; ++j)
-        ok = bcr_segment(a, I, I.iscr[ISCR_KEPT + j], I.iscr[ISCR_KEPT + j + 1], I.scr + SCR_SEG + j * EQW) && ok;
+        ok = bcr_segment(a, I, I.iscr[ISCR_KEPT + j], I.iscr[ISCR_KEPT + j + 1], seg_of(I, j)) && ok;
     int dense_ok = 1;
     if (lane == 0) {
         const int n = nk * M;
-        double* G = I.scr + SCR_DENSE;
-        double* rhs = I.scr + SCR_RHS;
-        for (int q = 0; q < n * n; ++q) G[q] = 0.0;
+        JT* G = reinterpret_cast<JT*>(I.scr + SCR_DENSE);
+        JT* rhs = reinterpret_cast<JT*>(I.scr + SCR_RHS);
+        for (int q = 0; q < n * n; ++q) G[q] = JT(0);
         for (int j = 0; j + 1 < nk; ++j) {
-            const double* seg = I.scr + SCR_SEG + j * EQW;
+            const JT* seg = seg_of(I, j);
             for (int r = 0; r < M; ++r) {
                 const int row = j * M + r;
                 for (int c = 0; c < M; ++c) {
@@ -812,13 +745,14 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
             int kj = 0;
             while (I.iscr[ISCR_KEPT + kj] != node) ++kj;
             for (int r = 0; r < M; ++r)
-                for (int c = 0; c < M; ++c) G[(row0 + r) * n + kj * M + c] += I.scr[SCR_BCBLK + k * M * M + r * M + c];
+                for (int c = 0; c < M; ++c)
+                    G[(row0 + r) * n + kj * M + c] += JT(I.scr[SCR_BCBLK + k * M * M + r * M + c]);
         }
-        for (int r = 0; r < M; ++r) rhs[row0 + r] = -I.scr[SCR_BCRES + r];
-        dense_ok = dense_solve(n, G, rhs) ? 1 : 0;
+        for (int r = 0; r < M; ++r) rhs[row0 + r] = JT(-I.scr[SCR_BCRES + r]);
+        dense_ok = dense_solve<JT>(n, G, rhs) ? 1 : 0;
         for (int j = 0; j < nk; ++j) {
             JT* d = a.delta + (I.nb + I.iscr[ISCR_KEPT + j]) * M;
-            for (int r = 0; r < M; ++r) d[r] = JT(rhs[j * M + r]);
+            for (int r = 0; r < M; ++r) d[r] = rhs[j * M + r];
         }
     }
     dense_ok = __shfl_sync(FULL, dense_ok, 0);
@@ -837,17 +771,34 @@ BVP_DEV void copy_y(double* dst, const double* src, int n) {
     __syncwarp();
 }
 
+// JT copy of the current iterate
+BVP_DEV void refresh_yj(const Args& a, const Inst& I) {
+    const double* y = y_of(a, I, I.cur);
+    JT* yj = yj_of(a, I);
+    for (int k = lane_id(); k < I.N * M; k += 32) yj[k] = JT(y[k]);
+    __syncwarp();
+}
+
+// Mixed-precision Newton: while ||F|| from the FP32 residual is above 100 abstol the
+// iterations use it; from then on, and for every convergence decision, the FP64 residual.
 BVP_DEV bool newton_attempt(const Args& a, Inst& I, bool linesearch, int& iters, double& nrm_out) {
     const int lane = lane_id();
     double* y = y_of(a, I, I.cur);
+    JT* yj = yj_of(a, I);
     double* yb = a.ybase + I.nb * M;
     const int nM = I.N * M;
     iters = 0;
-    double nrm = residual(a, I);
+    refresh_yj(a, I);
+    bool f32 = F32_PHASE_OK && a.fp32_phase && !linesearch;
+    const double switch_tol = 100.0 * a.abstol;
+    double nrm;
+    if constexpr (F32_PHASE_OK) nrm = f32 ? residual<float>(a, I) : residual<double>(a, I);
+    else nrm = residual<double>(a, I);
+    if (f32 && !(nrm > switch_tol)) { f32 = false; nrm = residual<double>(a, I); }
     nrm_out = nrm;
     if (!isfinite(nrm)) return false;
     if (nrm <= a.abstol) return true;
-    const double nrm0 = nrm;
+    double nrm0 = nrm;
     double best = nrm;
     int stall = 0;
     for (int it = 0; it < a.max_newton; ++it) {
@@ -856,18 +807,27 @@ BVP_DEV bool newton_attempt(const Args& a, Inst& I, bool linesearch, int& iters,
         ++iters;
         const JT* dl = a.delta + I.nb * M;
         if (!linesearch) {
-            for (int k = lane; k < nM; k += 32) y[k] += double(dl[k]);
+            for (int k = lane; k < nM; k += 32) {
+                const double v = y[k] + double(dl[k]);
+                y[k] = v;
+                yj[k] = JT(v);
+            }
             __syncwarp();
-            nrm = residual(a, I);
+            if constexpr (F32_PHASE_OK) nrm = f32 ? residual<float>(a, I) : residual<double>(a, I);
+            else nrm = residual<double>(a, I);
         } else {
             const double f0 = residual_sq(a, I);
             copy_y(yb, y, nM);
             double alpha = 1.0;
             bool ok = false;
             for (int ls = 0; ls < 20; ++ls) {
-                for (int k = lane; k < nM; k += 32) y[k] = yb[k] + alpha * double(dl[k]);
+                for (int k = lane; k < nM; k += 32) {
+                    const double v = yb[k] + alpha * double(dl[k]);
+                    y[k] = v;
+                    yj[k] = JT(v);
+                }
                 __syncwarp();
-                nrm = residual(a, I);
+                nrm = residual<double>(a, I);
                 const double f1 = residual_sq(a, I);
                 if (isfinite(nrm) && f1 <= (1.0 - 2e-4 * alpha) * f0) { ok = true; break; }
                 alpha *= 0.5;
@@ -875,6 +835,18 @@ BVP_DEV bool newton_attempt(const Args& a, Inst& I, bool linesearch, int& iters,
             if (!ok) { nrm_out = nrm; return false; }
         }
         nrm_out = nrm;
+        if (f32 && (!(nrm > switch_tol) || !(nrm < best))) {
+            // close enough, or the FP32 residual stopped improving at its roundoff floor:
+            // continue on the FP64 residual, which restarts the stall bookkeeping
+            f32 = false;
+            nrm = residual<double>(a, I);
+            nrm_out = nrm;
+            if (!isfinite(nrm)) return false;
+            if (nrm <= a.abstol) return true;
+            nrm0 = fmax(nrm0, nrm);
+            best = nrm; stall = 0;
+            continue;
+        }
         if (!isfinite(nrm)) return false;
         if (nrm <= a.abstol) return true;
         if (nrm > a.divergence_factor * nrm0) return false;
@@ -909,8 +881,8 @@ BVP_DEV double defect(const Args& a, const Inst& I) {
     const double* h = h_of(a, I, I.cur);
     const double* y = y_of(a, I, I.cur);
     double w1[SS], w1p[SS], w2[SS], w2p[SS];
-    interp_weights(tau_star(), w1, w1p);
-    interp_weights(1.0 - tau_star(), w2, w2p);
+    interp_weights<double>(tau_star(), w1, w1p);
+    interp_weights<double>(1.0 - tau_star(), w2, w2p);
     double dn = 0.0;
     bool bad = false;
     for (int i = lane; i < I.N - 1; i += 32) {
@@ -930,7 +902,7 @@ BVP_DEV double defect(const Args& a, const Inst& I) {
             const double* w = smp ? w2 : w1;
             const double* wp = smp ? w2p : w1p;
             double z[M], zp[M], fz[M];
-            sum_stages<double>(w, yi, Ki, KIi, h[i], z);
+            sum_stages<double, double>(w, yi, Ki, KIi, h[i], z);
 #pragma unroll
             for (int m = 0; m < M; ++m) {
                 double acc = Ki[m] * wp[0];
@@ -953,7 +925,7 @@ BVP_DEV double defect(const Args& a, const Inst& I) {
     }
     __syncwarp();
     dn = warp_max(dn);
-    return warp_any(bad) ? __longlong_as_double(0x7ff0000000000000LL) : dn;
+    return warp_any(bad) ? dinf() : dn;
 }
 
 // ---- mesh selection (adaptivity.jl:23-75, 250-304) -------------------------------------------
@@ -977,14 +949,14 @@ BVP_DEV void half_mesh(const Args& a, Inst& I, int src, int dst) {
 
 BVP_DEV long round_even(double x) { return (long)rint(x); }
 
-// Returns 1 on success (new mesh in buffer cur^1, I.N updated), 0 on Failure.
+// Returns 1 on success (new mesh in buffer cur^1, newN set), 0 on Failure.
 BVP_DEV int mesh_selector(const Args& a, Inst& I, int& newN) {
     const int lane = lane_id();
     const int n = I.N - 1;
     const double* h0 = h_of(a, I, I.cur);
     double* e = a.err + I.nb;
     const double ex = 1.0 / (ORD + 1);
-    double r1 = -__longlong_as_double(0x7ff0000000000000LL), r2 = 0.0;
+    double r1 = -dinf(), r2 = 0.0;
     for (int i = lane; i < n; i += 32) {
         const double sh = pow(e[i] / a.abstol, ex);
         e[i] = sh;
@@ -1063,7 +1035,7 @@ BVP_DEV void transfer(const Args& a, Inst& I, int newN) {
         const double dt = oh[i];
         const double tau = (t - om[i]) / dt;
         double w[SS], wp[SS];
-        interp_weights(tau, w, wp);
+        interp_weights<double>(tau, w, wp);
         const double* Kg = a.K + (I.nb + i) * (S * M);
         const double* KIg = a.KI + (I.nb + i) * (NSXA * M);
 #pragma unroll
@@ -1115,7 +1087,7 @@ BVP_DEV void init_instance(const Args& a, Inst& I) {
 }
 
 BVP_DEV void finalize_stages(const Args& a, Inst& I) {
-    residual(a, I);
+    residual<double>(a, I);
     const double* mesh = mesh_of(a, I, I.cur);
     const double* h = h_of(a, I, I.cur);
     const double* y = y_of(a, I, I.cur);
@@ -1219,7 +1191,7 @@ BVP_DEV Inst make_inst(const Args& a, int q) {
 // ---- kernels ---------------------------------------------------------------------------------
 // Persistent fused solve: each warp repeatedly takes the next instance from the work
 // counter and runs its complete adaptive solve.
-extern "C" __global__ void __launch_bounds__(128) bvp_solve_fused(const bvp::Args a) {
+extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::Args a) {
     const int lane = bvp::lane_id();
     while (true) {
         int k = 0;
@@ -1244,7 +1216,8 @@ extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, i
         bvp::Inst I = bvp::make_inst(a, a.order[k]);
         I.N = a.st[I.q].N;
         I.cur = 0;
-        double v = bvp::residual(a, I);
+        bvp::refresh_yj(a, I);
+        double v = bvp::residual<double>(a, I);
         if (stage >= 1 && stage <= 2) bvp::jacobian(a, I);
         if (stage == 2) v = bvp::linear_solve(a, I) ? 0.0 : 1.0;
         if (stage == 3) v = bvp::defect(a, I);

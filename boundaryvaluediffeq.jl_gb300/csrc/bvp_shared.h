@@ -29,7 +29,7 @@ struct BvpInstState {
 struct BvpArgs {
     int n_inst, n_params;
     int adaptive, max_sub, max_newton, max_rounds, stall_steps;
-    int transfer_inplace, bc_jac_exact, linesearch, want_stages, y0_mode;
+    int transfer_inplace, bc_jac_exact, linesearch, want_stages, y0_mode, fp32_phase;
     double abstol, defect_threshold, divergence_factor;
     double bc_t[16];
     bvp_i64 tot;                   // total node capacity (sum over instances)
@@ -59,6 +59,8 @@ struct BvpArgs {
     BVP_JT_PTR* rec;               // [tot][RECW]
     BVP_JT_PTR* eq;                // [2][tot][EQW]
     BVP_JT_PTR* delta;             // [tot][M]
+    BVP_JT_PTR* yj;                // [tot][M]  current iterate in the Jacobian precision
+    BVP_JT_PTR* Fj;                // [tot][M]  collocation residual in the Jacobian precision
     double* scr;                   // per-instance scratch, SCRW doubles each
     int* iscr;                     // per-instance int scratch, ISCRW ints each
     BvpInstState* st;
@@ -67,8 +69,8 @@ struct BvpArgs {
 // Scratch layout as a function of (M, order, BC evaluation points, two-point).
 struct BvpLayout {
     int M, S, SS, NSX, NSXA, EQW, RECW, NBCB, KMAX, NDENSE;
-    int SCR_BCRES, SCR_BCBLK, SCR_SEG, SCR_DENSE, SCR_RHS, SCRW;
-    int ISCR_NK, ISCR_KEPT, ISCR_NB, ISCR_BNODE, ISCRW;
+    int SCR_BCRES, SCR_BCBLK, SCR_SEG, SCR_DENSE, SCR_RHS, SCR_UA, SCRW;
+    int ISCR_NK, ISCR_KEPT, ISCR_NB, ISCR_BNODE, ISCR_UNODE, ISCR_UIN, ISCRW;
 };
 
 #ifdef __CUDACC_RTC__
@@ -94,11 +96,14 @@ BVP_LAYOUT_FN BvpLayout bvp_make_layout(int M, int order, int nbc, int twopoint)
     L.SCR_SEG = L.SCR_BCBLK + L.NBCB * M * M;
     L.SCR_DENSE = L.SCR_SEG + (L.KMAX - 1) * L.EQW;
     L.SCR_RHS = L.SCR_DENSE + L.NDENSE * L.NDENSE;
-    L.SCRW = L.SCR_RHS + L.NDENSE;
+    L.SCR_UA = L.SCR_RHS + L.NDENSE;
+    L.SCRW = L.SCR_UA + (twopoint ? 2 : nbc) * M;
     L.ISCR_NK = 0;
     L.ISCR_KEPT = 1;
     L.ISCR_NB = L.ISCR_KEPT + L.KMAX;
     L.ISCR_BNODE = L.ISCR_NB + 1;
-    L.ISCRW = L.ISCR_BNODE + L.NBCB;
+    L.ISCR_UNODE = L.ISCR_BNODE + L.NBCB;
+    L.ISCR_UIN = L.ISCR_UNODE + (twopoint ? 2 : nbc);
+    L.ISCRW = L.ISCR_UIN + (twopoint ? 2 : nbc);
     return L;
 }

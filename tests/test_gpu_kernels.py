@@ -83,12 +83,35 @@ def test_k2_jacobian_blocks_match_oracle(pkg, problems, name, order):
         assert np.abs(gR - R).max() <= 2e-5 * sc
 
 
-@pytest.mark.parametrize("jac_precision,tol", [(32, 2e-3), (64, 1e-9)])
+def _apply_jacobian(p, S, R, nodes, blocks, delta):
+    """J δ in the reference's row order: BC rows, then collocation rows."""
+    N, M = delta.shape
+    colloc = np.einsum("iab,ib->ia", S, delta[:-1]) + np.einsum("iab,ib->ia", R, delta[1:])
+    bc = np.zeros(M)
+    for nd, B in zip(nodes, blocks):
+        bc += B @ delta[nd]
+    return bc, colloc
+
+
+def _backward_error(p, o, params, mesh, y, delta, order):
+    F, K, _ = o.residual(params, mesh, y, order=order)
+    S, R, nodes, blocks = o.jacobian(params, mesh, y, order=order)
+    N, M = len(mesh), p.M
+    La = p.La if p.twopoint else M
+    Fc = F[La:La + (N - 1) * M].reshape(N - 1, M)
+    Fb = np.concatenate([F[:La], F[La + (N - 1) * M:]]) if p.twopoint else F[:M]
+    bc, colloc = _apply_jacobian(p, S, R, nodes, blocks, delta)
+    r = max(np.abs(bc + Fb).max(), np.abs(colloc + Fc).max())
+    Jn = max(np.abs(S).sum(2).max() + np.abs(R).sum(2).max(), np.abs(blocks).sum(2).max() * len(blocks))
+    return r / (Jn * np.abs(delta).max() + np.abs(F).max())
+
+
 @pytest.mark.parametrize("name,order", CASES)
-def test_k3_newton_direction_matches_oracle(pkg, problems, name, order, jac_precision, tol):
-    # The structured cyclic-reduction solve against the oracle's sequential elimination.
+def test_k3_newton_direction_fp64_matches_oracle(pkg, problems, name, order):
+    # FP64 factorisation: the structured cyclic reduction agrees with the oracle's
+    # sequential elimination to roundoff times the systems' conditioning
     p, params, meshes, ys = _cases(problems, name, order=order)
-    sv = pkg.BatchSolver(p, order=order, jac_precision=jac_precision)
+    sv = pkg.BatchSolver(p, order=order, jac_precision=64)
     out = sv.eval_stage(2, params, meshes, ys)
     assert (out["norm"] == 0).all(), "singular system reported"
     o = _oracle(p)
@@ -97,8 +120,26 @@ def test_k3_newton_direction_matches_oracle(pkg, problems, name, order, jac_prec
         d = o.newton_step(params[q], meshes[q], ys[q], order=order)
         N = len(meshes[q])
         got = out["delta"][off[q]:off[q] + N]
-        # conditioning of the random-state systems varies; compare relative to |δ|
-        assert np.abs(got - d).max() <= tol * max(1.0, np.abs(d).max()), (q, np.abs(got - d).max())
+        assert np.abs(got - d).max() <= 1e-8 * max(1.0, np.abs(d).max()), (q, np.abs(got - d).max())
+        assert _backward_error(p, o, params[q], meshes[q], ys[q], got, order) <= 1e-13
+
+
+@pytest.mark.parametrize("name,order", CASES)
+def test_k3_newton_direction_fp32_backward_stable(pkg, problems, name, order):
+    # FP32 factorisation: a backward-stable solve of the FP32-rounded system, i.e. the
+    # residual of J δ = -F (evaluated in FP64 with the oracle's Jacobian) is at FP32
+    # roundoff relative to |J||δ| + |F|; the forward error then follows the conditioning
+    p, params, meshes, ys = _cases(problems, name, order=order)
+    sv = pkg.BatchSolver(p, order=order, jac_precision=32)
+    out = sv.eval_stage(2, params, meshes, ys)
+    assert (out["norm"] == 0).all(), "singular system reported"
+    o = _oracle(p)
+    off = out["offsets"]
+    for q in range(len(meshes)):
+        N = len(meshes[q])
+        got = out["delta"][off[q]:off[q] + N]
+        eta = _backward_error(p, o, params[q], meshes[q], ys[q], got, order)
+        assert eta <= 2e-5, (q, eta)
 
 
 @pytest.mark.parametrize("name,order", CASES)
