@@ -79,10 +79,9 @@ using Args = BvpArgs;
 constexpr int SCR_BCRES = 0;                           // M        BC residual (FP64)
 constexpr int SCR_BCBLK = SCR_BCRES + M;               // NBCB x M x M  BC Jacobian blocks
 constexpr int SCR_SEG = SCR_BCBLK + NBCB * M * M;      // (KMAX-1) x EQW segment relations (JT)
-constexpr int SCR_DENSE = SCR_SEG + (KMAX - 1) * EQW;  // NDENSE x NDENSE separator system (JT)
-constexpr int SCR_RHS = SCR_DENSE + NDENSE * NDENSE;   // NDENSE (JT)
-constexpr int SCR_UA = SCR_RHS + NDENSE;               // NBCP x M  u at the BC points (FP64)
-constexpr int SCRW = SCR_UA + NBCP * M;
+constexpr int SCR_UA = SCR_SEG + (KMAX - 1) * EQW;     // NBCP x M  u at the BC points (FP64)
+constexpr int SCR_BCW = SCR_UA + NBCP * M;             // NBCP x SS interpolant weights at the BC points
+constexpr int SCRW = SCR_BCW + NBCP * SS;
 // int scratch
 constexpr int ISCR_NK = 0;                   // kept count
 constexpr int ISCR_KEPT = 1;                 // KMAX kept nodes
@@ -90,7 +89,9 @@ constexpr int ISCR_NB = ISCR_KEPT + KMAX;    // number of BC blocks
 constexpr int ISCR_BNODE = ISCR_NB + 1;      // NBCB block nodes
 constexpr int ISCR_UNODE = ISCR_BNODE + NBCB;  // NBCP: node each BC point maps to
 constexpr int ISCR_UIN = ISCR_UNODE + NBCP;    // NBCP: 1 if the point is interior
-constexpr int ISCRW = ISCR_UIN + NBCP;
+constexpr int ISCR_LOFF = ISCR_UIN + NBCP;     // KMAX+1: first lane of each segment
+constexpr int ISCRW = ISCR_LOFF + KMAX + 1;
+static_assert(KMAX - 1 <= 32, "one lane at least per separator segment");
 
 // ---- warp helpers ------------------------------------------------------------------------
 BVP_DEV int lane_id() { return threadIdx.x & 31; }
@@ -155,9 +156,11 @@ constexpr bool NODE_SHARE = S >= 2 && ORD >= 4;
 // ---- Φ for one interval (collocation.jl:44-72) ------------------------------------------
 // With `node` non-null and NODE_SHARE, stage 0 is taken from node[] (f at the left node)
 // and stage 1 is evaluated at the right node with t = t_{i+1} and written back to node[].
+// With `dy` non-null the residual uses the FP64 difference y_{i+1} - y_i instead of the
+// one formed from yi, yi1 (the FP32 residual keeps its roundoff near h|K| eps32).
 template <class T, class PT>
 BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, double ti, double hi_d,
-                          T* node = nullptr, double ti1 = 0.0) {
+                          T* node = nullptr, double ti1 = 0.0, const double* dy = nullptr) {
     const PT hi = PT(hi_d);
     T Y[M];
 #pragma unroll
@@ -189,7 +192,8 @@ BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, 
         T acc = Ki[m] * PT(tab_b(0));
 #pragma unroll
         for (int r = 1; r < S; ++r) acc = acc + Ki[r * M + m] * PT(tab_b(r));
-        ri[m] = (yi1[m] - yi[m]) - hi * acc;
+        if (dy) ri[m] = T(PT(dy[m])) - hi * acc;
+        else ri[m] = (yi1[m] - yi[m]) - hi * acc;
     }
 }
 
@@ -227,45 +231,71 @@ BVP_DEV void sum_stages(const W* w, const T* yi, const T* Ki, const T* KIi, W hi
     }
 }
 
-// EvalSol u(t) of the current iterate in precision R (interpolation.jl:214-242); one lane.
-// Returns the node the reference attributes the BC Jacobian to (the exact endpoint, else
-// the interval's left node); *interior is set for points strictly inside the mesh.
-// With R = double the interval's stages come from K (written by the FP64 residual);
-// with R = float they are recomputed.
-template <class R>
-BVP_DEV int eval_sol(const Args& a, const Inst& I, double t, R* z, bool* interior) {
-    const double* mesh = mesh_of(a, I, I.cur);
-    const double* h = h_of(a, I, I.cur);
-    const int N = I.N;
-    if (t == mesh[0]) {
-#pragma unroll
-        for (int m = 0; m < M; ++m) z[m] = y_at<R>(a, I, m);
-        *interior = false; return 0;
+// Per-mesh setup (lane 0), redone whenever the mesh changes:
+//  * each BC evaluation time t_k is located as the reference's EvalSol does
+//    (interpolation.jl:214-242): the exact endpoints give y_1 / y_N, any other t the
+//    interval ii = interval(mesh, t) with the interpolant weights at τ = (t - t_ii)/h_ii;
+//    the node the BC Jacobian row is attributed to is the endpoint or ii (the reference
+//    differentiates the BCs with the interpolant's stages held fixed, mirk.jl:565-572);
+//  * the separator nodes of the partition solve: 0, N-1 and every node a BC row touches;
+//  * the lanes per separator segment: a power of two no larger than the segment,
+//    proportional to its share of the mesh, at least one, 32 in all.
+BVP_DEV void mesh_setup(const Args& a, const Inst& I) {
+    if (lane_id() == 0) {
+        const double* mesh = mesh_of(a, I, I.cur);
+        const double* h = h_of(a, I, I.cur);
+        const int N = I.N;
+        int kept[KMAX];
+        int nk = 0;
+        kept[nk++] = 0;
+        kept[nk++] = N - 1;
+        if (TWOPOINT) {
+            I.iscr[ISCR_UNODE] = 0; I.iscr[ISCR_UNODE + 1] = N - 1;
+            I.iscr[ISCR_UIN] = 0; I.iscr[ISCR_UIN + 1] = 0;
+        } else {
+            for (int k = 0; k < NBC; ++k) {
+                const double t = a.bc_t[k];
+                int node, in = 0;
+                if (t == mesh[0]) node = 0;
+                else if (t == mesh[N - 1]) node = N - 1;
+                else {
+                    node = interval_of(mesh, N, t);
+                    in = 1;
+                    double w[SS], wp[SS];
+                    interp_weights<double>((t - mesh[node]) / h[node], w, wp);
+                    for (int s = 0; s < SS; ++s) I.scr[SCR_BCW + k * SS + s] = w[s];
+                }
+                I.iscr[ISCR_UNODE + k] = node;
+                I.iscr[ISCR_UIN + k] = in;
+                kept[nk++] = node;
+                if (in && a.bc_jac_exact) kept[nk++] = node + 1;
+            }
+        }
+        for (int u = 1; u < nk; ++u) {
+            const int v = kept[u];
+            int w2 = u - 1;
+            while (w2 >= 0 && kept[w2] > v) { kept[w2 + 1] = kept[w2]; --w2; }
+            kept[w2 + 1] = v;
+        }
+        int nu = 0;
+        for (int u = 0; u < nk; ++u)
+            if (nu == 0 || kept[u] != kept[nu - 1]) kept[nu++] = kept[u];
+        I.iscr[ISCR_NK] = nu;
+        for (int u = 0; u < nu; ++u) I.iscr[ISCR_KEPT + u] = kept[u];
+        const int ns = nu - 1, m = N - 1;
+        int o = 0;
+        for (int j = 0; j < ns; ++j) {
+            const int len = kept[j + 1] - kept[j];
+            int want = 1 + ((32 - ns) * len) / m;
+            want = want < len ? want : len;
+            int L = 1;
+            while (2 * L <= want) L *= 2;
+            I.iscr[ISCR_LOFF + j] = o;
+            o += L;
+        }
+        I.iscr[ISCR_LOFF + ns] = o;
     }
-    if (t == mesh[N - 1]) {
-#pragma unroll
-        for (int m = 0; m < M; ++m) z[m] = y_at<R>(a, I, (N - 1) * M + m);
-        *interior = false; return N - 1;
-    }
-    const int ii = interval_of(mesh, N, t);
-    const R tau = R((t - mesh[ii]) / h[ii]);
-    R w[SS], wp[SS];
-    interp_weights<R>(tau, w, wp);
-    R yi[M], yi1[M], Ki[S * M], KIi[NSXA * M], ri[M];
-#pragma unroll
-    for (int m = 0; m < M; ++m) { yi[m] = y_at<R>(a, I, ii * M + m); yi1[m] = y_at<R>(a, I, (ii + 1) * M + m); }
-    const R* pr = params_as<R>(I);
-    if constexpr (sizeof(R) == 8) {
-        const double* Kg = a.K + (I.nb + ii) * (S * M);
-#pragma unroll
-        for (int k = 0; k < S * M; ++k) Ki[k] = Kg[k];
-    } else {
-        phi_interval<R, R>(yi, yi1, Ki, ri, pr, mesh[ii], h[ii]);
-    }
-    interp_stages<R, R>(yi, yi1, Ki, KIi, pr, mesh[ii], h[ii]);
-    sum_stages<R, R>(w, yi, Ki, KIi, R(h[ii]), z);
-    *interior = true;
-    return ii;
+    __syncwarp();
 }
 
 // ---- K1: residual and stages (warp). Returns ||F||_inf (+inf if non-finite). -----------
@@ -294,11 +324,36 @@ BVP_DEV double residual(const Args& a, const Inst& I) {
         for (int m = 0; m < M; ++m) y0v[m] = y_at<R>(a, I, i0 * M + m);
         bvp_f<R, R>(node, y0v, pr, R(mesh[i0]));
     }
+    const double* y64 = y_of(a, I, I.cur);
+    // interior BC points: the lane whose block holds the interval evaluates the
+    // interpolant there from its registers (the stages it just computed)
+    int bc_iv[NBCP];
+#pragma unroll
+    for (int k = 0; k < NBCP; ++k) bc_iv[k] = (!TWOPOINT && I.iscr[ISCR_UIN + k]) ? I.iscr[ISCR_UNODE + k] : -1;
     for (int i = i0; i < i1; ++i) {
         R yi[M], yi1[M], Ki[S * M], ri[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) { yi[m] = y_at<R>(a, I, i * M + m); yi1[m] = y_at<R>(a, I, (i + 1) * M + m); }
-        phi_interval<R, R>(yi, yi1, Ki, ri, pr, mesh[i], h[i], NODE_SHARE ? node : nullptr, mesh[i + 1]);
+        if constexpr (sizeof(R) == 8) {
+            phi_interval<R, R>(yi, yi1, Ki, ri, pr, mesh[i], h[i], NODE_SHARE ? node : nullptr, mesh[i + 1]);
+        } else {
+            double dy[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) dy[m] = y64[(i + 1) * M + m] - y64[i * M + m];
+            phi_interval<R, R>(yi, yi1, Ki, ri, pr, mesh[i], h[i], NODE_SHARE ? node : nullptr, mesh[i + 1], dy);
+        }
+#pragma unroll
+        for (int k = 0; k < NBCP; ++k) {
+            if (bc_iv[k] == i) {
+                R KIi[NSXA * M], w[SS], z[M];
+                interp_stages<R, R>(yi, yi1, Ki, KIi, pr, mesh[i], h[i]);
+#pragma unroll
+                for (int s = 0; s < SS; ++s) w[s] = R(I.scr[SCR_BCW + k * SS + s]);
+                sum_stages<R, R>(w, yi, Ki, KIi, R(h[i]), z);
+#pragma unroll
+                for (int m = 0; m < M; ++m) I.scr[SCR_UA + k * M + m] = double(z[m]);
+            }
+        }
         JT* Fj = a.Fj + (I.nb + i) * M;
         if constexpr (sizeof(R) == 8) {
             double* Kg = a.K + (I.nb + i) * (S * M);
@@ -331,21 +386,26 @@ BVP_DEV double residual(const Args& a, const Inst& I) {
             for (int k = 0; k < LA; ++k) res[k] = ra[k];
             for (int k = LA; k < M; ++k) res[k] = rb[k - LA];
             for (int m = 0; m < M; ++m) { ua_c[m] = double(ya[m]); ua_c[M + m] = double(yb[m]); }
-            I.iscr[ISCR_UNODE] = 0; I.iscr[ISCR_UNODE + 1] = I.N - 1;
-            I.iscr[ISCR_UIN] = 0; I.iscr[ISCR_UIN + 1] = 0;
         } else {
             R ua[NBC * M];
             const R* ptrs[NBC];
 #pragma unroll
             for (int k = 0; k < NBC; ++k) {
-                bool in;
-                const int nd = eval_sol<R>(a, I, a.bc_t[k], &ua[k * M], &in);
+                if (I.iscr[ISCR_UIN + k]) {
+#pragma unroll
+                    for (int m = 0; m < M; ++m) ua[k * M + m] = R(ua_c[k * M + m]);
+                } else {
+                    // exact endpoints: EvalSol returns y_1 / y_N
+                    const int nd = I.iscr[ISCR_UNODE + k];
+#pragma unroll
+                    for (int m = 0; m < M; ++m) {
+                        ua[k * M + m] = y_at<R>(a, I, nd * M + m);
+                        ua_c[k * M + m] = double(ua[k * M + m]);
+                    }
+                }
                 ptrs[k] = &ua[k * M];
-                I.iscr[ISCR_UNODE + k] = nd;
-                I.iscr[ISCR_UIN + k] = in ? 1 : 0;
             }
             bvp_bc<R, R>(res, ptrs, pr);
-            for (int k = 0; k < NBC * M; ++k) ua_c[k] = double(ua[k]);
         }
 #pragma unroll
         for (int m = 0; m < M; ++m) {
@@ -379,17 +439,19 @@ BVP_DEV double residual_sq(const Args& a, const Inst& I) {
 // ---- K2: Jacobian blocks (warp) ------------------------------------------------------------
 // S_i = ∂r_i/∂y_i and R_i = ∂r_i/∂y_{i+1} by forward mode with 2M tangents in JT, from the
 // JT copy of the iterate. BC rows use u at the BC points cached by the last residual.
-BVP_DEV void add_bc_block(const Inst& I, int node, const double* G) {
-    int nb = I.iscr[ISCR_NB];
-    for (int k = 0; k < nb; ++k)
-        if (I.iscr[ISCR_BNODE + k] == node) {
-            for (int q = 0; q < M * M; ++q) I.scr[SCR_BCBLK + k * M * M + q] += G[q];
-            return;
-        }
-    I.iscr[ISCR_BNODE + nb] = node;
-    for (int q = 0; q < M * M; ++q) I.scr[SCR_BCBLK + nb * M * M + q] = G[q];
-    I.iscr[ISCR_NB] = nb + 1;
-}
+// BC Jacobian blocks: one (node, L x M) block per BC contribution, accumulated on lane 0 in
+// registers and written once; the separator solve adds blocks that share a node.
+struct BcBlocks {
+    int n;
+    int node[NBCB];
+    double G[NBCB][M * M];
+    BVP_DEV void add(int nd, const double* g) {
+        node[n] = nd;
+#pragma unroll
+        for (int q = 0; q < M * M; ++q) G[n][q] = g[q];
+        ++n;
+    }
+};
 
 BVP_DEV void jacobian(const Args& a, const Inst& I) {
     using DI = Dual<JT, D>;
@@ -417,7 +479,8 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
             }
     }
     if (lane == 0) {
-        I.iscr[ISCR_NB] = 0;
+        BcBlocks bb;
+        bb.n = 0;
         double G[M * M];
         const double* ua_c = I.scr + SCR_UA;
         if (TWOPOINT) {
@@ -426,12 +489,12 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
             bvp_bca<DU, JT>(ra, ua, I.pj);
             for (int q = 0; q < M * M; ++q) G[q] = 0.0;
             for (int r = 0; r < LA; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(ra[r].d[c]);
-            add_bc_block(I, 0, G);
+            bb.add(0, G);
             for (int m = 0; m < M; ++m) { ua[m] = DU(JT(ua_c[M + m])); ua[m].d[m] = JT(1); }
             bvp_bcb<DU, JT>(ra, ua, I.pj);
             for (int q = 0; q < M * M; ++q) G[q] = 0.0;
             for (int r = LA; r < M; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(ra[r - LA].d[c]);
-            add_bc_block(I, I.N - 1, G);
+            bb.add(I.N - 1, G);
         } else {
             for (int k = 0; k < NBC; ++k) {
                 DU ua[NBC * M];
@@ -450,13 +513,13 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
                 if (!I.iscr[ISCR_UIN + k] || !a.bc_jac_exact) {
                     // the interpolant's stages are held at their primal values: du(t)/dy = I
                     // on the interval's left node (interpolation.jl:214-242, mirk.jl:565-572)
-                    add_bc_block(I, node, G);
+                    bb.add(node, G);
                 } else {
                     // exact: chain through the interval's stages and extra stages
                     const int ii = node;
-                    const JT tau = JT((a.bc_t[k] - mesh[ii]) / h[ii]);
-                    JT w[SS], wp[SS];
-                    interp_weights<JT>(tau, w, wp);
+                    JT w[SS];
+#pragma unroll
+                    for (int s2 = 0; s2 < SS; ++s2) w[s2] = JT(I.scr[SCR_BCW + k * SS + s2]);
                     DI yi[M], yi1[M], Ki[S * M], KIi[NSXA * M], ri[M], z[M];
                     for (int m = 0; m < M; ++m) {
                         yi[m] = DI(yj[ii * M + m]); yi[m].d[m] = JT(1);
@@ -475,39 +538,34 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
                             }
                             JL[r * M + c] = sl; JR[r * M + c] = sr;
                         }
-                    add_bc_block(I, ii, JL);
-                    add_bc_block(I, ii + 1, JR);
+                    bb.add(ii, JL);
+                    bb.add(ii + 1, JR);
                 }
             }
         }
-        // kept (separator) nodes: 0, N-1 and every node a BC row touches
-        int kept[KMAX];
-        int nk = 0;
-        kept[nk++] = 0;
-        kept[nk++] = I.N - 1;
-        const int nb = I.iscr[ISCR_NB];
-        for (int k = 0; k < nb; ++k) kept[nk++] = I.iscr[ISCR_BNODE + k];
-        for (int u = 1; u < nk; ++u) {
-            const int v = kept[u];
-            int w2 = u - 1;
-            while (w2 >= 0 && kept[w2] > v) { kept[w2 + 1] = kept[w2]; --w2; }
-            kept[w2 + 1] = v;
+        I.iscr[ISCR_NB] = bb.n;
+        for (int k = 0; k < bb.n; ++k) {
+            I.iscr[ISCR_BNODE + k] = bb.node[k];
+            for (int q = 0; q < M * M; ++q) I.scr[SCR_BCBLK + k * M * M + q] = bb.G[k][q];
         }
-        int nu = 0;
-        for (int u = 0; u < nk; ++u)
-            if (nu == 0 || kept[u] != kept[nu - 1]) kept[nu++] = kept[u];
-        I.iscr[ISCR_NK] = nu;
-        for (int u = 0; u < nu; ++u) I.iscr[ISCR_KEPT + u] = kept[u];
     }
     __syncwarp();
 }
 
 // ---- K3: structured factorisation + solve (warp) -----------------------------------------
-// Block cyclic reduction with partial pivoting over each segment between separator
-// nodes: pairs of neighbouring block rows eliminate their shared node (Gaussian
-// elimination with row pivoting on that node's 2M x M column block), halving the
-// segment at each level. The separator system is solved densely and the eliminated nodes
-// are recovered level by level.
+// Partition method over the almost-block-diagonal system. The separator nodes (0, N-1 and
+// every node a BC row touches) split the collocation chain into segments; each segment gets
+// a power-of-two group of lanes and each lane a contiguous block of its intervals.
+//   1. every lane eliminates its block's interior nodes in turn (registers), leaving one
+//      relation A δ_a + B δ_b = g between its block ends;
+//   2. a shuffle tree inside each lane group eliminates the block-end nodes pairwise until
+//      the group's root holds the segment relation;
+//   3. the segment relations and the BC rows form a small dense system in the separator
+//      values, solved on one lane;
+//   4. the tree is unwound (block-end values), then each lane back-substitutes its block.
+// Every elimination is Gaussian elimination with row pivoting on the shared node's 2M x M
+// column block (the reference factors the same matrix with an almost-banded QR/LU,
+// mirk.jl:721-777).
 BVP_DEV void load_eq0(const Args& a, const Inst& I, int i, JT* A, JT* B, JT* g) {
     const JT* Sg = a.Sb + (I.nb + i) * (M * M);
     const JT* Rg = a.Rb + (I.nb + i) * (M * M);
@@ -591,96 +649,25 @@ BVP_DEV bool eliminate_pair(const JT* Al, const JT* Bl, const JT* gl, const JT* 
 
 BVP_DEV JT* seg_of(const Inst& I, int j) { return reinterpret_cast<JT*>(I.scr + SCR_SEG) + j * EQW; }
 
-// reduce segment [na, nb]; its final relation A δ_na + B δ_nb = g goes to seg_of(j)
-BVP_DEV bool bcr_segment(const Args& a, const Inst& I, int na, int nbn, JT* seg) {
-    const int lane = lane_id();
-    const int m = nbn - na;
-    JT A[M * M], B[M * M], g[M];
-    if (m == 1) {
-        if (lane == 0) {
-            load_eq0(a, I, na, A, B, g);
-            store_eq(seg, A, B, g);
-        }
-        __syncwarp();
-        return true;
+// δ_x from an elimination record: U δ_x = g - X δ_lo - Y δ_hi (U upper triangular)
+BVP_DEV void back_solve(const JT* rg, const JT* dlo, const JT* dhi, JT* dx) {
+    JT t[M];
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+        JT s = rg[3 * M * M + r];
+#pragma unroll
+        for (int c = 0; c < M; ++c) s -= rg[M * M + r * M + c] * dlo[c] + rg[2 * M * M + r * M + c] * dhi[c];
+        t[r] = s;
     }
-    bool bad = false;
-    int ml = m, lvl = 0, buf = 0;
-    JT* eqb[2] = {a.eq + I.nb * EQW, a.eq + (a.tot + I.nb) * EQW};
-    while (ml > 1) {
-        const int np = ml >> 1;
-        for (int e = lane; e < np; e += 32) {
-            JT Al[M * M], Bl[M * M], gl[M], Ar[M * M], Br[M * M], gr[M];
-            if (lvl == 0) {
-                load_eq0(a, I, na + 2 * e, Al, Bl, gl);
-                load_eq0(a, I, na + 2 * e + 1, Ar, Br, gr);
-            } else {
-                load_eq(eqb[buf] + (2 * e) * EQW, Al, Bl, gl);
-                load_eq(eqb[buf] + (2 * e + 1) * EQW, Ar, Br, gr);
-            }
-            const int mid = na + ((2 * e + 1) << lvl);
-            JT* rg = a.rec + (I.nb + mid) * RECW;
-            const bool ok = eliminate_pair(Al, Bl, gl, Ar, Br, gr, rg, A, B, g);
-            bad |= !ok;
-            store_eq(eqb[buf ^ 1] + e * EQW, A, B, g);
-        }
-        if ((ml & 1) && lane == (np & 31)) {
-            if (lvl == 0) load_eq0(a, I, na + ml - 1, A, B, g);
-            else load_eq(eqb[buf] + (ml - 1) * EQW, A, B, g);
-            store_eq(eqb[buf ^ 1] + np * EQW, A, B, g);
-        }
-        __syncwarp();
-        buf ^= 1;
-        ml = (ml + 1) >> 1;
-        ++lvl;
+#pragma unroll
+    for (int r = M - 1; r >= 0; --r) {
+        JT s = t[r];
+#pragma unroll
+        for (int c = r + 1; c < M; ++c) s -= rg[r * M + c] * t[c];
+        t[r] = s / rg[r * M + r];
     }
-    if (lane == 0) {
-        load_eq(eqb[buf], A, B, g);
-        store_eq(seg, A, B, g);
-    }
-    __syncwarp();
-    return !warp_any(bad);
-}
-
-BVP_DEV void bcr_backsub(const Args& a, const Inst& I, int na, int nbn) {
-    const int lane = lane_id();
-    const int m = nbn - na;
-    if (m <= 1) return;
-    int L = 0;
-    while ((1 << L) < m) ++L;
-    for (int lvl = L - 1; lvl >= 0; --lvl) {
-        const int ml = (m + (1 << lvl) - 1) >> lvl;
-        const int np = ml >> 1;
-        for (int e = lane; e < np; e += 32) {
-            const int lo = na + ((2 * e) << lvl);
-            const int mid = na + ((2 * e + 1) << lvl);
-            int hi = na + ((2 * e + 2) << lvl);
-            hi = hi > nbn ? nbn : hi;
-            const JT* rg = a.rec + (I.nb + mid) * RECW;
-            const JT* dlo = a.delta + (I.nb + lo) * M;
-            const JT* dhi = a.delta + (I.nb + hi) * M;
-            JT t[M];
 #pragma unroll
-            for (int r = 0; r < M; ++r) {
-                JT s = rg[3 * M * M + r];
-#pragma unroll
-                for (int c = 0; c < M; ++c)
-                    s -= rg[M * M + r * M + c] * dlo[c] + rg[2 * M * M + r * M + c] * dhi[c];
-                t[r] = s;
-            }
-            JT* dm = a.delta + (I.nb + mid) * M;
-#pragma unroll
-            for (int r = M - 1; r >= 0; --r) {
-                JT s = t[r];
-#pragma unroll
-                for (int c = r + 1; c < M; ++c) s -= rg[r * M + c] * t[c];
-                t[r] = s / rg[r * M + r];
-            }
-#pragma unroll
-            for (int r = 0; r < M; ++r) dm[r] = t[r];
-        }
-        __syncwarp();
-    }
+    for (int r = 0; r < M; ++r) dx[r] = t[r];
 }
 
 // dense Gaussian elimination with partial pivoting, one lane
@@ -718,14 +705,60 @@ BVP_DEV bool dense_solve(int n, R* A, R* b) {
 BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     const int lane = lane_id();
     const int nk = I.iscr[ISCR_NK];
-    bool ok = true;
-    for (int j = 0; j + 1 < nk; ++j)
-        ok = bcr_segment(a, I, I.iscr[ISCR_KEPT + j], I.iscr[ISCR_KEPT + j + 1], seg_of(I, j)) && ok;
+    const int ns = nk - 1;
+    // this lane's segment, position in its lane group and interval block
+    int seg = -1, t = 0, L = 1, na = 0, nbk = 0;
+    for (int j = 0; j < ns; ++j) {
+        const int o0 = I.iscr[ISCR_LOFF + j], o1 = I.iscr[ISCR_LOFF + j + 1];
+        if (lane >= o0 && lane < o1) { seg = j; t = lane - o0; L = o1 - o0; }
+    }
+    const bool active = seg >= 0;
+    if (active) { na = I.iscr[ISCR_KEPT + seg]; nbk = I.iscr[ISCR_KEPT + seg + 1]; }
+    const int len = nbk - na;
+    const int blo = na + (t * len) / L;            // block [blo, bhi)
+    const int bhi = na + ((t + 1) * len) / L;
+    bool bad = false;
+    // 1. sequential elimination inside the block
+    JT A[M * M], B[M * M], g[M];
+    if (active) {
+        load_eq0(a, I, blo, A, B, g);
+        for (int c = blo + 1; c < bhi; ++c) {
+            JT Ar[M * M], Br[M * M], gr[M];
+            load_eq0(a, I, c, Ar, Br, gr);
+            bad |= !eliminate_pair(A, B, g, Ar, Br, gr, a.rec + (I.nb + c) * RECW, A, B, g);
+        }
+    }
+    // 2. shuffle tree over the block relations of each lane group
+    int bnode = bhi;
+    int xs[5];
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+        const int step = 1 << s;
+        JT Ap[M * M], Bp[M * M], gp[M];
+#pragma unroll
+        for (int q = 0; q < M * M; ++q) {
+            Ap[q] = __shfl_down_sync(FULL, A[q], step);
+            Bp[q] = __shfl_down_sync(FULL, B[q], step);
+        }
+#pragma unroll
+        for (int q = 0; q < M; ++q) gp[q] = __shfl_down_sync(FULL, g[q], step);
+        const int bp = __shfl_down_sync(FULL, bnode, step);
+        xs[s] = bnode;
+        if (active && (t % (2 * step)) == 0 && t + step < L) {
+            bad |= !eliminate_pair(A, B, g, Ap, Bp, gp, a.rec + (I.nb + bnode) * RECW, A, B, g);
+            bnode = bp;
+        }
+    }
+    if (active && t == 0) store_eq(seg_of(I, seg), A, B, g);
+    __syncwarp();
+    // 3. separator system
     int dense_ok = 1;
     if (lane == 0) {
+        // in thread-local storage (L1-resident), not the global scratch: the elimination
+        // reads back what it just wrote
         const int n = nk * M;
-        JT* G = reinterpret_cast<JT*>(I.scr + SCR_DENSE);
-        JT* rhs = reinterpret_cast<JT*>(I.scr + SCR_RHS);
+        JT G[NDENSE * NDENSE];
+        JT rhs[NDENSE];
         for (int q = 0; q < n * n; ++q) G[q] = JT(0);
         for (int j = 0; j + 1 < nk; ++j) {
             const JT* seg = seg_of(I, j);
@@ -757,11 +790,62 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     }
     dense_ok = __shfl_sync(FULL, dense_ok, 0);
     __syncwarp();
-    ok = ok && dense_ok;
-    if (!ok) return false;
-    for (int j = 0; j + 1 < nk; ++j) bcr_backsub(a, I, I.iscr[ISCR_KEPT + j], I.iscr[ISCR_KEPT + j + 1]);
-    bool bad = false;
-    for (int k = lane; k < I.N * M; k += 32) bad |= !isfinite(a.delta[I.nb * M + k]);
+    if (warp_any(bad) || !dense_ok) return false;
+    // 4a. unwind the tree: every lane gets δ at its block ends
+    JT da[M], db[M];
+    if (active && t == 0) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            da[m] = a.delta[(I.nb + na) * M + m];
+            db[m] = a.delta[(I.nb + nbk) * M + m];
+        }
+    }
+#pragma unroll
+    for (int s = 4; s >= 0; --s) {
+        const int step = 1 << s;
+        const bool comb = active && (t % (2 * step)) == 0 && t + step < L;
+        JT dx[M];
+        if (comb) {
+            back_solve(a.rec + (I.nb + xs[s]) * RECW, da, db, dx);
+            JT* dg = a.delta + (I.nb + xs[s]) * M;
+#pragma unroll
+            for (int m = 0; m < M; ++m) dg[m] = dx[m];
+        }
+        JT r1[M], r2[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            r1[m] = __shfl_up_sync(FULL, comb ? dx[m] : JT(0), step);
+            r2[m] = __shfl_up_sync(FULL, db[m], step);
+        }
+        const bool recv = active && (t % (2 * step)) == step;
+        if (recv) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) { da[m] = r1[m]; db[m] = r2[m]; }
+        }
+        if (comb) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) db[m] = dx[m];
+        }
+    }
+    // 4b. back substitution inside the block
+    if (active) {
+        JT* dgl = a.delta + (I.nb + blo) * M;
+#pragma unroll
+        for (int m = 0; m < M; ++m) dgl[m] = da[m];
+        JT dn[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) dn[m] = db[m];
+        for (int c = bhi - 1; c > blo; --c) {
+            JT dc[M];
+            back_solve(a.rec + (I.nb + c) * RECW, da, dn, dc);
+            JT* dg = a.delta + (I.nb + c) * M;
+#pragma unroll
+            for (int m = 0; m < M; ++m) { dg[m] = dc[m]; dn[m] = dc[m]; bad |= !isfinite(dc[m]); }
+        }
+#pragma unroll
+        for (int m = 0; m < M; ++m) bad |= !isfinite(da[m]) || !isfinite(db[m]);
+    }
+    __syncwarp();
     return !warp_any(bad);
 }
 
@@ -779,8 +863,11 @@ BVP_DEV void refresh_yj(const Args& a, const Inst& I) {
     __syncwarp();
 }
 
-// Mixed-precision Newton: while ||F|| from the FP32 residual is above 100 abstol the
-// iterations use it; from then on, and for every convergence decision, the FP64 residual.
+// Mixed-precision Newton: the iterations run on the FP32 residual (stages in FP32, node
+// differences in FP64, roundoff about h|K| eps32) until it falls to 100 abstol or stops
+// improving near that level; the last steps then take the FP64 residual as right-hand side,
+// so the accepted iterate is the one an FP64 Newton reaches (an FP32 right-hand side would
+// move it by cond(J) times its roundoff). Every convergence decision is made in FP64.
 BVP_DEV bool newton_attempt(const Args& a, Inst& I, bool linesearch, int& iters, double& nrm_out) {
     const int lane = lane_id();
     double* y = y_of(a, I, I.cur);
@@ -835,9 +922,10 @@ BVP_DEV bool newton_attempt(const Args& a, Inst& I, bool linesearch, int& iters,
             if (!ok) { nrm_out = nrm; return false; }
         }
         nrm_out = nrm;
-        if (f32 && (!(nrm > switch_tol) || !(nrm < best))) {
-            // close enough, or the FP32 residual stopped improving at its roundoff floor:
-            // continue on the FP64 residual, which restarts the stall bookkeeping
+        if (f32 && (!(nrm > switch_tol) || (!(nrm < best) && best < 10.0 * switch_tol))) {
+            // close enough, or the FP32 residual stopped improving near its roundoff floor
+            // (far from it a non-decreasing step is ordinary Newton behaviour): continue on
+            // the FP64 residual, which restarts the stall bookkeeping
             f32 = false;
             nrm = residual<double>(a, I);
             nrm_out = nrm;
@@ -1087,6 +1175,8 @@ BVP_DEV void init_instance(const Args& a, Inst& I) {
 }
 
 BVP_DEV void finalize_stages(const Args& a, Inst& I) {
+    mesh_setup(a, I);
+    refresh_yj(a, I);
     residual<double>(a, I);
     const double* mesh = mesh_of(a, I, I.cur);
     const double* h = h_of(a, I, I.cur);
@@ -1116,6 +1206,7 @@ BVP_DEV void solve_instance(const Args& a, Inst& I) {
     bool maxed = false;
     while (true) {
         ++s.rounds;
+        mesh_setup(a, I);
         double error_norm = 2 * a.abstol;
         const bool nl_ok = newton(a, I, s);
         if (!a.adaptive) { s.retcode = nl_ok ? RET_SUCCESS : RET_FAILURE; info_ok = nl_ok; break; }
@@ -1191,14 +1282,29 @@ BVP_DEV Inst make_inst(const Args& a, int q) {
 // ---- kernels ---------------------------------------------------------------------------------
 // Persistent fused solve: each warp repeatedly takes the next instance from the work
 // counter and runs its complete adaptive solve.
+// Per-warp scratch in shared memory when it fits (it is read back right after being
+// written, by other lanes of the warp); otherwise the global scratch arrays.
+namespace bvp {
+constexpr int WARPS_PER_BLOCK = 4;
+constexpr bool SCR_SMEM = WARPS_PER_BLOCK * (SCRW * 8 + ISCRW * 4) <= 40 * 1024;
+constexpr int SM_SCRW = SCR_SMEM ? SCRW : 1;
+constexpr int SM_ISCRW = SCR_SMEM ? ISCRW : 1;
+}  // namespace bvp
+
+// Persistent fused solve: each warp repeatedly takes the next instance from the work
+// counter and runs its complete adaptive solve.
 extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::Args a) {
+    __shared__ double s_scr[bvp::WARPS_PER_BLOCK][bvp::SM_SCRW];
+    __shared__ int s_iscr[bvp::WARPS_PER_BLOCK][bvp::SM_ISCRW];
     const int lane = bvp::lane_id();
+    const int w = threadIdx.x >> 5;
     while (true) {
         int k = 0;
         if (lane == 0) k = atomicAdd(a.work_counter, 1);
         k = __shfl_sync(bvp::FULL, k, 0);
         if (k >= a.n_inst) break;
         bvp::Inst I = bvp::make_inst(a, a.order[k]);
+        if (bvp::SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
         bvp::solve_instance(a, I);
     }
 }
@@ -1206,22 +1312,35 @@ extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::
 // Stage kernels on caller-provided (mesh, y) in buffer 0 with N = st[q].N. Used by the
 // per-kernel parity tests; stage: 0 residual (F, K, BC residual), 1 Jacobian blocks,
 // 2 Newton direction (residual + Jacobian + factor/solve), 3 defect (residual + defect).
+// The scratch ends in the global arrays for the host to read.
 extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, int stage, double* out_norm) {
+    __shared__ double s_scr[bvp::WARPS_PER_BLOCK][bvp::SM_SCRW];
+    __shared__ int s_iscr[bvp::WARPS_PER_BLOCK][bvp::SM_ISCRW];
     const int lane = bvp::lane_id();
+    const int w = threadIdx.x >> 5;
     while (true) {
         int k = 0;
         if (lane == 0) k = atomicAdd(a.work_counter, 1);
         k = __shfl_sync(bvp::FULL, k, 0);
         if (k >= a.n_inst) break;
         bvp::Inst I = bvp::make_inst(a, a.order[k]);
+        double* g_scr = I.scr;
+        int* g_iscr = I.iscr;
+        if (bvp::SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
         I.N = a.st[I.q].N;
         I.cur = 0;
+        bvp::mesh_setup(a, I);
         bvp::refresh_yj(a, I);
         double v = bvp::residual<double>(a, I);
         if (stage >= 1 && stage <= 2) bvp::jacobian(a, I);
         if (stage == 2) v = bvp::linear_solve(a, I) ? 0.0 : 1.0;
         if (stage == 3) v = bvp::defect(a, I);
         if (lane == 0) out_norm[I.q] = v;
+        __syncwarp();
+        if (bvp::SCR_SMEM) {
+            for (int q = lane; q < bvp::SCRW; q += 32) g_scr[q] = I.scr[q];
+            for (int q = lane; q < bvp::ISCRW; q += 32) g_iscr[q] = I.iscr[q];
+        }
         __syncwarp();
     }
 }

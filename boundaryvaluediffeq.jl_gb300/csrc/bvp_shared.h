@@ -57,7 +57,6 @@ struct BvpArgs {
     BVP_JT_PTR* Sb;                // [tot][M][M]
     BVP_JT_PTR* Rb;                // [tot][M][M]
     BVP_JT_PTR* rec;               // [tot][RECW]
-    BVP_JT_PTR* eq;                // [2][tot][EQW]
     BVP_JT_PTR* delta;             // [tot][M]
     BVP_JT_PTR* yj;                // [tot][M]  current iterate in the Jacobian precision
     BVP_JT_PTR* Fj;                // [tot][M]  collocation residual in the Jacobian precision
@@ -69,8 +68,8 @@ struct BvpArgs {
 // Scratch layout as a function of (M, order, BC evaluation points, two-point).
 struct BvpLayout {
     int M, S, SS, NSX, NSXA, EQW, RECW, NBCB, KMAX, NDENSE;
-    int SCR_BCRES, SCR_BCBLK, SCR_SEG, SCR_DENSE, SCR_RHS, SCR_UA, SCRW;
-    int ISCR_NK, ISCR_KEPT, ISCR_NB, ISCR_BNODE, ISCR_UNODE, ISCR_UIN, ISCRW;
+    int SCR_BCRES, SCR_BCBLK, SCR_SEG, SCR_UA, SCR_BCW, SCRW;
+    int ISCR_NK, ISCR_KEPT, ISCR_NB, ISCR_BNODE, ISCR_UNODE, ISCR_UIN, ISCR_LOFF, ISCRW;
 };
 
 #ifdef __CUDACC_RTC__
@@ -94,16 +93,16 @@ BVP_LAYOUT_FN BvpLayout bvp_make_layout(int M, int order, int nbc, int twopoint)
     L.SCR_BCRES = 0;
     L.SCR_BCBLK = L.SCR_BCRES + M;
     L.SCR_SEG = L.SCR_BCBLK + L.NBCB * M * M;
-    L.SCR_DENSE = L.SCR_SEG + (L.KMAX - 1) * L.EQW;
-    L.SCR_RHS = L.SCR_DENSE + L.NDENSE * L.NDENSE;
-    L.SCR_UA = L.SCR_RHS + L.NDENSE;
-    L.SCRW = L.SCR_UA + (twopoint ? 2 : nbc) * M;
+    L.SCR_UA = L.SCR_SEG + (L.KMAX - 1) * L.EQW;
+    L.SCR_BCW = L.SCR_UA + (twopoint ? 2 : nbc) * M;
+    L.SCRW = L.SCR_BCW + (twopoint ? 2 : nbc) * L.SS;
     L.ISCR_NK = 0;
     L.ISCR_KEPT = 1;
     L.ISCR_NB = L.ISCR_KEPT + L.KMAX;
     L.ISCR_BNODE = L.ISCR_NB + 1;
     L.ISCR_UNODE = L.ISCR_BNODE + L.NBCB;
     L.ISCR_UIN = L.ISCR_UNODE + (twopoint ? 2 : nbc);
-    L.ISCRW = L.ISCR_UIN + (twopoint ? 2 : nbc);
+    L.ISCR_LOFF = L.ISCR_UIN + (twopoint ? 2 : nbc);
+    L.ISCRW = L.ISCR_LOFF + L.KMAX + 1;
     return L;
 }

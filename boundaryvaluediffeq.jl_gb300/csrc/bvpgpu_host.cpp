@@ -297,7 +297,7 @@ static bvp_status ensure_arena(bvp_handle* h, long long tot, int n, long long y0
               ensure_dev(h->d_err, T * 8) && ensure_dev(h->d_inc, T * M * 8) &&
               ensure_dev(h->d_iold, T * 4) && ensure_dev(h->d_Sb, T * M * M * js) &&
               ensure_dev(h->d_Rb, T * M * M * js) && ensure_dev(h->d_rec, T * L.RECW * js) &&
-              ensure_dev(h->d_eq, 2 * T * L.EQW * js) && ensure_dev(h->d_delta, T * M * js) &&
+              ensure_dev(h->d_delta, T * M * js) &&
               ensure_dev(h->d_yj, T * M * js) && ensure_dev(h->d_Fj, T * M * js) &&
               ensure_dev(h->d_scr, size_t(n) * L.SCRW * 8) && ensure_dev(h->d_iscr, size_t(n) * L.ISCRW * 4) &&
               ensure_dev(h->d_st, size_t(n) * sizeof(BvpInstState)) && ensure_dev(h->d_order, size_t(n) * 4) &&
@@ -359,7 +359,6 @@ static void fill_args(bvp_handle* h, BvpArgs& a, int n, long long tot, int y0_mo
     a.Sb = h->d_Sb.p;
     a.Rb = h->d_Rb.p;
     a.rec = h->d_rec.p;
-    a.eq = h->d_eq.p;
     a.delta = h->d_delta.p;
     a.yj = h->d_yj.p;
     a.Fj = h->d_Fj.p;

@@ -62,8 +62,9 @@ typedef struct {
     int32_t stall_steps;          /* Newton stops after this many non-improving steps */
     int32_t jac_precision;        /* 32: FP32 Jacobian blocks and factorisation, 64: FP64 */
     int32_t want_stages;          /* 1: keep K and the interpolant stages for dense output */
-    int32_t fp32_phase;           /* 1: Newton iterates on an FP32 residual while ||F|| > 100 abstol
-                                     (jac_precision 32 only); convergence is always decided in FP64 */
+    int32_t fp32_phase;           /* 1: Newton iterates on an FP32 residual down to 100 abstol
+                                     (jac_precision 32 only); the final steps and every
+                                     convergence decision use the FP64 residual */
     double abstol;
     double defect_threshold;
     double divergence_factor;     /* Newton stops when ||F|| exceeds this times its start */
