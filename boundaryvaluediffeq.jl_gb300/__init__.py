@@ -7,3 +7,4 @@ factorisation and the defect estimate, driven per instance by a persistent kerne
 from . import problems  # noqa: F401
 from ._lib import build_library, load_library, LIB_PATH, EXPORTS  # noqa: F401
 from .solver import BatchSolver, BatchResult, BVPError, RET_SUCCESS, RET_FAILURE, RET_MAXITERS  # noqa: F401
+from .surrogate import MLP, Surrogate, resample_host  # noqa: F401

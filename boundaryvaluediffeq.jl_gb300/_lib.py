@@ -94,9 +94,9 @@ def build_library(verbose: bool = False, force: bool = False, check_problems=Non
         _write_embedded()
         jobs = []
         tmp = LIB_PATH + f".tmp{os.getpid()}"
-        host_cmd = [NVCC, "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", ARCH,
+        host_cmd = [NVCC, "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", ARCH, "-lineinfo",
                     "-I", INCLUDE, "-I", CSRC, "-I", BUILD, os.path.join(CSRC, "bvpgpu_host.cpp"),
-                    "-o", tmp, "-lnvrtc", "-ldl"]
+                    os.path.join(CSRC, "bvp_mlp.cu"), "-o", tmp, "-lnvrtc", "-ldl"]
         jobs.append(subprocess.Popen(host_cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
         checks = check_problems if check_problems is not None else [
             (P.PENDULUM, 4, 0), (P.SINGULAR_PERTURBATION, 6, 0)]
@@ -155,6 +155,9 @@ class Results(C.Structure):
 
 EXPORTS = ("bvp_default_options", "bvp_create", "bvp_solve_batch", "bvp_solve_batch_device",
            "bvp_fetch_results", "bvp_get_solution", "bvp_get_packed", "bvp_eval_stage",
+           "bvp_dense_output", "bvp_mlp_create", "bvp_mlp_num_params", "bvp_mlp_set_params",
+           "bvp_mlp_get_params", "bvp_mlp_set_normalization", "bvp_mlp_forward", "bvp_mlp_loss_grad",
+           "bvp_mlp_train", "bvp_mlp_forward_device", "bvp_resample_guess_device", "bvp_mlp_destroy",
            "bvp_last_timing", "bvp_stream", "bvp_last_error", "bvp_destroy")
 
 
@@ -183,6 +186,31 @@ def load_library(path: str | None = None):
     lib.bvp_get_packed.restype = C.c_int
     lib.bvp_eval_stage.argtypes = [vp, i32, i32, f64p, i32p, f64p, f64p] + [f64p] * 8
     lib.bvp_eval_stage.restype = C.c_int
+    lib.bvp_dense_output.argtypes = [vp, i32, f64p, i32, f64p]
+    lib.bvp_dense_output.restype = C.c_int
+    f32p = C.POINTER(C.c_float)
+    lib.bvp_mlp_create.argtypes = [i32, i32p, C.POINTER(vp)]
+    lib.bvp_mlp_create.restype = C.c_int
+    lib.bvp_mlp_num_params.argtypes = [vp]
+    lib.bvp_mlp_num_params.restype = C.c_int64
+    lib.bvp_mlp_set_params.argtypes = [vp, f32p]
+    lib.bvp_mlp_set_params.restype = C.c_int
+    lib.bvp_mlp_get_params.argtypes = [vp, f32p]
+    lib.bvp_mlp_get_params.restype = C.c_int
+    lib.bvp_mlp_set_normalization.argtypes = [vp, f32p, f32p, f32p, f32p]
+    lib.bvp_mlp_set_normalization.restype = C.c_int
+    lib.bvp_mlp_forward.argtypes = [vp, i32, f32p, f32p]
+    lib.bvp_mlp_forward.restype = C.c_int
+    lib.bvp_mlp_loss_grad.argtypes = [vp, i32, f32p, f32p, f32p, f32p]
+    lib.bvp_mlp_loss_grad.restype = C.c_int
+    lib.bvp_mlp_train.argtypes = [vp, i32, f32p, f32p, i32, i32, C.c_float, C.c_uint64, f32p]
+    lib.bvp_mlp_train.restype = C.c_int
+    lib.bvp_mlp_forward_device.argtypes = [vp, i32, vp, vp, vp]
+    lib.bvp_mlp_forward_device.restype = C.c_int
+    lib.bvp_resample_guess_device.argtypes = [i32, i32, i32, vp, vp, vp, vp, vp, vp]
+    lib.bvp_resample_guess_device.restype = C.c_int
+    lib.bvp_mlp_destroy.argtypes = [vp]
+    lib.bvp_mlp_destroy.restype = None
     lib.bvp_last_timing.argtypes = [vp, f64p]
     lib.bvp_last_timing.restype = C.c_int
     lib.bvp_stream.argtypes = [vp]

@@ -1366,6 +1366,42 @@ extern "C" __global__ void bvp_pack(const bvp::Args a, const long long* out_off,
     }
 }
 
+// Dense output of the last solve (needs want_stages): u(t) or u'(t) at nq query times per
+// instance through the MIRK interpolant (interpolation.jl:17-204: interval(mesh, t),
+// τ = (t - t_i)/h_i, u = y_i + h Σ w_r(τ) K_r, u' = Σ w'_r(τ) K_r). One warp per instance,
+// lanes over queries.
+extern "C" __global__ void bvp_dense(const bvp::Args a, int nq, const double* tq, int deriv, double* out) {
+    using namespace bvp;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = lane_id();
+    if (warp >= a.n_inst) return;
+    const int q = warp;
+    const long long nb = a.node_off[q];
+    const int N = a.st[q].N;
+    const double* mesh = a.mesh + nb;
+    const double* y = a.y + nb * M;
+    for (int j = lane; j < nq; j += 32) {
+        const double t = tq[(long long)q * nq + j];
+        const int i = interval_of(mesh, N, t);
+        const double dt = a.h[nb + i];
+        double w[SS], wp[SS];
+        interp_weights<double>((t - mesh[i]) / dt, w, wp);
+        const double* wv = deriv ? wp : w;
+        const double* Kg = a.K + (nb + i) * (S * M);
+        const double* KIg = a.KI + (nb + i) * (NSXA * M);
+        double* o = out + ((long long)q * nq + j) * M;
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            double acc = Kg[m] * wv[0];
+#pragma unroll
+            for (int r = 1; r < S; ++r) acc += Kg[r * M + m] * wv[r];
+#pragma unroll
+            for (int qq = 0; qq < NSX; ++qq) acc += KIg[qq * M + m] * wv[S + qq];
+            o[m] = deriv ? acc : acc * dt + y[i * M + m];
+        }
+    }
+}
+
 // Device-side layout constants, checked against the host's at handle creation.
 extern "C" __global__ void bvp_layout_probe(int* out) {
     out[0] = bvp::SCRW;

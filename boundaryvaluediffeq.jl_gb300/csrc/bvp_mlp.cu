@@ -1,0 +1,485 @@
+// Surrogate warm start: a GELU multilayer perceptron with BF16 weights and activations and
+// FP32 accumulation, trained and evaluated by hand-written kernels (tensor-core GEMM with
+// mma.sync m16n8k16, bias/GELU epilogues, MSE loss, Adam), plus the kernel that resamples
+// grid guesses onto each instance's initial mesh. The reference has no surrogate; its
+// output replaces the constant initial guess copied to every mesh node
+// (lib/BoundaryValueDiffEqCore/src/utils.jl:766-769).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "bvpgpu.h"
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+// ---- GEMM: C (Mr x Nc, fp32, row-major, ldc) = op(A) (Mr x K) * op(B) (K x Nc) ----------
+// op(A)(m,k) = TA ? A[k*lda + m] : A[m*lda + k];  op(B)(k,n) = TB ? B[n*ldb + k] : B[k*ldb + n]
+// 64 x 64 CTA tile, 4 warps of 32 x 32, K steps of 32 staged in shared memory as
+// As[m][k] and Bs[n][k] (k contiguous), the operand layouts of mma.m16n8k16.row.col.
+constexpr int TM = 64, TN = 64, TK = 32, SP = TK + 8;
+
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) gemm_bf16(int Mr, int Nc, int K, const bf16* __restrict__ A, int lda,
+                                                 const bf16* __restrict__ B, int ldb, float* __restrict__ C,
+                                                 int ldc) {
+    __shared__ __align__(16) bf16 As[TM][SP];
+    __shared__ __align__(16) bf16 Bs[TN][SP];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+    const bf16 zero = __float2bfloat16(0.f);
+    for (int k0 = 0; k0 < K; k0 += TK) {
+        for (int e = tid; e < TM * TK; e += 128) {
+            const int mm = e / TK, kk = e % TK;
+            const int gm = m0 + mm, gk = k0 + kk;
+            bf16 v = zero;
+            if (gm < Mr && gk < K) v = TA ? A[(long long)gk * lda + gm] : A[(long long)gm * lda + gk];
+            As[mm][kk] = v;
+        }
+        for (int e = tid; e < TN * TK; e += 128) {
+            const int nn = e / TK, kk = e % TK;
+            const int gn = n0 + nn, gk = k0 + kk;
+            bf16 v = zero;
+            if (gn < Nc && gk < K) v = TB ? B[(long long)gn * ldb + gk] : B[(long long)gk * ldb + gn];
+            Bs[nn][kk] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < TK; kk += 16) {
+            uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = wm + i * 16;
+                af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r + g][kk + 2 * t]);
+                af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + g + 8][kk + 2 * t]);
+                af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r + g][kk + 2 * t + 8]);
+                af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + g + 8][kk + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = wn + j * 8;
+                bfr[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[c + g][kk + 2 * t]);
+                bfr[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[c + g][kk + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = m0 + wm + i * 16 + g, c = n0 + wn + j * 8 + 2 * t;
+            if (r < Mr && c < Nc) C[(long long)r * ldc + c] = acc[i][j][0];
+            if (r < Mr && c + 1 < Nc) C[(long long)r * ldc + c + 1] = acc[i][j][1];
+            if (r + 8 < Mr && c < Nc) C[(long long)(r + 8) * ldc + c] = acc[i][j][2];
+            if (r + 8 < Mr && c + 1 < Nc) C[(long long)(r + 8) * ldc + c + 1] = acc[i][j][3];
+        }
+}
+
+// ---- elementwise kernels -------------------------------------------------------------------
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_d(float z) {
+    return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.3989422804014327f * expf(-0.5f * z * z);
+}
+
+// x_n = (x - mu) / sd as BF16
+__global__ void k_input(int B, int N, const float* x, const float* mu, const float* sd, bf16* h) {
+    const long long n = (long long)B * N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int c = int(e % N);
+        h[e] = __float2bfloat16((x[e] - mu[c]) / sd[c]);
+    }
+}
+
+// Z += b; hidden: H = bf16(gelu(Z)); output: y = Z * sd + mu (when y non-null)
+__global__ void k_bias_act(int B, int N, float* Z, const float* b, bf16* H, float* y, const float* mu,
+                           const float* sd) {
+    const long long n = (long long)B * N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int c = int(e % N);
+        const float z = Z[e] + b[c];
+        Z[e] = z;
+        if (H) H[e] = __float2bfloat16(gelu(z));
+        if (y) y[e] = z * sd[c] + mu[c];
+    }
+}
+
+// MSE on normalised outputs: L = mean((z - (t - mu)/sd)^2); dZ = dL/dz
+__global__ void k_mse(int B, int N, const float* Z, const float* T, const float* mu, const float* sd, float* dZ,
+                      bf16* dZb, float* loss) {
+    const long long n = (long long)B * N;
+    const float s = 1.f / float(n);
+    float part = 0.f;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int c = int(e % N);
+        const float d = Z[e] - (T[e] - mu[c]) / sd[c];
+        part += d * d * s;
+        dZ[e] = 2.f * d * s;
+        dZb[e] = __float2bfloat16(2.f * d * s);
+    }
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, part);
+}
+
+// dZ = dH * gelu'(Z) (fp32 and bf16 copies)
+__global__ void k_gelu_bwd(int B, int N, const float* dH, const float* Z, float* dZ, bf16* dZb) {
+    const long long n = (long long)B * N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const float v = dH[e] * gelu_d(Z[e]);
+        dZ[e] = v;
+        dZb[e] = __float2bfloat16(v);
+    }
+}
+
+// db[c] = sum_r dZ[r][c]
+__global__ void k_colsum(int B, int N, const float* dZ, float* db) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    float s = 0.f;
+    for (int r = 0; r < B; ++r) s += dZ[(long long)r * N + c];
+    db[c] = s;
+}
+
+__global__ void k_adam(long long n, float* w, const float* g, float* m, float* v, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const float gg = g[e];
+        const float mm = b1 * m[e] + (1.f - b1) * gg;
+        const float vv = b2 * v[e] + (1.f - b2) * gg * gg;
+        m[e] = mm;
+        v[e] = vv;
+        w[e] -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+    }
+}
+
+__global__ void k_to_bf16(long long n, const float* src, bf16* dst) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        dst[e] = __float2bfloat16(src[e]);
+}
+
+__global__ void k_gather(int B, int N, const int* idx, const float* src, float* dst) {
+    const long long n = (long long)B * N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const long long r = e / N;
+        dst[e] = src[(long long)idx[r] * N + e % N];
+    }
+}
+
+// linear resampling of a uniform-grid guess onto each instance's uniform initial mesh
+__global__ void k_resample(int n_inst, int n_grid, int M, const float* grid, const double* tspans, const int* nint,
+                           const long long* off, double* y0) {
+    const int q = blockIdx.x;
+    if (q >= n_inst) return;
+    const int n = nint[q];
+    const float* gq = grid + (long long)q * n_grid * M;
+    double* out = y0 + off[q] * M;
+    for (int j = threadIdx.x; j <= n; j += blockDim.x) {
+        const double s = double(j) / double(n) * double(n_grid - 1);
+        int i0 = int(floor(s));
+        i0 = i0 < 0 ? 0 : (i0 > n_grid - 2 ? n_grid - 2 : i0);
+        const double f = s - i0;
+        for (int m = 0; m < M; ++m)
+            out[(long long)j * M + m] = (1.0 - f) * double(gq[i0 * M + m]) + f * double(gq[(i0 + 1) * M + m]);
+    }
+}
+
+int grid1d(long long n) { return int(std::min<long long>((n + 255) / 256, 4096)); }
+
+}  // namespace
+
+struct bvp_mlp_s {
+    int L = 0;
+    std::vector<int> w;
+    std::vector<long long> offW, offb;
+    long long np = 0;
+    float *d_p = nullptr, *d_g = nullptr, *d_m = nullptr, *d_v = nullptr;
+    bf16* d_pb = nullptr;  // BF16 copy of the parameters (the W blocks are used)
+    float *d_norm = nullptr;  // in_mu (w0), in_sd (w0), out_mu (wL), out_sd (wL)
+    int cap = 0;
+    std::vector<float*> Z;   // per layer pre-activations (cap x w[l+1])
+    std::vector<bf16*> H;    // per layer inputs (cap x w[l]); H[0] the input
+    float *d_dH = nullptr, *d_dZ = nullptr, *d_x = nullptr, *d_t = nullptr, *d_y = nullptr, *d_loss = nullptr;
+    bf16* d_dZb = nullptr;
+    int* d_idx = nullptr;
+    cudaStream_t stream = nullptr;
+    long long step = 0;
+    std::string err;
+};
+
+namespace {
+
+bool mlp_reserve(bvp_mlp* n, int batch) {
+    if (batch <= n->cap) return true;
+    for (auto p : n->Z) cudaFree(p);
+    for (auto p : n->H) cudaFree(p);
+    cudaFree(n->d_dH); cudaFree(n->d_dZ); cudaFree(n->d_dZb); cudaFree(n->d_x); cudaFree(n->d_t);
+    cudaFree(n->d_y); cudaFree(n->d_idx);
+    n->Z.assign(n->L, nullptr);
+    n->H.assign(n->L, nullptr);
+    int wmax = 0;
+    for (int v : n->w) wmax = std::max(wmax, v);
+    bool ok = true;
+    for (int l = 0; l < n->L; ++l) {
+        ok = ok && cudaMalloc(&n->Z[l], size_t(batch) * n->w[l + 1] * 4) == cudaSuccess;
+        ok = ok && cudaMalloc(&n->H[l], size_t(batch) * n->w[l] * 2) == cudaSuccess;
+    }
+    ok = ok && cudaMalloc(&n->d_dH, size_t(batch) * wmax * 4) == cudaSuccess;
+    ok = ok && cudaMalloc(&n->d_dZ, size_t(batch) * wmax * 4) == cudaSuccess;
+    ok = ok && cudaMalloc(&n->d_dZb, size_t(batch) * wmax * 2) == cudaSuccess;
+    ok = ok && cudaMalloc(&n->d_x, size_t(batch) * n->w[0] * 4) == cudaSuccess;
+    ok = ok && cudaMalloc(&n->d_t, size_t(batch) * n->w[n->L] * 4) == cudaSuccess;
+    ok = ok && cudaMalloc(&n->d_y, size_t(batch) * n->w[n->L] * 4) == cudaSuccess;
+    ok = ok && cudaMalloc(&n->d_idx, size_t(batch) * 4) == cudaSuccess;
+    if (ok) n->cap = batch;
+    return ok;
+}
+
+void gemm(cudaStream_t s, bool ta, bool tb, int Mr, int Nc, int K, const bf16* A, int lda, const bf16* B, int ldb,
+          float* C, int ldc) {
+    dim3 grid((Nc + TN - 1) / TN, (Mr + TM - 1) / TM);
+    if (!ta && !tb) gemm_bf16<false, false><<<grid, 128, 0, s>>>(Mr, Nc, K, A, lda, B, ldb, C, ldc);
+    else if (ta && !tb) gemm_bf16<true, false><<<grid, 128, 0, s>>>(Mr, Nc, K, A, lda, B, ldb, C, ldc);
+    else if (!ta && tb) gemm_bf16<false, true><<<grid, 128, 0, s>>>(Mr, Nc, K, A, lda, B, ldb, C, ldc);
+    else gemm_bf16<true, true><<<grid, 128, 0, s>>>(Mr, Nc, K, A, lda, B, ldb, C, ldc);
+}
+
+// forward of a batch already in n->d_x; writes Z of every layer, y when y != nullptr
+void forward(bvp_mlp* n, int B, const float* d_x, float* d_y) {
+    const int L = n->L;
+    const float* nrm = n->d_norm;
+    const long long w0 = n->w[0], wL = n->w[L];
+    k_input<<<grid1d(B * w0), 256, 0, n->stream>>>(B, int(w0), d_x, nrm, nrm + w0, n->H[0]);
+    for (int l = 0; l < L; ++l) {
+        const int ni = n->w[l], no = n->w[l + 1];
+        gemm(n->stream, false, false, B, no, ni, n->H[l], ni, n->d_pb + n->offW[l], no, n->Z[l], no);
+        const bool last = l == L - 1;
+        k_bias_act<<<grid1d((long long)B * no), 256, 0, n->stream>>>(
+            B, no, n->Z[l], n->d_p + n->offb[l], last ? nullptr : n->H[l + 1], last ? d_y : nullptr,
+            nrm + 2 * w0, nrm + 2 * w0 + wL);
+    }
+}
+
+// backward of the MSE loss for the batch in d_x / d_t; gradient into n->d_g, loss added to *d_loss
+void backward(bvp_mlp* n, int B, const float* d_t) {
+    const int L = n->L;
+    const long long w0 = n->w[0], wL = n->w[L];
+    const float* nrm = n->d_norm;
+    k_mse<<<grid1d(B * wL), 256, 0, n->stream>>>(B, int(wL), n->Z[L - 1], d_t, nrm + 2 * w0, nrm + 2 * w0 + wL,
+                                                  n->d_dZ, n->d_dZb, n->d_loss);
+    for (int l = L - 1; l >= 0; --l) {
+        const int ni = n->w[l], no = n->w[l + 1];
+        // dW = H_l^T dZ (ni x no), db = colsum dZ
+        gemm(n->stream, true, false, ni, no, B, n->H[l], ni, n->d_dZb, no, n->d_g + n->offW[l], no);
+        k_colsum<<<(no + 127) / 128, 128, 0, n->stream>>>(B, no, n->d_dZ, n->d_g + n->offb[l]);
+        if (l > 0) {
+            // dH = dZ W^T (B x ni), then through the activation of layer l-1
+            gemm(n->stream, false, true, B, ni, no, n->d_dZb, no, n->d_pb + n->offW[l], no, n->d_dH, ni);
+            k_gelu_bwd<<<grid1d((long long)B * ni), 256, 0, n->stream>>>(B, ni, n->d_dH, n->Z[l - 1], n->d_dZ,
+                                                                          n->d_dZb);
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+bvp_status bvp_mlp_create(int32_t n_layers, const int32_t* widths, bvp_mlp** out) {
+    if (!out || n_layers < 1 || n_layers > 16 || !widths) return BVP_ERR_INVALID;
+    *out = nullptr;
+    for (int l = 0; l <= n_layers; ++l)
+        if (widths[l] < 1 || widths[l] > 8192) return BVP_ERR_INVALID;
+    bvp_mlp* n = new bvp_mlp_s();
+    n->L = n_layers;
+    n->w.assign(widths, widths + n_layers + 1);
+    long long o = 0;
+    for (int l = 0; l < n_layers; ++l) {
+        n->offW.push_back(o);
+        o += (long long)n->w[l] * n->w[l + 1];
+        n->offb.push_back(o);
+        o += n->w[l + 1];
+    }
+    n->np = o;
+    *out = n;
+    const long long w0 = n->w[0], wL = n->w[n_layers];
+    bool ok = cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaMalloc(&n->d_p, o * 4) == cudaSuccess && cudaMalloc(&n->d_g, o * 4) == cudaSuccess &&
+         cudaMalloc(&n->d_m, o * 4) == cudaSuccess && cudaMalloc(&n->d_v, o * 4) == cudaSuccess &&
+         cudaMalloc(&n->d_pb, o * 2) == cudaSuccess && cudaMalloc(&n->d_norm, (2 * w0 + 2 * wL) * 4) == cudaSuccess &&
+         cudaMalloc(&n->d_loss, 4) == cudaSuccess;
+    if (!ok) { n->err = "allocation failed"; return BVP_ERR_CUDA; }
+    std::vector<float> nrm(2 * w0 + 2 * wL);
+    for (long long k = 0; k < w0; ++k) { nrm[k] = 0.f; nrm[w0 + k] = 1.f; }
+    for (long long k = 0; k < wL; ++k) { nrm[2 * w0 + k] = 0.f; nrm[2 * w0 + wL + k] = 1.f; }
+    cudaMemcpy(n->d_norm, nrm.data(), nrm.size() * 4, cudaMemcpyHostToDevice);
+    cudaMemset(n->d_p, 0, o * 4);
+    cudaMemset(n->d_pb, 0, o * 2);
+    return BVP_OK;
+}
+
+int64_t bvp_mlp_num_params(bvp_mlp* n) { return n ? n->np : 0; }
+
+bvp_status bvp_mlp_set_params(bvp_mlp* n, const float* params) {
+    if (!n || !params) return BVP_ERR_INVALID;
+    if (cudaMemcpy(n->d_p, params, n->np * 4, cudaMemcpyHostToDevice) != cudaSuccess) return BVP_ERR_CUDA;
+    cudaMemset(n->d_m, 0, n->np * 4);
+    cudaMemset(n->d_v, 0, n->np * 4);
+    n->step = 0;
+    k_to_bf16<<<grid1d(n->np), 256, 0, n->stream>>>(n->np, n->d_p, n->d_pb);
+    return cudaStreamSynchronize(n->stream) == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
+}
+
+bvp_status bvp_mlp_get_params(bvp_mlp* n, float* params) {
+    if (!n || !params) return BVP_ERR_INVALID;
+    cudaStreamSynchronize(n->stream);
+    return cudaMemcpy(params, n->d_p, n->np * 4, cudaMemcpyDeviceToHost) == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
+}
+
+// Input and output normalisation: x_n = (x - in_mu)/in_sd, y = z out_sd + out_mu.
+bvp_status bvp_mlp_set_normalization(bvp_mlp* n, const float* in_mu, const float* in_sd, const float* out_mu,
+                                     const float* out_sd) {
+    if (!n || !in_mu || !in_sd || !out_mu || !out_sd) return BVP_ERR_INVALID;
+    const long long w0 = n->w[0], wL = n->w[n->L];
+    std::vector<float> nrm(2 * w0 + 2 * wL);
+    std::memcpy(nrm.data(), in_mu, w0 * 4);
+    std::memcpy(nrm.data() + w0, in_sd, w0 * 4);
+    std::memcpy(nrm.data() + 2 * w0, out_mu, wL * 4);
+    std::memcpy(nrm.data() + 2 * w0 + wL, out_sd, wL * 4);
+    return cudaMemcpy(n->d_norm, nrm.data(), nrm.size() * 4, cudaMemcpyHostToDevice) == cudaSuccess ? BVP_OK
+                                                                                                  : BVP_ERR_CUDA;
+}
+
+bvp_status bvp_mlp_forward_device(bvp_mlp* n, int32_t B, const float* d_x, float* d_y, void* stream) {
+    if (!n || B < 1 || !d_x || !d_y) return BVP_ERR_INVALID;
+    if (!mlp_reserve(n, B)) return BVP_ERR_NOMEM;
+    cudaStream_t prev = n->stream;
+    if (stream) n->stream = static_cast<cudaStream_t>(stream);
+    forward(n, B, d_x, d_y);
+    const cudaError_t e = cudaGetLastError();
+    n->stream = prev;
+    return e == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
+}
+
+bvp_status bvp_mlp_forward(bvp_mlp* n, int32_t B, const float* x, float* y) {
+    if (!n || B < 1 || !x || !y) return BVP_ERR_INVALID;
+    if (!mlp_reserve(n, B)) return BVP_ERR_NOMEM;
+    const long long w0 = n->w[0], wL = n->w[n->L];
+    cudaMemcpyAsync(n->d_x, x, B * w0 * 4, cudaMemcpyHostToDevice, n->stream);
+    forward(n, B, n->d_x, n->d_y);
+    cudaMemcpyAsync(y, n->d_y, B * wL * 4, cudaMemcpyDeviceToHost, n->stream);
+    return cudaStreamSynchronize(n->stream) == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
+}
+
+bvp_status bvp_mlp_loss_grad(bvp_mlp* n, int32_t B, const float* x, const float* t, float* loss, float* grad) {
+    if (!n || B < 1 || !x || !t) return BVP_ERR_INVALID;
+    if (!mlp_reserve(n, B)) return BVP_ERR_NOMEM;
+    const long long w0 = n->w[0], wL = n->w[n->L];
+    cudaMemcpyAsync(n->d_x, x, B * w0 * 4, cudaMemcpyHostToDevice, n->stream);
+    cudaMemcpyAsync(n->d_t, t, B * wL * 4, cudaMemcpyHostToDevice, n->stream);
+    cudaMemsetAsync(n->d_loss, 0, 4, n->stream);
+    forward(n, B, n->d_x, nullptr);
+    backward(n, B, n->d_t);
+    if (loss) cudaMemcpyAsync(loss, n->d_loss, 4, cudaMemcpyDeviceToHost, n->stream);
+    if (grad) cudaMemcpyAsync(grad, n->d_g, n->np * 4, cudaMemcpyDeviceToHost, n->stream);
+    return cudaStreamSynchronize(n->stream) == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
+}
+
+bvp_status bvp_mlp_train(bvp_mlp* n, int32_t N, const float* x, const float* t, int32_t epochs, int32_t B, float lr,
+                         uint64_t seed, float* last_loss) {
+    if (!n || N < 1 || !x || !t || epochs < 1 || B < 1) return BVP_ERR_INVALID;
+    B = std::min(B, N);
+    if (!mlp_reserve(n, B)) return BVP_ERR_NOMEM;
+    const long long w0 = n->w[0], wL = n->w[n->L];
+    float *dX = nullptr, *dT = nullptr;
+    int* dperm = nullptr;
+    if (cudaMalloc(&dX, (long long)N * w0 * 4) != cudaSuccess || cudaMalloc(&dT, (long long)N * wL * 4) != cudaSuccess ||
+        cudaMalloc(&dperm, (long long)N * 4) != cudaSuccess) {
+        cudaFree(dX); cudaFree(dT); cudaFree(dperm);
+        return BVP_ERR_NOMEM;
+    }
+    cudaMemcpyAsync(dX, x, (long long)N * w0 * 4, cudaMemcpyHostToDevice, n->stream);
+    cudaMemcpyAsync(dT, t, (long long)N * wL * 4, cudaMemcpyHostToDevice, n->stream);
+    std::mt19937_64 rng(seed);
+    std::vector<int> perm(N);
+    const int steps = N / B;
+    float epoch_loss = 0.f;
+    for (int ep = 0; ep < epochs; ++ep) {
+        for (int i = 0; i < N; ++i) perm[i] = i;
+        std::shuffle(perm.begin(), perm.end(), rng);
+        cudaMemcpyAsync(dperm, perm.data(), (long long)N * 4, cudaMemcpyHostToDevice, n->stream);
+        cudaMemsetAsync(n->d_loss, 0, 4, n->stream);
+        // cosine decay of the step size over the run
+        for (int s = 0; s < steps; ++s) {
+            const double frac = (double(ep) * steps + s) / (double(epochs) * steps);
+            const float lr_s = float(0.5 * lr * (1.0 + std::cos(3.141592653589793 * frac)));
+            k_gather<<<grid1d((long long)B * w0), 256, 0, n->stream>>>(B, int(w0), dperm + (long long)s * B, dX, n->d_x);
+            k_gather<<<grid1d((long long)B * wL), 256, 0, n->stream>>>(B, int(wL), dperm + (long long)s * B, dT, n->d_t);
+            forward(n, B, n->d_x, nullptr);
+            backward(n, B, n->d_t);
+            ++n->step;
+            const float b1 = 0.9f, b2 = 0.999f;
+            const float c1 = 1.f - std::pow(b1, float(n->step)), c2 = 1.f - std::pow(b2, float(n->step));
+            k_adam<<<grid1d(n->np), 256, 0, n->stream>>>(n->np, n->d_p, n->d_g, n->d_m, n->d_v, lr_s, b1, b2, 1e-8f, c1, c2);
+            k_to_bf16<<<grid1d(n->np), 256, 0, n->stream>>>(n->np, n->d_p, n->d_pb);
+        }
+        cudaMemcpyAsync(&epoch_loss, n->d_loss, 4, cudaMemcpyDeviceToHost, n->stream);
+        if (cudaStreamSynchronize(n->stream) != cudaSuccess) break;
+        epoch_loss /= float(std::max(steps, 1));
+    }
+    const cudaError_t e = cudaStreamSynchronize(n->stream);
+    cudaFree(dX); cudaFree(dT); cudaFree(dperm);
+    if (last_loss) *last_loss = epoch_loss;
+    return e == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
+}
+
+bvp_status bvp_resample_guess_device(int32_t n_inst, int32_t n_grid, int32_t M, const float* d_grid,
+                                     const double* d_tspans, const int32_t* d_n_intervals, const int64_t* d_y0_off,
+                                     double* d_y0, void* stream) {
+    if (n_inst < 1 || n_grid < 2 || M < 1 || !d_grid || !d_n_intervals || !d_y0_off || !d_y0) return BVP_ERR_INVALID;
+    (void)d_tspans;  // the grid spans each instance's own tspan
+    k_resample<<<n_inst, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+        n_inst, n_grid, M, d_grid, d_tspans, d_n_intervals, reinterpret_cast<const long long*>(d_y0_off), d_y0);
+    return cudaGetLastError() == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
+}
+
+void bvp_mlp_destroy(bvp_mlp* n) {
+    if (!n) return;
+    for (auto p : n->Z) cudaFree(p);
+    for (auto p : n->H) cudaFree(p);
+    cudaFree(n->d_p); cudaFree(n->d_g); cudaFree(n->d_m); cudaFree(n->d_v); cudaFree(n->d_pb);
+    cudaFree(n->d_norm); cudaFree(n->d_dH); cudaFree(n->d_dZ); cudaFree(n->d_dZb); cudaFree(n->d_x);
+    cudaFree(n->d_t); cudaFree(n->d_y); cudaFree(n->d_loss); cudaFree(n->d_idx);
+    if (n->stream) cudaStreamDestroy(n->stream);
+    delete n;
+}
+
+}  // extern "C"

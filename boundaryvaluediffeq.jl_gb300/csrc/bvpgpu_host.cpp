@@ -52,7 +52,7 @@ struct bvp_handle_s {
     cudaStream_t stream = nullptr;
     cudaLibrary_t lib = nullptr;
     cudaKernel_t k_fused = nullptr, k_stage = nullptr, k_pack = nullptr, k_probe = nullptr,
-                 k_convert = nullptr, k_prep = nullptr;
+                 k_convert = nullptr, k_prep = nullptr, k_dense = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     // device arrays
     DevBuf d_mesh, d_h, d_y, d_ybak, d_ybase, d_K, d_KI, d_F, d_err, d_inc, d_iold, d_Sb, d_Rb,
@@ -229,6 +229,7 @@ static bvp_status compile_and_load(bvp_handle* h) {
     CU(cudaLibraryGetKernel(&h->k_probe, h->lib, "bvp_layout_probe"));
     CU(cudaLibraryGetKernel(&h->k_convert, h->lib, "bvp_convert_params"));
     CU(cudaLibraryGetKernel(&h->k_prep, h->lib, "bvp_prep"));
+    CU(cudaLibraryGetKernel(&h->k_dense, h->lib, "bvp_dense"));
     return BVP_OK;
 }
 
@@ -557,6 +558,33 @@ bvp_status bvp_fetch_results(bvp_handle* h, bvp_results* out) {
         return BVP_OK;
     }
     return finish(h, out);
+}
+
+bvp_status bvp_dense_output(bvp_handle* h, int32_t nq, const double* tq, int32_t deriv, double* out) {
+    if (!h) return BVP_ERR_INVALID;
+    if (!h->have_results && !h->pending_device) return fail(h, BVP_ERR_STATE, "no solve to interpolate");
+    if (!h->opt.want_stages) return fail(h, BVP_ERR_STATE, "dense output needs want_stages = 1");
+    if (nq < 1 || !tq || !out) return fail(h, BVP_ERR_INVALID, "invalid arguments");
+    const int n = h->last_n, M = h->L.M;
+    DevBuf dt, dout;
+    if (!ensure_dev(dt, size_t(n) * nq * 8) || !ensure_dev(dout, size_t(n) * nq * M * 8))
+        return fail(h, BVP_ERR_NOMEM, "device allocation failed");
+    bvp_status s = BVP_OK;
+    do {
+        if (cudaMemcpyAsync(dt.p, tq, size_t(n) * nq * 8, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "H2D"); break; }
+        BvpArgs a;
+        fill_args(h, a, n, h->last_tot, 0, static_cast<const double*>(h->d_params.p), nullptr, nullptr, nullptr, nullptr);
+        int nqq = nq, dv = deriv;
+        const double* tp = static_cast<const double*>(dt.p);
+        double* op = static_cast<double*>(dout.p);
+        void* args[] = {&a, &nqq, &tp, &dv, &op};
+        if (cudaLaunchKernel((const void*)h->k_dense, dim3((n * 32 + 127) / 128), dim3(128), args, 0, h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "dense launch"); break; }
+        if (cudaMemcpyAsync(out, dout.p, size_t(n) * nq * M * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "D2H"); break; }
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "sync"); break; }
+    } while (0);
+    cudaFree(dt.p);
+    cudaFree(dout.p);
+    return s;
 }
 
 bvp_status bvp_last_timing(bvp_handle* h, double* ms2) {

@@ -174,6 +174,15 @@ class BatchSolver:
         self._check(self.lib.bvp_fetch_results(self.h, C.byref(cr)), "bvp_fetch_results")
         return self._collect(r)
 
+    def dense(self, tq, deriv: int = 0):
+        """u(t) (deriv 0) or u'(t) (deriv 1) of every instance of the last solve at the
+        query times tq (n_inst x nq); needs want_stages=1."""
+        tq = np.ascontiguousarray(tq, dtype=np.float64)
+        n, nq = tq.shape
+        out = np.zeros((n, nq, self.M))
+        self._check(self.lib.bvp_dense_output(self.h, nq, f64(tq), deriv, f64(out)), "bvp_dense_output")
+        return out
+
     def timing_ms(self):
         t = np.zeros(2)
         self._check(self.lib.bvp_last_timing(self.h, f64(t)), "bvp_last_timing")

@@ -141,6 +141,50 @@ bvp_status bvp_eval_stage(bvp_handle* h, int32_t stage, int32_t n_inst, const do
                           double* norm, double* F, double* bc_res, double* K, double* S,
                           double* R, double* delta, double* err);
 
+/* Dense output of the last solve (needs options.want_stages = 1): u(t) (deriv 0) or u'(t)
+ * (deriv 1) at nq times per instance; tq is n_inst x nq, out n_inst x nq x M. Replaces
+ * evaluating the returned solution, sol(t) / sol(t, Val{1})
+ * (lib/BoundaryValueDiffEqMIRK/src/interpolation.jl:17-204). */
+bvp_status bvp_dense_output(bvp_handle* h, int32_t nq, const double* tq, int32_t deriv, double* out);
+
+/* ---- surrogate warm start --------------------------------------------------------------
+ * A multilayer perceptron (GELU hidden layers, linear output) with BF16 weights and
+ * activations and FP32 accumulation, trained and evaluated by the library's own tensor-core
+ * kernels. It maps instance parameters to a solution guess on a fixed grid; the reference
+ * has no counterpart: the guess stands in for the constant initial guess that __init copies
+ * to every node (lib/BoundaryValueDiffEqCore/src/utils.jl:766-769) and enters the solve as
+ * the reference's vector-of-arrays initial guess (utils.jl:750-765, y0_mode 1 above).
+ * Parameters are packed as W_1 (w_0 x w_1, row-major), b_1, W_2, b_2, ... in FP32. */
+typedef struct bvp_mlp_s bvp_mlp;
+
+bvp_status bvp_mlp_create(int32_t n_layers, const int32_t* widths, bvp_mlp** out);
+int64_t bvp_mlp_num_params(bvp_mlp* net);
+bvp_status bvp_mlp_set_params(bvp_mlp* net, const float* params);
+bvp_status bvp_mlp_get_params(bvp_mlp* net, float* params);
+/* Input and output scaling applied inside the network: x_n = (x - in_mu) / in_sd on entry,
+ * y = z out_sd + out_mu on exit; the training loss is the MSE of z against the scaled targets. */
+bvp_status bvp_mlp_set_normalization(bvp_mlp* net, const float* in_mu, const float* in_sd,
+                                     const float* out_mu, const float* out_sd);
+/* y = net(x) for a batch (host arrays, batch x w_0 in, batch x w_L out). */
+bvp_status bvp_mlp_forward(bvp_mlp* net, int32_t batch, const float* x, float* y);
+/* Mean-squared-error loss of one batch and its gradient (packed like the parameters). */
+bvp_status bvp_mlp_loss_grad(bvp_mlp* net, int32_t batch, const float* x, const float* t, float* loss,
+                             float* grad);
+/* Adam on minibatches drawn from (x, t) (n samples, host arrays); returns the mean loss of
+ * the last epoch. */
+bvp_status bvp_mlp_train(bvp_mlp* net, int32_t n, const float* x, const float* t, int32_t epochs,
+                         int32_t batch, float lr, uint64_t seed, float* last_loss);
+/* Device-pointer forward on the given stream (cudaStream_t as void*); no synchronisation. */
+bvp_status bvp_mlp_forward_device(bvp_mlp* net, int32_t batch, const float* d_x, float* d_y, void* stream);
+/* Resample guesses given on a uniform grid of n_grid points over each instance's tspan
+ * (grid: n_inst x n_grid x M) onto each instance's uniform initial mesh of n_intervals[i]
+ * intervals by linear interpolation, packed as y0_mode 1 expects. Device pointers; y0_off
+ * (n_inst + 1 offsets, in M-vectors) is the packing. */
+bvp_status bvp_resample_guess_device(int32_t n_inst, int32_t n_grid, int32_t M, const float* d_grid,
+                                     const double* d_tspans, const int32_t* d_n_intervals,
+                                     const int64_t* d_y0_off, double* d_y0, void* stream);
+void bvp_mlp_destroy(bvp_mlp* net);
+
 /* Device time of the last solve's kernels in milliseconds (CUDA events on the handle's
  * stream): [0] whole solve, [1] fused solve kernel. */
 bvp_status bvp_last_timing(bvp_handle* h, double* ms2);
