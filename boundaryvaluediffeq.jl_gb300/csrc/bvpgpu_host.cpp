@@ -58,7 +58,7 @@ struct bvp_handle_s {
     DevBuf d_mesh, d_h, d_y, d_ybak, d_ybase, d_K, d_KI, d_F, d_err, d_inc, d_iold, d_Sb, d_Rb,
         d_rec, d_eq, d_delta, d_yj, d_Fj, d_scr, d_iscr, d_st, d_order, d_cap, d_node_off, d_counter,
         d_params, d_params_j, d_n_init, d_tspans, d_y0, d_y0_off, d_out_off, d_out_mesh,
-        d_out_y, d_out_K, d_out_KI, d_norm;
+        d_out_y, d_out_K, d_out_KI, d_norm, d_feat, d_grid;
     // pinned host staging
     HostBuf h_in, h_st, h_off, h_mesh, h_y, h_K, h_KI;
     // last batch
@@ -66,6 +66,7 @@ struct bvp_handle_s {
     long long last_tot = 0;
     bool have_results = false;
     bool pending_device = false;
+    bool stages_ok = false;  // K and KI on the device belong to the last batch
     int pending_n = 0;
     double timing_ms[2] = {0, 0};
     std::vector<BvpInstState> st;
@@ -308,7 +309,7 @@ static bvp_status ensure_arena(bvp_handle* h, long long tot, int n, long long y0
               ensure_dev(h->d_params_j, size_t(n) * std::max(1, h->desc.n_params) * js) &&
               ensure_dev(h->d_n_init, size_t(n) * 4) && ensure_dev(h->d_tspans, size_t(n) * 16) &&
               ensure_dev(h->d_y0, size_t(std::max<long long>(y0_vals, 1)) * 8) &&
-              ensure_dev(h->d_y0_off, size_t(n) * 8) && ensure_dev(h->d_out_off, size_t(n + 1) * 8) &&
+              ensure_dev(h->d_y0_off, size_t(n + 1) * 8) && ensure_dev(h->d_out_off, size_t(n + 1) * 8) &&
               ensure_dev(h->d_norm, size_t(n) * 8);
     if (!ok) return fail(h, BVP_ERR_NOMEM, "device allocation failed");
     return BVP_OK;
@@ -408,6 +409,7 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
     CU(cudaEventRecord(h->ev[2], h->stream));
     h->last_n = n;
     h->last_tot = tot;
+    h->stages_ok = h->opt.want_stages != 0;
     return BVP_OK;
 }
 
@@ -522,6 +524,126 @@ bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const
     return finish(h, out);
 }
 
+bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t n_features, const float* features,
+                                int32_t n_grid, const double* params, const int32_t* n_intervals,
+                                const double* tspans, const double* y0_plain, bvp_results* out,
+                                int32_t* n_fallback) {
+    if (!h) return BVP_ERR_INVALID;
+    const int M = h->L.M;
+    if (!net || n < 1 || n_features < 1 || !features || n_grid < 2 || !n_intervals || !tspans || !y0_plain ||
+        (h->desc.n_params > 0 && !params))
+        return fail(h, BVP_ERR_INVALID, "invalid arguments");
+    long long tot = 0, y0_vals = 0;
+    for (int q = 0; q < n; ++q) {
+        const int ni = n_intervals[q];
+        if (ni < 1) return fail(h, BVP_ERR_INVALID, "n_intervals must be >= 1");
+        if (!(tspans[2 * q + 1] > tspans[2 * q])) return fail(h, BVP_ERR_INVALID, "tspan must satisfy t0 < t1");
+        tot += std::max(ni, h->opt.max_subintervals) + 1;
+        y0_vals += (long long)(ni + 1) * M;
+    }
+    bvp_status s = ensure_arena(h, tot, n, y0_vals);
+    if (s != BVP_OK) return s;
+    const int P = h->desc.n_params;
+    const size_t b_params = size_t(n) * P * 8, b_ni = size_t(n) * 4, b_ts = size_t(n) * 16,
+                 b_off = size_t(n + 1) * 8;
+    if (!ensure_host(h->h_in, b_params + b_ni + b_ts + b_off + 64)) return fail(h, BVP_ERR_NOMEM, "pinned allocation failed");
+    char* hp = static_cast<char*>(h->h_in.p);
+    std::memcpy(hp, params, b_params);
+    std::memcpy(hp + b_params, n_intervals, b_ni);
+    std::memcpy(hp + b_params + b_ni, tspans, b_ts);
+    int64_t* yoff = reinterpret_cast<int64_t*>(hp + b_params + b_ni + b_ts);
+    {
+        long long acc = 0;
+        for (int q = 0; q < n; ++q) { yoff[q] = acc; acc += n_intervals[q] + 1; }
+        yoff[n] = acc;
+    }
+    if (b_params) CU(cudaMemcpyAsync(h->d_params.p, hp, b_params, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_n_init.p, hp + b_params, b_ni, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_tspans.p, hp + b_params + b_ni, b_ts, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_y0_off.p, yoff, b_off, cudaMemcpyHostToDevice, h->stream));
+    // features and the network's grid output
+    const int nfeat = n_features;
+    if (!ensure_dev(h->d_feat, size_t(n) * nfeat * 4) || !ensure_dev(h->d_grid, size_t(n) * n_grid * M * 4))
+        return fail(h, BVP_ERR_NOMEM, "device allocation failed");
+    CU(cudaMemcpyAsync(h->d_feat.p, features, size_t(n) * nfeat * 4, cudaMemcpyHostToDevice, h->stream));
+    if (bvp_mlp_forward_device(net, n, static_cast<const float*>(h->d_feat.p), static_cast<float*>(h->d_grid.p),
+                               h->stream) != BVP_OK)
+        return fail(h, BVP_ERR_CUDA, "surrogate forward failed");
+    if (bvp_resample_guess_device(n, n_grid, M, static_cast<const float*>(h->d_grid.p),
+                                  static_cast<const double*>(h->d_tspans.p), static_cast<const int*>(h->d_n_init.p),
+                                  static_cast<const int64_t*>(h->d_y0_off.p), static_cast<double*>(h->d_y0.p),
+                                  h->stream) != BVP_OK)
+        return fail(h, BVP_ERR_CUDA, "guess resampling failed");
+    s = launch_solve(h, n, tot, 1, static_cast<const double*>(h->d_params.p), static_cast<const int*>(h->d_n_init.p),
+                     static_cast<const double*>(h->d_tspans.p), static_cast<const double*>(h->d_y0.p),
+                     static_cast<const long long*>(h->d_y0_off.p));
+    if (s != BVP_OK) return s;
+    s = finish(h, nullptr);
+    if (s != BVP_OK) return s;
+    // plain-guess fallback for the instances the warm start did not bring to convergence
+    std::vector<int> bad;
+    for (int q = 0; q < n; ++q)
+        if (h->st[q].retcode != BVP_RET_SUCCESS) bad.push_back(q);
+    if (n_fallback) *n_fallback = int(bad.size());
+    if (!bad.empty()) {
+        std::vector<BvpInstState> st0 = h->st;
+        std::vector<int64_t> off0 = h->offsets;
+        const long long tot0 = off0[n];
+        std::vector<double> mesh0(static_cast<const double*>(h->h_mesh.p), static_cast<const double*>(h->h_mesh.p) + tot0);
+        std::vector<double> y00(static_cast<const double*>(h->h_y.p), static_cast<const double*>(h->h_y.p) + tot0 * M);
+        const int nb = int(bad.size());
+        std::vector<double> bp(size_t(nb) * P), bts(size_t(nb) * 2), by0(size_t(nb) * M);
+        std::vector<int32_t> bni(nb);
+        for (int k = 0; k < nb; ++k) {
+            const int q = bad[k];
+            for (int c = 0; c < P; ++c) bp[size_t(k) * P + c] = params[size_t(q) * P + c];
+            bts[2 * k] = tspans[2 * q]; bts[2 * k + 1] = tspans[2 * q + 1];
+            for (int m = 0; m < M; ++m) by0[size_t(k) * M + m] = y0_plain[size_t(q) * M + m];
+            bni[k] = n_intervals[q];
+        }
+        s = bvp_solve_batch(h, nb, bp.data(), bni.data(), bts.data(), 0, by0.data(), nullptr);
+        if (s != BVP_OK) return s;
+        std::vector<BvpInstState> st1 = h->st;
+        std::vector<int64_t> off1 = h->offsets;
+        std::vector<double> mesh1(static_cast<const double*>(h->h_mesh.p), static_cast<const double*>(h->h_mesh.p) + off1[nb]);
+        std::vector<double> y1(static_cast<const double*>(h->h_y.p), static_cast<const double*>(h->h_y.p) + off1[nb] * M);
+        std::vector<int> slot(n, -1);
+        for (int k = 0; k < nb; ++k) slot[bad[k]] = k;
+        h->st.resize(n);
+        h->offsets.assign(n + 1, 0);
+        for (int q = 0; q < n; ++q) {
+            h->st[q] = slot[q] >= 0 ? st1[slot[q]] : st0[q];
+            h->offsets[q + 1] = h->offsets[q] + h->st[q].N;
+        }
+        const long long totm = h->offsets[n];
+        if (!ensure_host(h->h_mesh, size_t(totm) * 8) || !ensure_host(h->h_y, size_t(totm) * M * 8))
+            return fail(h, BVP_ERR_NOMEM, "pinned allocation failed");
+        double* hm = static_cast<double*>(h->h_mesh.p);
+        double* hy = static_cast<double*>(h->h_y.p);
+        for (int q = 0; q < n; ++q) {
+            const int k = slot[q];
+            const double* sm = k >= 0 ? &mesh1[off1[k]] : &mesh0[off0[q]];
+            const double* sy = k >= 0 ? &y1[off1[k] * M] : &y00[off0[q] * M];
+            std::memcpy(hm + h->offsets[q], sm, size_t(h->st[q].N) * 8);
+            std::memcpy(hy + h->offsets[q] * M, sy, size_t(h->st[q].N) * M * 8);
+        }
+        h->last_n = n;
+        h->stages_ok = false;  // the stages on the device belong to the fallback subset only
+    }
+    if (out) {
+        for (int q = 0; q < n; ++q) {
+            const BvpInstState& st = h->st[q];
+            if (out->retcode) out->retcode[q] = st.retcode;
+            if (out->n_nodes) out->n_nodes[q] = st.N;
+            if (out->newton_iters) out->newton_iters[q] = st.newton_iters;
+            if (out->rounds) out->rounds[q] = st.rounds;
+            if (out->defect) out->defect[q] = st.defect;
+            if (out->resid) out->resid[q] = st.resid;
+        }
+    }
+    return BVP_OK;
+}
+
 bvp_status bvp_solve_batch_device(bvp_handle* h, int32_t n, const double* d_params, const int32_t* d_n_intervals,
                                   const double* d_tspans, int32_t y0_mode, const double* d_y0,
                                   const int64_t* d_y0_off, int32_t max_intervals) {
@@ -563,7 +685,7 @@ bvp_status bvp_fetch_results(bvp_handle* h, bvp_results* out) {
 bvp_status bvp_dense_output(bvp_handle* h, int32_t nq, const double* tq, int32_t deriv, double* out) {
     if (!h) return BVP_ERR_INVALID;
     if (!h->have_results && !h->pending_device) return fail(h, BVP_ERR_STATE, "no solve to interpolate");
-    if (!h->opt.want_stages) return fail(h, BVP_ERR_STATE, "dense output needs want_stages = 1");
+    if (!h->stages_ok) return fail(h, BVP_ERR_STATE, "dense output needs want_stages = 1 and a solve without fallback");
     if (nq < 1 || !tq || !out) return fail(h, BVP_ERR_INVALID, "invalid arguments");
     const int n = h->last_n, M = h->L.M;
     DevBuf dt, dout;
@@ -623,8 +745,8 @@ bvp_status bvp_get_packed(bvp_handle* h, const int64_t** offsets, const double**
     if (offsets) *offsets = h->offsets.data();
     if (mesh) *mesh = static_cast<const double*>(h->h_mesh.p);
     if (y) *y = static_cast<const double*>(h->h_y.p);
-    if (K) *K = h->opt.want_stages ? static_cast<const double*>(h->h_K.p) : nullptr;
-    if (KI) *KI = h->opt.want_stages ? static_cast<const double*>(h->h_KI.p) : nullptr;
+    if (K) *K = h->stages_ok ? static_cast<const double*>(h->h_K.p) : nullptr;
+    if (KI) *KI = h->stages_ok ? static_cast<const double*>(h->h_KI.p) : nullptr;
     return BVP_OK;
 }
 
@@ -710,7 +832,7 @@ void bvp_destroy(bvp_handle* h) {
                       &h->d_delta, &h->d_yj, &h->d_Fj, &h->d_scr, &h->d_iscr, &h->d_st, &h->d_order, &h->d_cap,
                       &h->d_node_off, &h->d_counter, &h->d_params, &h->d_params_j, &h->d_n_init,
                       &h->d_tspans, &h->d_y0, &h->d_y0_off, &h->d_out_off, &h->d_out_mesh,
-                      &h->d_out_y, &h->d_out_K, &h->d_out_KI, &h->d_norm};
+                      &h->d_out_y, &h->d_out_K, &h->d_out_KI, &h->d_norm, &h->d_feat, &h->d_grid};
     for (DevBuf* b : devs)
         if (b->p) cudaFree(b->p);
     HostBuf* hosts[] = {&h->h_in, &h->h_st, &h->h_off, &h->h_mesh, &h->h_y, &h->h_K, &h->h_KI};

@@ -156,6 +156,24 @@ class BatchSolver:
         self._check(st, "bvp_solve_batch")
         return self._collect(r)
 
+    def solve_warm(self, net, features, n_grid, params, n_intervals, tspans, y0_plain):
+        """Surrogate-warm solve through the C ABI (bvp_solve_batch_warm): network guess,
+        resampling, solve and plain-guess fallback on the device. Returns
+        (BatchResult, number of instances that needed the fallback)."""
+        feats = np.ascontiguousarray(features, dtype=np.float32)
+        n_int = np.ascontiguousarray(n_intervals, dtype=np.int32).ravel()
+        n = len(n_int)
+        params = np.ascontiguousarray(params, dtype=np.float64).reshape(n, -1) if self.problem.n_params else None
+        tsp = np.ascontiguousarray(tspans, dtype=np.float64).reshape(n, 2)
+        y0p = np.ascontiguousarray(y0_plain, dtype=np.float64).reshape(n, self.M)
+        r, cr = self._results(n)
+        nfb = np.zeros(1, np.int32)
+        st = self.lib.bvp_solve_batch_warm(self.h, net.h, n, feats.shape[1],
+                                           feats.ctypes.data_as(C.POINTER(C.c_float)), int(n_grid),
+                                           f64(params), i32(n_int), f64(tsp), f64(y0p), C.byref(cr), i32(nfb))
+        self._check(st, "bvp_solve_batch_warm")
+        return self._collect(r), int(nfb[0])
+
     def solve_device(self, d_params, d_n_intervals, d_tspans, d_y0, max_intervals, *, y0_mode=0, d_y0_off=None):
         """Launch a solve on inputs already in device memory (integer device pointers or
         objects with data_ptr()); returns without synchronising."""

@@ -185,6 +185,18 @@ bvp_status bvp_resample_guess_device(int32_t n_inst, int32_t n_grid, int32_t M, 
                                      const int64_t* d_y0_off, double* d_y0, void* stream);
 void bvp_mlp_destroy(bvp_mlp* net);
 
+/* Surrogate-warm batched solve: the network maps each instance's n_features features to a
+ * guess on n_grid uniform points of its tspan (output width n_grid x M), the guess is
+ * resampled onto the instance's initial mesh and the batch is solved from it; instances that
+ * do not converge are solved again from y0_plain (n_inst x M, the constant guess) and
+ * their results replace the warm attempt's. The plain MIRK Newton judges every result.
+ * *n_fallback receives the number of re-solved instances. Results as bvp_solve_batch (the
+ * stages are kept only when no instance needed the fallback). */
+bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n_inst, int32_t n_features,
+                                const float* features, int32_t n_grid, const double* params,
+                                const int32_t* n_intervals, const double* tspans,
+                                const double* y0_plain, bvp_results* out, int32_t* n_fallback);
+
 /* Device time of the last solve's kernels in milliseconds (CUDA events on the handle's
  * stream): [0] whole solve, [1] fused solve kernel. */
 bvp_status bvp_last_timing(bvp_handle* h, double* ms2);
