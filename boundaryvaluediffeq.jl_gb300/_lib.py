@@ -157,7 +157,8 @@ EXPORTS = ("bvp_default_options", "bvp_create", "bvp_solve_batch", "bvp_solve_ba
            "bvp_fetch_results", "bvp_get_solution", "bvp_get_packed", "bvp_eval_stage",
            "bvp_dense_output", "bvp_mlp_create", "bvp_mlp_num_params", "bvp_mlp_set_params",
            "bvp_mlp_get_params", "bvp_mlp_set_normalization", "bvp_mlp_forward", "bvp_mlp_loss_grad",
-           "bvp_mlp_train", "bvp_mlp_forward_device", "bvp_resample_guess_device", "bvp_mlp_destroy",
+           "bvp_mlp_train", "bvp_mlp_forward_device", "bvp_mlp_forward_noalloc", "bvp_resample_guess_device",
+           "bvp_mlp_destroy",
            "bvp_solve_batch_warm",
            "bvp_last_timing", "bvp_stream", "bvp_last_error", "bvp_destroy")
 
@@ -208,6 +209,8 @@ def load_library(path: str | None = None):
     lib.bvp_mlp_train.restype = C.c_int
     lib.bvp_mlp_forward_device.argtypes = [vp, i32, vp, vp, vp]
     lib.bvp_mlp_forward_device.restype = C.c_int
+    lib.bvp_mlp_forward_noalloc.argtypes = [vp, i32, vp, vp, vp]
+    lib.bvp_mlp_forward_noalloc.restype = C.c_int
     lib.bvp_resample_guess_device.argtypes = [i32, i32, i32, vp, vp, vp, vp, vp, vp]
     lib.bvp_resample_guess_device.restype = C.c_int
     lib.bvp_mlp_destroy.argtypes = [vp]

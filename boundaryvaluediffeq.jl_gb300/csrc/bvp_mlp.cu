@@ -8,9 +8,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <random>
 #include <string>
 #include <vector>
@@ -483,3 +485,56 @@ void bvp_mlp_destroy(bvp_mlp* n) {
 }
 
 }  // extern "C"
+
+// ---- forward without allocation ------------------------------------------------------------
+// bvp_mlp_forward_noalloc runs the forward's kernels on scratch carved from this static
+// device array instead of the network's cudaMalloc'd activation buffers: two BF16 activation
+// buffers used in turn (layer input / layer output) and one FP32 pre-activation buffer.
+static __device__ __align__(256) unsigned char bvp_mlp_static_scratch[BVP_MLP_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kNoAllocDevices = 64;
+std::atomic<void*> g_noalloc_scratch[kNoAllocDevices];  // device address of the array, per device
+std::mutex g_noalloc_mu;
+
+size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+}  // namespace
+
+extern "C" bvp_status bvp_mlp_forward_noalloc(bvp_mlp* n, int32_t B, const float* d_x, float* d_y, void* stream) {
+    if (!n || B < 1 || !d_x || !d_y) return BVP_ERR_INVALID;
+    int wmax = 0;
+    for (int v : n->w) wmax = std::max(wmax, v);
+    const size_t hb = round256(size_t(B) * wmax * sizeof(bf16)), zb = round256(size_t(B) * wmax * sizeof(float));
+    if (2 * hb + zb > size_t(BVP_MLP_NOALLOC_SCRATCH_BYTES)) return BVP_ERR_TOO_LARGE;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return BVP_ERR_CUDA;
+    if (dev < 0 || dev >= kNoAllocDevices) return BVP_ERR_INVALID;
+    void* base = g_noalloc_scratch[dev].load(std::memory_order_acquire);
+    if (!base) {
+        // first call on this device: the lookup loads the module that holds the array
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        base = g_noalloc_scratch[dev].load(std::memory_order_relaxed);
+        if (!base) {
+            if (cudaGetSymbolAddress(&base, bvp_mlp_static_scratch) != cudaSuccess || !base) return BVP_ERR_CUDA;
+            g_noalloc_scratch[dev].store(base, std::memory_order_release);
+        }
+    }
+    char* scr = static_cast<char*>(base);
+    bf16* hin = reinterpret_cast<bf16*>(scr);
+    bf16* hout = reinterpret_cast<bf16*>(scr + hb);
+    float* Z = reinterpret_cast<float*>(scr + 2 * hb);
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int L = n->L;
+    const float* nrm = n->d_norm;
+    const long long w0 = n->w[0], wL = n->w[L];
+    k_input<<<grid1d(B * w0), 256, 0, s>>>(B, int(w0), d_x, nrm, nrm + w0, hin);
+    for (int l = 0; l < L; ++l) {
+        const int ni = n->w[l], no = n->w[l + 1];
+        gemm(s, false, false, B, no, ni, hin, ni, n->d_pb + n->offW[l], no, Z, no);
+        const bool last = l == L - 1;
+        k_bias_act<<<grid1d((long long)B * no), 256, 0, s>>>(B, no, Z, n->d_p + n->offb[l], last ? nullptr : hout,
+                                                              last ? d_y : nullptr, nrm + 2 * w0, nrm + 2 * w0 + wL);
+        std::swap(hin, hout);
+    }
+    return cudaGetLastError() == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
+}

@@ -15,7 +15,7 @@ import numpy as np
 from . import _lib
 from ._lib import f64, i32
 
-STATUS = {0: "OK", 1: "INVALID", 2: "COMPILE", 3: "CUDA", 4: "NOMEM", 5: "STATE"}
+STATUS = {0: "OK", 1: "INVALID", 2: "COMPILE", 3: "CUDA", 4: "NOMEM", 5: "STATE", 6: "TOO_LARGE"}
 RET_SUCCESS, RET_FAILURE, RET_MAXITERS = 0, 1, 2
 S_OF = {2: 1, 3: 2, 4: 3, 5: 4, 6: 5}
 NSX_OF = {2: 2, 3: 1, 4: 1, 5: 2, 6: 4}

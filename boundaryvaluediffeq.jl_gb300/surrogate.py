@@ -112,6 +112,17 @@ class MLP:
                                              C.c_void_p(stream) if stream else None)
         self._check(st, "bvp_mlp_forward_device")
 
+    def forward_noalloc(self, d_x, d_y, batch, stream=None):
+        """forward_device on the library's static scratch (bvp_mlp_forward_noalloc): no
+        device allocation; batch x widest layer is bounded by BVP_MLP_NOALLOC_SCRATCH_BYTES."""
+        def ptr(v):
+            return C.c_void_p(v.data_ptr() if hasattr(v, "data_ptr") else int(v))
+        st = self.lib.bvp_mlp_forward_noalloc(self.h, batch, ptr(d_x), ptr(d_y), C.c_void_p(stream) if stream else None)
+        if st == 6:
+            raise BVPError(f"bvp_mlp_forward_noalloc: batch {batch} x widest layer {max(self.widths)} does not fit "
+                           "the static scratch")
+        self._check(st, "bvp_mlp_forward_noalloc")
+
 
 def resample_host(grid, n_intervals):
     """Linear resampling of uniform-grid guesses (n x G x M) onto uniform meshes with
