@@ -225,12 +225,15 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--jac-precision", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--instances", type=int, default=N_INST,
+                    help="batch size (4096 is the benchmark; smaller batches only for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     args.warmup = max(args.warmup, 3)
 
     ws, rank = _dist()
+    n_inst = args.instances
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
@@ -254,7 +257,7 @@ def main():
     net = sur.net
 
     # every rank solves its own 4096-instance batch (instances are independent: weak scaling)
-    params, nint, tsp, y0 = P.pendulum_family(N_INST, seed=SEED + rank)
+    params, nint, tsp, y0 = P.pendulum_family(n_inst, seed=SEED + rank)
     feats = params.astype(np.float32)
     sv = pkg.BatchSolver(P.PENDULUM, order=4, abstol=1e-6, jac_precision=args.jac_precision)
     lib = sv.lib
@@ -263,7 +266,7 @@ def main():
     dts = torch.tensor(tsp, device="cuda")
     dy = torch.tensor(y0, device="cuda")
     dfeat = torch.tensor(feats, device="cuda")
-    dgrid = torch.empty(N_INST * GRID * M, dtype=torch.float32, device="cuda")
+    dgrid = torch.empty(n_inst * GRID * M, dtype=torch.float32, device="cuda")
     y0_off = np.concatenate([[0], np.cumsum(nint.astype(np.int64) + 1)]).astype(np.int64)
     dy0_off = torch.tensor(y0_off, device="cuda")
     dyw = torch.empty(int(y0_off[-1]) * M, dtype=torch.float64, device="cuda")
@@ -285,8 +288,8 @@ def main():
         sv.solve_device(dp, dn, dts, dy, nmax)
 
     def warm_kernels():
-        net.forward_device(dfeat, dgrid, N_INST, sptr)
-        st = lib.bvp_resample_guess_device(N_INST, GRID, M, _ptr(dgrid), _ptr(dts), _ptr(dn), _ptr(dy0_off),
+        net.forward_device(dfeat, dgrid, n_inst, sptr)
+        st = lib.bvp_resample_guess_device(n_inst, GRID, M, _ptr(dgrid), _ptr(dts), _ptr(dn), _ptr(dy0_off),
                                            _ptr(dyw), C_void(sptr))
         assert st == 0
         sv.solve_device(dp, dn, dts, dyw, nmax, y0_mode=1, d_y0_off=dy0_off)
@@ -332,16 +335,18 @@ def main():
 
     sampler = ClockSampler(local)
     with sampler:
+        torch.cuda.profiler.start()     # a profiler started with --profile-from-start off sees only this
         warm_s, warm_fused = run_device(warm_step)
         plain_s, plain_fused = run_device(lambda: timed(plain_kernels))
+        torch.cuda.profiler.stop()
     clocks = sampler.summary()
-    value = N_INST * ws * args.steps / warm_s
-    value_plain = N_INST * ws * args.steps / plain_s
+    value = n_inst * ws * args.steps / warm_s
+    value_plain = n_inst * ws * args.steps / plain_s
 
     # e2e through the C ABI with host buffers (copies in and results out inside the region)
     import ctypes as C
     from bvdiffeq_gb300._lib import f64, i32, Results
-    n = N_INST
+    n = n_inst
     out = {k: np.zeros(n, np.int32) for k in ("retcode", "n_nodes", "newton_iters", "rounds")}
     outd = {k: np.zeros(n) for k in ("defect", "resid")}
     cr = Results(i32(out["retcode"]), i32(out["n_nodes"]), i32(out["newton_iters"]), i32(out["rounds"]),
@@ -370,7 +375,7 @@ def main():
             st = call()
             ts.append(time.perf_counter() - t0)
             assert st == 0, lib.bvp_last_error(sv.h)
-        return N_INST * ws * args.steps / _max_over_ranks(sum(ts), ws)
+        return n_inst * ws * args.steps / _max_over_ranks(sum(ts), ws)
 
     e2e_plain_v = run_e2e(e2e_plain)
     plain_nodes = int(out["n_nodes"].sum())
@@ -401,7 +406,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": warm_s * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 residual/defect, f32 Jacobian/factorisation"
         if args.jac_precision == 32 else "f64", "data": "synthetic (seeded pendulum family)",
-        "config": {"workload": WORKLOAD, "instances": N_INST, "seed": SEED, "method": "MIRK4",
+        "config": {"workload": WORKLOAD, "instances": n_inst, "seed": SEED, "method": "MIRK4",
                    "form": "surrogate-warm (BF16 MLP guess, plain-guess fallback)",
                    "jac_precision": args.jac_precision,
                    "l2": "flushed between timed steps (256 MB write)",

@@ -158,9 +158,9 @@ constexpr bool NODE_SHARE = S >= 2 && ORD >= 4;
 // and stage 1 is evaluated at the right node with t = t_{i+1} and written back to node[].
 // With `dy` non-null the residual uses the FP64 difference y_{i+1} - y_i instead of the
 // one formed from yi, yi1 (the FP32 residual keeps its roundoff near h|K| eps32).
-template <class T, class PT>
-BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, double ti, double hi_d,
-                          T* node = nullptr, double ti1 = 0.0, const double* dy = nullptr) {
+template <class T, class PT, class TT>
+BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, TT ti, TT hi_d,
+                          T* node = nullptr, TT ti1 = TT(0), const double* dy = nullptr) {
     const PT hi = PT(hi_d);
     T Y[M];
 #pragma unroll
@@ -185,7 +185,7 @@ BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, 
                 for (int m = 0; m < M; ++m) Y[m] = Y[m] + hi * (Ki[j * M + m] * PT(tab_x(r, j)));
             }
         }
-        bvp_f<T, PT>(&Ki[r * M], Y, p, PT(ti + tab_c(r) * hi_d));
+        bvp_f<T, PT>(&Ki[r * M], Y, p, PT(ti + TT(tab_c(r)) * hi_d));
     }
 #pragma unroll
     for (int m = 0; m < M; ++m) {
@@ -295,6 +295,17 @@ BVP_DEV void mesh_setup(const Args& a, const Inst& I) {
         }
         I.iscr[ISCR_LOFF + ns] = o;
     }
+    {
+        // the mesh in the Jacobian precision (FP32 stage times without FP64 conversions)
+        const double* mesh = mesh_of(a, I, I.cur);
+        const double* h = h_of(a, I, I.cur);
+        JT* tj = a.tj + I.nb;
+        JT* hj = a.hj + I.nb;
+        for (int i = lane_id(); i < I.N; i += 32) {
+            tj[i] = JT(mesh[i]);
+            if (i < I.N - 1) hj[i] = JT(h[i]);
+        }
+    }
     __syncwarp();
 }
 
@@ -322,7 +333,7 @@ BVP_DEV double residual(const Args& a, const Inst& I) {
         R y0v[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) y0v[m] = y_at<R>(a, I, i0 * M + m);
-        bvp_f<R, R>(node, y0v, pr, R(mesh[i0]));
+        bvp_f<R, R>(node, y0v, pr, sizeof(R) == 8 ? R(mesh[i0]) : R(a.tj[I.nb + i0]));
     }
     const double* y64 = y_of(a, I, I.cur);
     // interior BC points: the lane whose block holds the interval evaluates the
@@ -335,12 +346,15 @@ BVP_DEV double residual(const Args& a, const Inst& I) {
 #pragma unroll
         for (int m = 0; m < M; ++m) { yi[m] = y_at<R>(a, I, i * M + m); yi1[m] = y_at<R>(a, I, (i + 1) * M + m); }
         if constexpr (sizeof(R) == 8) {
-            phi_interval<R, R>(yi, yi1, Ki, ri, pr, mesh[i], h[i], NODE_SHARE ? node : nullptr, mesh[i + 1]);
+            phi_interval<R, R, double>(yi, yi1, Ki, ri, pr, mesh[i], h[i], NODE_SHARE ? node : nullptr, mesh[i + 1]);
         } else {
             double dy[M];
 #pragma unroll
             for (int m = 0; m < M; ++m) dy[m] = y64[(i + 1) * M + m] - y64[i * M + m];
-            phi_interval<R, R>(yi, yi1, Ki, ri, pr, mesh[i], h[i], NODE_SHARE ? node : nullptr, mesh[i + 1], dy);
+            const JT* tj = a.tj + I.nb;
+            const JT* hj = a.hj + I.nb;
+            phi_interval<R, R, R>(yi, yi1, Ki, ri, pr, R(tj[i]), R(hj[i]), NODE_SHARE ? node : nullptr, R(tj[i + 1]),
+                                  dy);
         }
 #pragma unroll
         for (int k = 0; k < NBCP; ++k) {
@@ -439,27 +453,26 @@ BVP_DEV double residual_sq(const Args& a, const Inst& I) {
 // ---- K2: Jacobian blocks (warp) ------------------------------------------------------------
 // S_i = ∂r_i/∂y_i and R_i = ∂r_i/∂y_{i+1} by forward mode with 2M tangents in JT, from the
 // JT copy of the iterate. BC rows use u at the BC points cached by the last residual.
-// BC Jacobian blocks: one (node, L x M) block per BC contribution, accumulated on lane 0 in
-// registers and written once; the separator solve adds blocks that share a node.
-struct BcBlocks {
-    int n;
-    int node[NBCB];
-    double G[NBCB][M * M];
-    BVP_DEV void add(int nd, const double* g) {
-        node[n] = nd;
+// BC Jacobian blocks: one (node, L x M) block per slot of the scratch; lane k evaluates the
+// BCs' derivative with respect to u at BC point k (two-point: lane 0 bca, lane 1 bcb). With
+// the exact BC Jacobian an interior point gives two blocks (its interval's nodes), so each
+// point owns two slots, the second one zero for an endpoint. The separator solve adds the
+// blocks that share a node.
+BVP_DEV void write_bc_block(const Inst& I, int slot, int node, const double* G) {
+    I.iscr[ISCR_BNODE + slot] = node;
+    double* dst = I.scr + SCR_BCBLK + slot * M * M;
 #pragma unroll
-        for (int q = 0; q < M * M; ++q) G[n][q] = g[q];
-        ++n;
-    }
-};
+    for (int q = 0; q < M * M; ++q) dst[q] = G[q];
+}
 
 BVP_DEV void jacobian(const Args& a, const Inst& I) {
     using DI = Dual<JT, D>;
-    using DU = Dual<JT, M>;
     const int lane = lane_id();
     const double* mesh = mesh_of(a, I, I.cur);
     const double* h = h_of(a, I, I.cur);
     const JT* yj = yj_of(a, I);
+    const JT* tj = a.tj + I.nb;
+    const JT* hj = a.hj + I.nb;
     for (int i = lane; i < I.N - 1; i += 32) {
         DI yi[M], yi1[M], Ki[S * M], ri[M];
 #pragma unroll
@@ -467,7 +480,7 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
             yi[m] = DI(yj[i * M + m]); yi[m].d[m] = JT(1);
             yi1[m] = DI(yj[(i + 1) * M + m]); yi1[m].d[M + m] = JT(1);
         }
-        phi_interval<DI, JT>(yi, yi1, Ki, ri, I.pj, mesh[i], h[i]);
+        phi_interval<DI, JT, JT>(yi, yi1, Ki, ri, I.pj, tj[i], hj[i]);
         JT* Sg = a.Sb + (I.nb + i) * (M * M);
         JT* Rg = a.Rb + (I.nb + i) * (M * M);
 #pragma unroll
@@ -478,76 +491,88 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
                 Rg[r * M + c] = ri[r].d[M + c];
             }
     }
-    if (lane == 0) {
-        BcBlocks bb;
-        bb.n = 0;
-        double G[M * M];
-        const double* ua_c = I.scr + SCR_UA;
-        if (TWOPOINT) {
+    using DU = Dual<JT, M>;
+    const double* ua_c = I.scr + SCR_UA;
+    double G[M * M];
+    if (TWOPOINT) {
+        if (lane < 2) {
             DU ua[M], ra[M];
-            for (int m = 0; m < M; ++m) { ua[m] = DU(JT(ua_c[m])); ua[m].d[m] = JT(1); }
-            bvp_bca<DU, JT>(ra, ua, I.pj);
-            for (int q = 0; q < M * M; ++q) G[q] = 0.0;
-            for (int r = 0; r < LA; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(ra[r].d[c]);
-            bb.add(0, G);
-            for (int m = 0; m < M; ++m) { ua[m] = DU(JT(ua_c[M + m])); ua[m].d[m] = JT(1); }
-            bvp_bcb<DU, JT>(ra, ua, I.pj);
-            for (int q = 0; q < M * M; ++q) G[q] = 0.0;
-            for (int r = LA; r < M; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(ra[r - LA].d[c]);
-            bb.add(I.N - 1, G);
-        } else {
-            for (int k = 0; k < NBC; ++k) {
-                DU ua[NBC * M];
-                const DU* ptrs[NBC];
-                for (int qq = 0; qq < NBC; ++qq) {
-                    for (int m = 0; m < M; ++m) {
-                        ua[qq * M + m] = DU(JT(ua_c[qq * M + m]));
-                        if (qq == k) ua[qq * M + m].d[m] = JT(1);
-                    }
-                    ptrs[qq] = &ua[qq * M];
-                }
-                DU res[M];
-                bvp_bc<DU, JT>(res, ptrs, I.pj);
-                for (int r = 0; r < M; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(res[r].d[c]);
-                const int node = I.iscr[ISCR_UNODE + k];
-                if (!I.iscr[ISCR_UIN + k] || !a.bc_jac_exact) {
-                    // the interpolant's stages are held at their primal values: du(t)/dy = I
-                    // on the interval's left node (interpolation.jl:214-242, mirk.jl:565-572)
-                    bb.add(node, G);
-                } else {
-                    // exact: chain through the interval's stages and extra stages
-                    const int ii = node;
-                    JT w[SS];
 #pragma unroll
-                    for (int s2 = 0; s2 < SS; ++s2) w[s2] = JT(I.scr[SCR_BCW + k * SS + s2]);
-                    DI yi[M], yi1[M], Ki[S * M], KIi[NSXA * M], ri[M], z[M];
-                    for (int m = 0; m < M; ++m) {
-                        yi[m] = DI(yj[ii * M + m]); yi[m].d[m] = JT(1);
-                        yi1[m] = DI(yj[(ii + 1) * M + m]); yi1[m].d[M + m] = JT(1);
-                    }
-                    phi_interval<DI, JT>(yi, yi1, Ki, ri, I.pj, mesh[ii], h[ii]);
-                    interp_stages<DI, JT>(yi, yi1, Ki, KIi, I.pj, mesh[ii], h[ii]);
-                    sum_stages<DI, JT>(w, yi, Ki, KIi, JT(h[ii]), z);
-                    double JL[M * M], JR[M * M];
-                    for (int r = 0; r < M; ++r)
-                        for (int c = 0; c < M; ++c) {
-                            double sl = 0.0, sr = 0.0;
-                            for (int qq = 0; qq < M; ++qq) {
-                                sl += G[r * M + qq] * double(z[qq].d[c]);
-                                sr += G[r * M + qq] * double(z[qq].d[M + c]);
-                            }
-                            JL[r * M + c] = sl; JR[r * M + c] = sr;
-                        }
-                    bb.add(ii, JL);
-                    bb.add(ii + 1, JR);
+            for (int m = 0; m < M; ++m) { ua[m] = DU(JT(ua_c[lane * M + m])); ua[m].d[m] = JT(1); }
+#pragma unroll
+            for (int q = 0; q < M * M; ++q) G[q] = 0.0;
+            if (lane == 0) {
+                bvp_bca<DU, JT>(ra, ua, I.pj);
+                for (int r = 0; r < LA; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(ra[r].d[c]);
+            } else {
+                bvp_bcb<DU, JT>(ra, ua, I.pj);
+                for (int r = LA; r < M; ++r) for (int c = 0; c < M; ++c) G[r * M + c] = double(ra[r - LA].d[c]);
+            }
+            write_bc_block(I, lane, lane == 0 ? 0 : I.N - 1, G);
+        }
+        if (lane == 0) I.iscr[ISCR_NB] = 2;
+    } else {
+        const int k = lane;
+        if (k < NBC) {
+            DU ua[NBC * M];
+            const DU* ptrs[NBC];
+#pragma unroll
+            for (int qq = 0; qq < NBC; ++qq) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    ua[qq * M + m] = DU(JT(ua_c[qq * M + m]));
+                    if (qq == k) ua[qq * M + m].d[m] = JT(1);
                 }
+                ptrs[qq] = &ua[qq * M];
+            }
+            DU res[M];
+            bvp_bc<DU, JT>(res, ptrs, I.pj);
+#pragma unroll
+            for (int r = 0; r < M; ++r)
+#pragma unroll
+                for (int c = 0; c < M; ++c) G[r * M + c] = double(res[r].d[c]);
+            const int node = I.iscr[ISCR_UNODE + k];
+            const int slot = a.bc_jac_exact ? 2 * k : k;
+            if (!I.iscr[ISCR_UIN + k] || !a.bc_jac_exact) {
+                // the interpolant's stages are held at their primal values: du(t)/dy = I
+                // on the interval's left node (interpolation.jl:214-242, mirk.jl:565-572)
+                write_bc_block(I, slot, node, G);
+                if (a.bc_jac_exact) {
+                    double Z[M * M];
+#pragma unroll
+                    for (int q = 0; q < M * M; ++q) Z[q] = 0.0;
+                    write_bc_block(I, slot + 1, node, Z);
+                }
+            } else {
+                // exact: chain through the interval's stages and extra stages
+                const int ii = node;
+                JT w[SS];
+#pragma unroll
+                for (int s2 = 0; s2 < SS; ++s2) w[s2] = JT(I.scr[SCR_BCW + k * SS + s2]);
+                DI yi[M], yi1[M], Ki[S * M], KIi[NSXA * M], ri[M], z[M];
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    yi[m] = DI(yj[ii * M + m]); yi[m].d[m] = JT(1);
+                    yi1[m] = DI(yj[(ii + 1) * M + m]); yi1[m].d[M + m] = JT(1);
+                }
+                phi_interval<DI, JT, double>(yi, yi1, Ki, ri, I.pj, mesh[ii], h[ii]);
+                interp_stages<DI, JT>(yi, yi1, Ki, KIi, I.pj, mesh[ii], h[ii]);
+                sum_stages<DI, JT>(w, yi, Ki, KIi, JT(h[ii]), z);
+                double JL[M * M], JR[M * M];
+                for (int r = 0; r < M; ++r)
+                    for (int c = 0; c < M; ++c) {
+                        double sl = 0.0, sr = 0.0;
+                        for (int qq = 0; qq < M; ++qq) {
+                            sl += G[r * M + qq] * double(z[qq].d[c]);
+                            sr += G[r * M + qq] * double(z[qq].d[M + c]);
+                        }
+                        JL[r * M + c] = sl; JR[r * M + c] = sr;
+                    }
+                write_bc_block(I, slot, ii, JL);
+                write_bc_block(I, slot + 1, ii + 1, JR);
             }
         }
-        I.iscr[ISCR_NB] = bb.n;
-        for (int k = 0; k < bb.n; ++k) {
-            I.iscr[ISCR_BNODE + k] = bb.node[k];
-            for (int q = 0; q < M * M; ++q) I.scr[SCR_BCBLK + k * M * M + q] = bb.G[k][q];
-        }
+        if (lane == 0) I.iscr[ISCR_NB] = a.bc_jac_exact ? 2 * NBC : NBC;
     }
     __syncwarp();
 }
@@ -701,6 +726,85 @@ BVP_DEV bool dense_solve(int n, R* A, R* b) {
     return true;
 }
 
+// The separator system on the whole warp: lane r holds row r (n = nk M rows, at most
+// NDENSE <= 16) and its right-hand side in registers. Gaussian elimination with partial
+// pivoting: the pivot row (largest |a_rk|, the first on ties, as dense_solve picks it) is
+// found by a warp reduction and exchanged with row k by shuffles; then back substitution by
+// broadcasts. Writes δ at the separator nodes.
+constexpr bool WARP_DENSE = NDENSE <= 16;
+BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
+    const int lane = lane_id();
+    const int n = nk * M;
+    const int row0 = (nk - 1) * M;
+    JT row[NDENSE];
+    JT rhs = JT(0);
+#pragma unroll
+    for (int c = 0; c < NDENSE; ++c) row[c] = JT(0);
+    if (lane < row0) {
+        // segment relation j: A δ_{kept j} + B δ_{kept j+1} = g
+        const int j = lane / M, r = lane - j * M;
+        const JT* seg = seg_of(I, j);
+#pragma unroll
+        for (int c = 0; c < NDENSE; ++c) {
+            const int cj = c - j * M;
+            if (cj >= 0 && cj < M) row[c] = seg[r * M + cj];
+            else if (cj >= M && cj < 2 * M) row[c] = seg[M * M + r * M + cj - M];
+        }
+        rhs = seg[2 * M * M + r];
+    } else if (lane < n) {
+        // BC row r: the blocks of every BC contribution, added at their separator columns
+        const int r = lane - row0;
+        const int nb = I.iscr[ISCR_NB];
+        for (int k = 0; k < nb; ++k) {
+            const int node = I.iscr[ISCR_BNODE + k];
+            int kj = 0;
+            while (kj < nk - 1 && I.iscr[ISCR_KEPT + kj] != node) ++kj;
+            const double* G = I.scr + SCR_BCBLK + k * M * M + r * M;
+#pragma unroll
+            for (int c = 0; c < NDENSE; ++c) {
+                const int cj = c - kj * M;
+                if (cj >= 0 && cj < M) row[c] += JT(G[cj]);
+            }
+        }
+        rhs = JT(-I.scr[SCR_BCRES + r]);
+    }
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < NDENSE; ++k) {
+        if (k < n) {
+            JT v = (lane >= k && lane < n) ? fabs(row[k]) : JT(-1);
+            int pr = lane;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const JT v2 = __shfl_xor_sync(FULL, v, o);
+                const int p2 = __shfl_xor_sync(FULL, pr, o);
+                if (v2 > v || (v2 == v && p2 < pr)) { v = v2; pr = p2; }
+            }
+            ok = ok && v > JT(0) && isfinite(v);
+            const int src = lane == k ? pr : (lane == pr ? k : lane);
+#pragma unroll
+            for (int c = 0; c < NDENSE; ++c) row[c] = __shfl_sync(FULL, row[c], src);
+            rhs = __shfl_sync(FULL, rhs, src);
+            const JT inv = JT(1) / __shfl_sync(FULL, row[k], k);
+            const JT mlt = (lane > k && lane < n) ? row[k] * inv : JT(0);
+#pragma unroll
+            for (int c = k + 1; c < NDENSE; ++c) row[c] -= mlt * __shfl_sync(FULL, row[c], k);
+            rhs -= mlt * __shfl_sync(FULL, rhs, k);
+        }
+    }
+    JT x = JT(0);
+#pragma unroll
+    for (int k = NDENSE - 1; k >= 0; --k) {
+        if (k < n) {
+            const JT xk = __shfl_sync(FULL, rhs / row[k], k);
+            if (lane == k) x = xk;
+            if (lane < k) rhs -= row[k] * xk;
+        }
+    }
+    if (ok && lane < n) a.delta[(I.nb + I.iscr[ISCR_KEPT + lane / M]) * M + lane % M] = x;
+    return ok;
+}
+
 // Newton direction δ (in a.delta) for J δ = -F. Returns false if singular.
 BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     const int lane = lane_id();
@@ -753,7 +857,9 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     __syncwarp();
     // 3. separator system
     int dense_ok = 1;
-    if (lane == 0) {
+    if constexpr (WARP_DENSE) {
+        dense_ok = separator_solve_warp(a, I, nk) ? 1 : 0;
+    } else if (lane == 0) {
         // in thread-local storage (L1-resident), not the global scratch: the elimination
         // reads back what it just wrote
         const int n = nk * M;
@@ -873,26 +979,68 @@ BVP_DEV bool newton_attempt(const Args& a, Inst& I, bool linesearch, int& iters,
     double* y = y_of(a, I, I.cur);
     JT* yj = yj_of(a, I);
     double* yb = a.ybase + I.nb * M;
+    const JT* dl = a.delta + I.nb * M;
     const int nM = I.N * M;
     iters = 0;
     refresh_yj(a, I);
     bool f32 = F32_PHASE_OK && a.fp32_phase && !linesearch;
     const double switch_tol = 100.0 * a.abstol;
-    double nrm;
-    if constexpr (F32_PHASE_OK) nrm = f32 ? residual<float>(a, I) : residual<double>(a, I);
-    else nrm = residual<double>(a, I);
-    if (f32 && !(nrm > switch_tol)) { f32 = false; nrm = residual<double>(a, I); }
-    nrm_out = nrm;
-    if (!isfinite(nrm)) return false;
-    if (nrm <= a.abstol) return true;
-    double nrm0 = nrm;
-    double best = nrm;
-    int stall = 0;
-    for (int it = 0; it < a.max_newton; ++it) {
+    // One residual evaluation per pass of this loop (a single inlined copy of each residual
+    // kernel); `why` says what the evaluation is for.
+    enum { R_START, R_SWITCH, R_STEP, R_TRIAL };
+    int why = R_START;
+    double nrm0 = 0.0, best = 0.0, f0 = 0.0, alpha = 1.0;
+    int stall = 0, ls = 0;
+#pragma unroll 1
+    while (true) {
+        double nrm;
+        if constexpr (F32_PHASE_OK) nrm = f32 ? residual<float>(a, I) : residual<double>(a, I);
+        else nrm = residual<double>(a, I);
+        if (why == R_TRIAL) {
+            // backtracking line search: accept when ||F||^2 decreased enough (Armijo)
+            const double f1 = residual_sq(a, I);
+            if (!(isfinite(nrm) && f1 <= (1.0 - 2e-4 * alpha) * f0)) {
+                alpha *= 0.5;
+                if (++ls >= 20) { nrm_out = nrm; return false; }
+                for (int k = lane; k < nM; k += 32) {
+                    const double v = yb[k] + alpha * double(dl[k]);
+                    y[k] = v;
+                    yj[k] = JT(v);
+                }
+                __syncwarp();
+                continue;
+            }
+            why = R_STEP;
+        }
+        nrm_out = nrm;
+        if (why == R_START) {
+            if (f32 && !(nrm > switch_tol)) { f32 = false; continue; }
+            if (!isfinite(nrm)) return false;
+            if (nrm <= a.abstol) return true;
+            nrm0 = nrm; best = nrm; stall = 0;
+        } else if (why == R_SWITCH) {
+            if (!isfinite(nrm)) return false;
+            if (nrm <= a.abstol) return true;
+            nrm0 = fmax(nrm0, nrm); best = nrm; stall = 0;
+        } else {
+            if (f32 && (!(nrm > switch_tol) || (!(nrm < best) && best < 10.0 * switch_tol))) {
+                // close enough, or the FP32 residual stopped improving near its roundoff floor
+                // (far from it a non-decreasing step is ordinary Newton behaviour): continue on
+                // the FP64 residual, which restarts the stall bookkeeping
+                f32 = false;
+                why = R_SWITCH;
+                continue;
+            }
+            if (!isfinite(nrm)) return false;
+            if (nrm <= a.abstol) return true;
+            if (nrm > a.divergence_factor * nrm0) return false;
+            if (nrm < best) { best = nrm; stall = 0; }
+            else if (++stall >= a.stall_steps) return false;
+        }
+        if (iters >= a.max_newton) return false;
         jacobian(a, I);
         if (!linear_solve(a, I)) return false;
         ++iters;
-        const JT* dl = a.delta + I.nb * M;
         if (!linesearch) {
             for (int k = lane; k < nM; k += 32) {
                 const double v = y[k] + double(dl[k]);
@@ -900,63 +1048,41 @@ BVP_DEV bool newton_attempt(const Args& a, Inst& I, bool linesearch, int& iters,
                 yj[k] = JT(v);
             }
             __syncwarp();
-            if constexpr (F32_PHASE_OK) nrm = f32 ? residual<float>(a, I) : residual<double>(a, I);
-            else nrm = residual<double>(a, I);
+            why = R_STEP;
         } else {
-            const double f0 = residual_sq(a, I);
+            f0 = residual_sq(a, I);
             copy_y(yb, y, nM);
-            double alpha = 1.0;
-            bool ok = false;
-            for (int ls = 0; ls < 20; ++ls) {
-                for (int k = lane; k < nM; k += 32) {
-                    const double v = yb[k] + alpha * double(dl[k]);
-                    y[k] = v;
-                    yj[k] = JT(v);
-                }
-                __syncwarp();
-                nrm = residual<double>(a, I);
-                const double f1 = residual_sq(a, I);
-                if (isfinite(nrm) && f1 <= (1.0 - 2e-4 * alpha) * f0) { ok = true; break; }
-                alpha *= 0.5;
+            alpha = 1.0; ls = 0;
+            for (int k = lane; k < nM; k += 32) {
+                const double v = yb[k] + double(dl[k]);
+                y[k] = v;
+                yj[k] = JT(v);
             }
-            if (!ok) { nrm_out = nrm; return false; }
+            __syncwarp();
+            why = R_TRIAL;
         }
-        nrm_out = nrm;
-        if (f32 && (!(nrm > switch_tol) || (!(nrm < best) && best < 10.0 * switch_tol))) {
-            // close enough, or the FP32 residual stopped improving near its roundoff floor
-            // (far from it a non-decreasing step is ordinary Newton behaviour): continue on
-            // the FP64 residual, which restarts the stall bookkeeping
-            f32 = false;
-            nrm = residual<double>(a, I);
-            nrm_out = nrm;
-            if (!isfinite(nrm)) return false;
-            if (nrm <= a.abstol) return true;
-            nrm0 = fmax(nrm0, nrm);
-            best = nrm; stall = 0;
-            continue;
-        }
-        if (!isfinite(nrm)) return false;
-        if (nrm <= a.abstol) return true;
-        if (nrm > a.divergence_factor * nrm0) return false;
-        if (nrm < best) { best = nrm; stall = 0; }
-        else if (++stall >= a.stall_steps) return false;
     }
-    return false;
 }
 
+// Newton, then Newton with backtracking from the same start when the first fails
+// (default_internal_solve.jl:31-45): one inlined copy of the attempt.
 BVP_DEV bool newton(const Args& a, Inst& I, InstState& s) {
     double* y = y_of(a, I, I.cur);
     const int nM = I.N * M;
     copy_y(a.ybak + I.nb * M, y, nM);
-    int it = 0;
-    double nrm;
-    bool ok = newton_attempt(a, I, false, it, nrm);
-    s.newton_iters += it;
-    if (!ok && a.linesearch) {
-        copy_y(y, a.ybak + I.nb * M, nM);
-        ok = newton_attempt(a, I, true, it, nrm);
+    bool ok = false;
+    double nrm = 0.0;
+#pragma unroll 1
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (attempt == 1) {
+            if (!a.linesearch) break;
+            copy_y(y, a.ybak + I.nb * M, nM);
+            s.flags |= 1;
+        }
+        int it = 0;
+        ok = newton_attempt(a, I, attempt == 1, it, nrm);
         s.newton_iters += it;
-        s.flags |= 1;
+        if (ok) break;
     }
     s.resid = nrm;
     return ok;

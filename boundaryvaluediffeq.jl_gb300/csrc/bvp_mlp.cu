@@ -205,12 +205,15 @@ __global__ void k_resample(int n_inst, int n_grid, int M, const float* grid, con
     const float* gq = grid + (long long)q * n_grid * M;
     double* out = y0 + off[q] * M;
     for (int j = threadIdx.x; j <= n; j += blockDim.x) {
-        const double s = double(j) / double(n) * double(n_grid - 1);
+        const double s = __dmul_rn(double(j) / double(n), double(n_grid - 1));
         int i0 = int(floor(s));
         i0 = i0 < 0 ? 0 : (i0 > n_grid - 2 ? n_grid - 2 : i0);
         const double f = s - i0;
+        // separately rounded products and sum (no FMA contraction): the same values as the
+        // host twin of this resampling
         for (int m = 0; m < M; ++m)
-            out[(long long)j * M + m] = (1.0 - f) * double(gq[i0 * M + m]) + f * double(gq[(i0 + 1) * M + m]);
+            out[(long long)j * M + m] =
+                __dadd_rn(__dmul_rn(1.0 - f, double(gq[i0 * M + m])), __dmul_rn(f, double(gq[(i0 + 1) * M + m])));
     }
 }
 

@@ -60,6 +60,8 @@ struct BvpArgs {
     BVP_JT_PTR* delta;             // [tot][M]
     BVP_JT_PTR* yj;                // [tot][M]  current iterate in the Jacobian precision
     BVP_JT_PTR* Fj;                // [tot][M]  collocation residual in the Jacobian precision
+    BVP_JT_PTR* tj;                // [tot]     mesh of the current round in the Jacobian precision
+    BVP_JT_PTR* hj;                // [tot]     its spacings in the Jacobian precision
     double* scr;                   // per-instance scratch, SCRW doubles each
     int* iscr;                     // per-instance int scratch, ISCRW ints each
     BvpInstState* st;

@@ -56,7 +56,7 @@ struct bvp_handle_s {
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     // device arrays
     DevBuf d_mesh, d_h, d_y, d_ybak, d_ybase, d_K, d_KI, d_F, d_err, d_inc, d_iold, d_Sb, d_Rb,
-        d_rec, d_eq, d_delta, d_yj, d_Fj, d_scr, d_iscr, d_st, d_order, d_cap, d_node_off, d_counter,
+        d_rec, d_tj, d_hj, d_delta, d_yj, d_Fj, d_scr, d_iscr, d_st, d_order, d_cap, d_node_off, d_counter,
         d_params, d_params_j, d_n_init, d_tspans, d_y0, d_y0_off, d_out_off, d_out_mesh,
         d_out_y, d_out_K, d_out_KI, d_norm, d_feat, d_grid;
     // pinned host staging
@@ -301,6 +301,7 @@ static bvp_status ensure_arena(bvp_handle* h, long long tot, int n, long long y0
               ensure_dev(h->d_Rb, T * M * M * js) && ensure_dev(h->d_rec, T * L.RECW * js) &&
               ensure_dev(h->d_delta, T * M * js) &&
               ensure_dev(h->d_yj, T * M * js) && ensure_dev(h->d_Fj, T * M * js) &&
+              ensure_dev(h->d_tj, T * js) && ensure_dev(h->d_hj, T * js) &&
               ensure_dev(h->d_scr, size_t(n) * L.SCRW * 8) && ensure_dev(h->d_iscr, size_t(n) * L.ISCRW * 4) &&
               ensure_dev(h->d_st, size_t(n) * sizeof(BvpInstState)) && ensure_dev(h->d_order, size_t(n) * 4) &&
               ensure_dev(h->d_cap, size_t(n) * 4) && ensure_dev(h->d_node_off, size_t(n) * 8) &&
@@ -364,6 +365,8 @@ static void fill_args(bvp_handle* h, BvpArgs& a, int n, long long tot, int y0_mo
     a.delta = h->d_delta.p;
     a.yj = h->d_yj.p;
     a.Fj = h->d_Fj.p;
+    a.tj = h->d_tj.p;
+    a.hj = h->d_hj.p;
     a.scr = static_cast<double*>(h->d_scr.p);
     a.iscr = static_cast<int*>(h->d_iscr.p);
     a.st = static_cast<BvpInstState*>(h->d_st.p);
@@ -828,7 +831,7 @@ bvp_status bvp_eval_stage(bvp_handle* h, int32_t stage, int32_t n, const double*
 void bvp_destroy(bvp_handle* h) {
     if (!h) return;
     DevBuf* devs[] = {&h->d_mesh, &h->d_h, &h->d_y, &h->d_ybak, &h->d_ybase, &h->d_K, &h->d_KI, &h->d_F,
-                      &h->d_err, &h->d_inc, &h->d_iold, &h->d_Sb, &h->d_Rb, &h->d_rec, &h->d_eq,
+                      &h->d_err, &h->d_inc, &h->d_iold, &h->d_Sb, &h->d_Rb, &h->d_rec, &h->d_tj, &h->d_hj,
                       &h->d_delta, &h->d_yj, &h->d_Fj, &h->d_scr, &h->d_iscr, &h->d_st, &h->d_order, &h->d_cap,
                       &h->d_node_off, &h->d_counter, &h->d_params, &h->d_params_j, &h->d_n_init,
                       &h->d_tspans, &h->d_y0, &h->d_y0_off, &h->d_out_off, &h->d_out_mesh,
