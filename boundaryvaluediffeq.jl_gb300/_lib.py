@@ -154,6 +154,7 @@ class Results(C.Structure):
 
 
 EXPORTS = ("bvp_default_options", "bvp_create", "bvp_solve_batch", "bvp_solve_batch_device",
+           "bvp_solve_batch_device_grid",
            "bvp_fetch_results", "bvp_get_solution", "bvp_get_packed", "bvp_eval_stage",
            "bvp_dense_output", "bvp_mlp_create", "bvp_mlp_num_params", "bvp_mlp_set_params",
            "bvp_mlp_get_params", "bvp_mlp_set_normalization", "bvp_mlp_forward", "bvp_mlp_loss_grad",
@@ -179,6 +180,8 @@ def load_library(path: str | None = None):
     lib.bvp_solve_batch.restype = C.c_int
     lib.bvp_solve_batch_device.argtypes = [vp, i32, vp, vp, vp, i32, vp, vp, i32]
     lib.bvp_solve_batch_device.restype = C.c_int
+    lib.bvp_solve_batch_device_grid.argtypes = [vp, i32, vp, vp, vp, vp, i32, i32]
+    lib.bvp_solve_batch_device_grid.restype = C.c_int
     lib.bvp_fetch_results.argtypes = [vp, C.POINTER(Results)]
     lib.bvp_fetch_results.restype = C.c_int
     lib.bvp_get_solution.argtypes = [vp, i32, f64p, f64p, i32, i32p]

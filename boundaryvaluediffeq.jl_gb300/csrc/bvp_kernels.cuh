@@ -1291,9 +1291,24 @@ BVP_DEV void init_instance(const Args& a, Inst& I) {
     if (a.y0_mode == 0) {
         const double* src = a.y0 + I.q * M;
         for (int k = lane; k < (n + 1) * M; k += 32) y[k] = src[k % M];
-    } else {
+    } else if (a.y0_mode == 1) {
         const double* src = a.y0 + a.y0_off[I.q] * M;
         for (int k = lane; k < (n + 1) * M; k += 32) y[k] = src[k];
+    } else {
+        // guess on a uniform grid of n_grid points over the tspan, resampled linearly onto
+        // the initial mesh (separately rounded products and sum, as the host resampling does)
+        const int G = a.n_grid;
+        const float* gq = a.y0_grid + (long long)I.q * G * M;
+        for (int j = lane; j <= n; j += 32) {
+            const double sg = __dmul_rn(double(j) / double(n), double(G - 1));
+            int i0 = int(floor(sg));
+            i0 = i0 < 0 ? 0 : (i0 > G - 2 ? G - 2 : i0);
+            const double f = sg - i0;
+#pragma unroll
+            for (int m = 0; m < M; ++m)
+                y[j * M + m] = __dadd_rn(__dmul_rn(1.0 - f, double(gq[i0 * M + m])),
+                                         __dmul_rn(f, double(gq[(i0 + 1) * M + m])));
+        }
     }
     __syncwarp();
     I.N = n + 1;

@@ -219,6 +219,123 @@ __global__ void k_resample(int n_inst, int n_grid, int M, const float* grid, con
 
 int grid1d(long long n) { return int(std::min<long long>((n + 255) / 256, 4096)); }
 
+// ---- fused inference: every layer of the network in one kernel --------------------------
+// A CTA takes FR rows of the batch through all layers: the activations stay in shared
+// memory (BF16, two buffers used in turn), each warp computes 8-column tiles of the layer
+// output with mma.m16n8k16 (FP32 accumulation over k16 steps in order, as gemm_bf16 does),
+// reading the weights from a transposed BF16 copy [N][Kp] (k contiguous: the B-fragment
+// pairs are single 32-bit loads, L1/L2-resident across CTAs). The epilogue adds the bias and
+// applies GELU (hidden layers) or the output de-normalisation (last layer), with the same
+// operations as k_bias_act, so the result equals the layer-by-layer forward.
+constexpr int FR = 32;            // rows per CTA
+constexpr int FWMAX = 256;        // widest layer the fused kernel takes
+constexpr int FLD = FWMAX + 8;    // shared row stride (bf16): conflict-free fragment loads
+constexpr int FLMAX = 8;          // layers
+constexpr int FQ = FWMAX / 8 / 4; // 8-column tiles per warp at the widest layer
+
+struct FusedNet {
+    int L;
+    int w[FLMAX + 1];
+    int kp[FLMAX];                // layer input width rounded up to 16
+    long long offWt[FLMAX];       // layer l's [N][kp] block in the transposed weights
+    long long offb[FLMAX];        // bias offsets in the FP32 parameters
+};
+
+__global__ void k_build_wt(int L, FusedNet fn, const long long* offW, const bf16* pb, bf16* wt) {
+    for (int l = 0; l < L; ++l) {
+        const int K = fn.w[l], N = fn.w[l + 1], Kp = fn.kp[l];
+        const bf16* W = pb + offW[l];
+        bf16* T = wt + fn.offWt[l];
+        const long long n = (long long)N * Kp;
+        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+             e += (long long)gridDim.x * blockDim.x) {
+            const int nn = int(e / Kp), k = int(e % Kp);
+            T[e] = k < K ? W[(long long)k * N + nn] : __float2bfloat16(0.f);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_mlp_forward_fused(const FusedNet fn, int B, const float* __restrict__ x,
+                                                           const bf16* __restrict__ wt, const float* __restrict__ p,
+                                                           const float* __restrict__ nrm, float* __restrict__ y) {
+    __shared__ __align__(16) bf16 act[2][FR][FLD];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const int r0 = blockIdx.x * FR;
+    const int w0 = fn.w[0], wL = fn.w[fn.L];
+    {
+        const int kp = fn.kp[0];
+        for (int e = tid; e < FR * kp; e += 128) {
+            const int r = e / kp, c = e % kp;
+            float v = 0.f;
+            if (c < w0 && r0 + r < B) v = (x[(long long)(r0 + r) * w0 + c] - nrm[c]) / nrm[w0 + c];
+            act[0][r][c] = __float2bfloat16(v);
+        }
+    }
+    __syncthreads();
+    int cur = 0;
+    for (int l = 0; l < fn.L; ++l) {
+        const int K = fn.kp[l], N = fn.w[l + 1];
+        const int ntiles = N / 8;
+        const bf16* W = wt + fn.offWt[l];
+        float acc[FQ][2][4];
+#pragma unroll
+        for (int q = 0; q < FQ; ++q)
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[q][i][c] = 0.f;
+        for (int k0 = 0; k0 < K; k0 += 16) {
+            uint32_t af[2][4];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = i * 16 + g;
+                af[i][0] = *reinterpret_cast<const uint32_t*>(&act[cur][r][k0 + 2 * t]);
+                af[i][1] = *reinterpret_cast<const uint32_t*>(&act[cur][r + 8][k0 + 2 * t]);
+                af[i][2] = *reinterpret_cast<const uint32_t*>(&act[cur][r][k0 + 2 * t + 8]);
+                af[i][3] = *reinterpret_cast<const uint32_t*>(&act[cur][r + 8][k0 + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int q = 0; q < FQ; ++q) {
+                const int j = warp + 4 * q;
+                if (j < ntiles) {
+                    const bf16* wr = W + (long long)(j * 8 + g) * K + k0 + 2 * t;
+                    uint32_t bfr[2];
+                    bfr[0] = *reinterpret_cast<const uint32_t*>(wr);
+                    bfr[1] = *reinterpret_cast<const uint32_t*>(wr + 8);
+                    mma_bf16(acc[q][0], af[0], bfr);
+                    mma_bf16(acc[q][1], af[1], bfr);
+                }
+            }
+        }
+        const float* bias = p + fn.offb[l];
+        const bool last = l == fn.L - 1;
+        const float* mu = nrm + 2 * w0;
+        const float* sd = nrm + 2 * w0 + wL;
+#pragma unroll
+        for (int q = 0; q < FQ; ++q) {
+            const int j = warp + 4 * q;
+            if (j >= ntiles) continue;
+            const int c = j * 8 + 2 * t;
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int r = i * 16 + g + 8 * hh;
+#pragma unroll
+                    for (int cc = 0; cc < 2; ++cc) {
+                        const float z = acc[q][i][2 * hh + cc] + bias[c + cc];
+                        if (!last) act[cur ^ 1][r][c + cc] = __float2bfloat16(gelu(z));
+                        else if (r0 + r < B) y[(long long)(r0 + r) * wL + c + cc] = z * sd[c + cc] + mu[c + cc];
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+}
+
 }  // namespace
 
 struct bvp_mlp_s {
@@ -238,6 +355,11 @@ struct bvp_mlp_s {
     cudaStream_t stream = nullptr;
     long long step = 0;
     std::string err;
+    // fused inference (k_mlp_forward_fused) when every width fits it
+    bool fused = false;
+    FusedNet fn{};
+    bf16* d_wt = nullptr;         // transposed BF16 weights, [N][Kp] per layer
+    long long* d_offW = nullptr;
 };
 
 namespace {
@@ -314,6 +436,24 @@ void backward(bvp_mlp* n, int B, const float* d_t) {
     }
 }
 
+// transposed weights for the fused forward, rebuilt whenever the BF16 weights change
+void refresh_wt(bvp_mlp* n) {
+    if (!n->fused) return;
+    k_build_wt<<<256, 256, 0, n->stream>>>(n->L, n->fn, n->d_offW, n->d_pb, n->d_wt);
+}
+
+// inference on device pointers: the fused kernel when the network fits it, else layer by layer
+void infer(bvp_mlp* n, int B, const float* d_x, float* d_y, cudaStream_t s) {
+    if (n->fused) {
+        k_mlp_forward_fused<<<(B + FR - 1) / FR, 128, 0, s>>>(n->fn, B, d_x, n->d_wt, n->d_p, n->d_norm, d_y);
+    } else {
+        cudaStream_t prev = n->stream;
+        n->stream = s;
+        forward(n, B, d_x, d_y);
+        n->stream = prev;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -342,6 +482,23 @@ bvp_status bvp_mlp_create(int32_t n_layers, const int32_t* widths, bvp_mlp** out
          cudaMalloc(&n->d_pb, o * 2) == cudaSuccess && cudaMalloc(&n->d_norm, (2 * w0 + 2 * wL) * 4) == cudaSuccess &&
          cudaMalloc(&n->d_loss, 4) == cudaSuccess;
     if (!ok) { n->err = "allocation failed"; return BVP_ERR_CUDA; }
+    n->fused = n_layers <= FLMAX && n->w[0] <= FWMAX;
+    for (int l = 1; l <= n_layers && n->fused; ++l) n->fused = n->w[l] <= FWMAX && n->w[l] % 8 == 0;
+    if (n->fused) {
+        FusedNet& f = n->fn;
+        f.L = n_layers;
+        long long ot = 0;
+        for (int l = 0; l <= n_layers; ++l) f.w[l] = n->w[l];
+        for (int l = 0; l < n_layers; ++l) {
+            f.kp[l] = (n->w[l] + 15) / 16 * 16;
+            f.offWt[l] = ot;
+            ot += (long long)n->w[l + 1] * f.kp[l];
+            f.offb[l] = n->offb[l];
+        }
+        ok = cudaMalloc(&n->d_wt, ot * 2) == cudaSuccess && cudaMalloc(&n->d_offW, n_layers * 8) == cudaSuccess &&
+             cudaMemcpy(n->d_offW, n->offW.data(), n_layers * 8, cudaMemcpyHostToDevice) == cudaSuccess;
+        if (!ok) { n->err = "allocation failed"; return BVP_ERR_CUDA; }
+    }
     std::vector<float> nrm(2 * w0 + 2 * wL);
     for (long long k = 0; k < w0; ++k) { nrm[k] = 0.f; nrm[w0 + k] = 1.f; }
     for (long long k = 0; k < wL; ++k) { nrm[2 * w0 + k] = 0.f; nrm[2 * w0 + wL + k] = 1.f; }
@@ -360,6 +517,7 @@ bvp_status bvp_mlp_set_params(bvp_mlp* n, const float* params) {
     cudaMemset(n->d_v, 0, n->np * 4);
     n->step = 0;
     k_to_bf16<<<grid1d(n->np), 256, 0, n->stream>>>(n->np, n->d_p, n->d_pb);
+    refresh_wt(n);
     return cudaStreamSynchronize(n->stream) == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
 }
 
@@ -385,13 +543,9 @@ bvp_status bvp_mlp_set_normalization(bvp_mlp* n, const float* in_mu, const float
 
 bvp_status bvp_mlp_forward_device(bvp_mlp* n, int32_t B, const float* d_x, float* d_y, void* stream) {
     if (!n || B < 1 || !d_x || !d_y) return BVP_ERR_INVALID;
-    if (!mlp_reserve(n, B)) return BVP_ERR_NOMEM;
-    cudaStream_t prev = n->stream;
-    if (stream) n->stream = static_cast<cudaStream_t>(stream);
-    forward(n, B, d_x, d_y);
-    const cudaError_t e = cudaGetLastError();
-    n->stream = prev;
-    return e == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
+    if (!n->fused && !mlp_reserve(n, B)) return BVP_ERR_NOMEM;
+    infer(n, B, d_x, d_y, stream ? static_cast<cudaStream_t>(stream) : n->stream);
+    return cudaGetLastError() == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
 }
 
 bvp_status bvp_mlp_forward(bvp_mlp* n, int32_t B, const float* x, float* y) {
@@ -399,7 +553,7 @@ bvp_status bvp_mlp_forward(bvp_mlp* n, int32_t B, const float* x, float* y) {
     if (!mlp_reserve(n, B)) return BVP_ERR_NOMEM;
     const long long w0 = n->w[0], wL = n->w[n->L];
     cudaMemcpyAsync(n->d_x, x, B * w0 * 4, cudaMemcpyHostToDevice, n->stream);
-    forward(n, B, n->d_x, n->d_y);
+    infer(n, B, n->d_x, n->d_y, n->stream);
     cudaMemcpyAsync(y, n->d_y, B * wL * 4, cudaMemcpyDeviceToHost, n->stream);
     return cudaStreamSynchronize(n->stream) == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
 }
@@ -460,6 +614,7 @@ bvp_status bvp_mlp_train(bvp_mlp* n, int32_t N, const float* x, const float* t, 
         if (cudaStreamSynchronize(n->stream) != cudaSuccess) break;
         epoch_loss /= float(std::max(steps, 1));
     }
+    refresh_wt(n);
     const cudaError_t e = cudaStreamSynchronize(n->stream);
     cudaFree(dX); cudaFree(dT); cudaFree(dperm);
     if (last_loss) *last_loss = epoch_loss;
@@ -483,6 +638,7 @@ void bvp_mlp_destroy(bvp_mlp* n) {
     cudaFree(n->d_p); cudaFree(n->d_g); cudaFree(n->d_m); cudaFree(n->d_v); cudaFree(n->d_pb);
     cudaFree(n->d_norm); cudaFree(n->d_dH); cudaFree(n->d_dZ); cudaFree(n->d_dZb); cudaFree(n->d_x);
     cudaFree(n->d_t); cudaFree(n->d_y); cudaFree(n->d_loss); cudaFree(n->d_idx);
+    cudaFree(n->d_wt); cudaFree(n->d_offW);
     if (n->stream) cudaStreamDestroy(n->stream);
     delete n;
 }

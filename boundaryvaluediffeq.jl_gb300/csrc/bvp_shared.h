@@ -39,8 +39,10 @@ struct BvpArgs {
     const BVP_JT_PTR* params_j;    // same, in the Jacobian precision
     const int* n_init;             // initial interval counts
     const double* tspans;          // n_inst x 2
-    const double* y0;              // y0_mode 0: n_inst x M; 1: packed per-node guesses
+    const double* y0;              // y0_mode 0: n_inst x M; 1: packed per-node guesses (2: y0_grid)
     const bvp_i64* y0_off;         // y0_mode 1: per-instance offsets (in M-vectors)
+    const float* y0_grid;          // y0_mode 2: n_inst x n_grid x M guesses on uniform grids
+    int n_grid;
     const bvp_i64* node_off;       // per-instance node offset into the arena
     const int* cap;                // per-instance node capacity
     double* mesh;                  // [2][tot]

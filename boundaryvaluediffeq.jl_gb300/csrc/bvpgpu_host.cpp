@@ -382,9 +382,11 @@ static int fused_grid(bvp_handle* h, int n) {
 // Launches prep + conversion + fused solve on the handle's stream.
 static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode, const double* d_params,
                                const int* d_n_init, const double* d_tspans, const double* d_y0,
-                               const long long* d_y0_off) {
+                               const long long* d_y0_off, const float* d_grid = nullptr, int n_grid = 0) {
     BvpArgs a;
     fill_args(h, a, n, tot, y0_mode, d_params, d_n_init, d_tspans, d_y0, d_y0_off);
+    a.y0_grid = d_grid;
+    a.n_grid = n_grid;
     CU(cudaEventRecord(h->ev[0], h->stream));
     {
         long long np = (long long)n * h->desc.n_params;
@@ -572,14 +574,10 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
     if (bvp_mlp_forward_device(net, n, static_cast<const float*>(h->d_feat.p), static_cast<float*>(h->d_grid.p),
                                h->stream) != BVP_OK)
         return fail(h, BVP_ERR_CUDA, "surrogate forward failed");
-    if (bvp_resample_guess_device(n, n_grid, M, static_cast<const float*>(h->d_grid.p),
-                                  static_cast<const double*>(h->d_tspans.p), static_cast<const int*>(h->d_n_init.p),
-                                  static_cast<const int64_t*>(h->d_y0_off.p), static_cast<double*>(h->d_y0.p),
-                                  h->stream) != BVP_OK)
-        return fail(h, BVP_ERR_CUDA, "guess resampling failed");
-    s = launch_solve(h, n, tot, 1, static_cast<const double*>(h->d_params.p), static_cast<const int*>(h->d_n_init.p),
+    // the solve resamples the grid guesses onto the initial meshes itself (y0_mode 2)
+    s = launch_solve(h, n, tot, 2, static_cast<const double*>(h->d_params.p), static_cast<const int*>(h->d_n_init.p),
                      static_cast<const double*>(h->d_tspans.p), static_cast<const double*>(h->d_y0.p),
-                     static_cast<const long long*>(h->d_y0_off.p));
+                     static_cast<const long long*>(h->d_y0_off.p), static_cast<const float*>(h->d_grid.p), n_grid);
     if (s != BVP_OK) return s;
     s = finish(h, nullptr);
     if (s != BVP_OK) return s;
@@ -659,6 +657,24 @@ bvp_status bvp_solve_batch_device(bvp_handle* h, int32_t n, const double* d_para
     const double* dp = d_params ? d_params : static_cast<const double*>(h->d_params.p);
     s = launch_solve(h, n, tot, y0_mode, dp, d_n_intervals, d_tspans, d_y0,
                      reinterpret_cast<const long long*>(d_y0_off));
+    if (s != BVP_OK) return s;
+    h->pending_device = true;
+    h->have_results = false;
+    return BVP_OK;
+}
+
+bvp_status bvp_solve_batch_device_grid(bvp_handle* h, int32_t n, const double* d_params,
+                                       const int32_t* d_n_intervals, const double* d_tspans, const float* d_grid,
+                                       int32_t n_grid, int32_t max_intervals) {
+    if (!h) return BVP_ERR_INVALID;
+    if (n < 1 || !d_n_intervals || !d_tspans || !d_grid || n_grid < 2 || max_intervals < 1 ||
+        (h->desc.n_params > 0 && !d_params))
+        return fail(h, BVP_ERR_INVALID, "invalid arguments");
+    const long long tot = (long long)n * (std::max<int>(max_intervals, h->opt.max_subintervals) + 1);
+    bvp_status s = ensure_arena(h, tot, n, 1);
+    if (s != BVP_OK) return s;
+    s = launch_solve(h, n, tot, 2, d_params, d_n_intervals, d_tspans, static_cast<const double*>(h->d_y0.p),
+                     static_cast<const long long*>(h->d_y0_off.p), d_grid, n_grid);
     if (s != BVP_OK) return s;
     h->pending_device = true;
     h->have_results = false;

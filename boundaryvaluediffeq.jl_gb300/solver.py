@@ -187,6 +187,18 @@ class BatchSolver:
         self._check(st, "bvp_solve_batch_device")
         self._pending_n = n
 
+    def solve_device_grid(self, d_params, d_n_intervals, d_tspans, d_grid, n_grid, max_intervals):
+        """solve_device with the initial guesses on uniform n_grid-point grids (FP32 device
+        array n_inst x n_grid x M), resampled onto the initial meshes inside the solve."""
+        def ptr(x):
+            return C.c_void_p(x.data_ptr() if hasattr(x, "data_ptr") else int(x))
+        n = int(d_n_intervals.numel() if hasattr(d_n_intervals, "numel") else len(d_n_intervals))
+        st = self.lib.bvp_solve_batch_device_grid(self.h, n, ptr(d_params) if d_params is not None else None,
+                                                  ptr(d_n_intervals), ptr(d_tspans), ptr(d_grid), int(n_grid),
+                                                  int(max_intervals))
+        self._check(st, "bvp_solve_batch_device_grid")
+        self._pending_n = n
+
     def fetch(self) -> BatchResult:
         r, cr = self._results(self._pending_n)
         self._check(self.lib.bvp_fetch_results(self.h, C.byref(cr)), "bvp_fetch_results")

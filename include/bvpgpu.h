@@ -114,6 +114,14 @@ bvp_status bvp_solve_batch_device(bvp_handle* h, int32_t n_inst, const double* d
                                   int32_t y0_mode, const double* d_y0, const int64_t* d_y0_off,
                                   int32_t max_intervals);
 
+/* bvp_solve_batch_device with the initial guess given on a uniform grid of n_grid points
+ * over each instance's tspan (d_grid: n_inst x n_grid x M, FP32, e.g. a surrogate's output),
+ * resampled linearly onto the initial mesh inside the solve: the vector-of-arrays guess
+ * form of __initial_guess_on_mesh (Core/src/utils.jl:750-765) without a separate pass. */
+bvp_status bvp_solve_batch_device_grid(bvp_handle* h, int32_t n_inst, const double* d_params,
+                                       const int32_t* d_n_intervals, const double* d_tspans,
+                                       const float* d_grid, int32_t n_grid, int32_t max_intervals);
+
 /* Synchronise and bring the results of the last solve to the host. */
 bvp_status bvp_fetch_results(bvp_handle* h, bvp_results* out);
 
