@@ -130,6 +130,7 @@ struct Inst {
     const JT* pj;
     double* scr;
     int* iscr;
+    JT* dns;               // per-warp shared memory for the separator system
 };
 
 BVP_DEV double* mesh_of(const Args& a, const Inst& I, int b) { return a.mesh + b * a.tot + I.nb; }
@@ -145,6 +146,49 @@ template <class R> BVP_DEV const R* params_as(const Inst& I) {
 template <class R> BVP_DEV R y_at(const Args& a, const Inst& I, int k) {
     if constexpr (sizeof(R) == 8) return y_of(a, I, I.cur)[k];
     else return R(yj_of(a, I)[k]);
+}
+
+// Every evaluation of the problem's f goes through call_f. The evaluations of one scalar
+// type can share one out-of-line copy (the user's f and its math library calls, e.g. sin
+// with its large-argument path, are then in the kernel once instead of at every call site),
+// which keeps the fused kernel's hot code, and its instruction-cache misses, smaller.
+#ifndef BVP_F64_NOINLINE
+#define BVP_F64_NOINLINE 1
+#endif
+#ifndef BVP_F32_NOINLINE
+#define BVP_F32_NOINLINE 0
+#endif
+#ifndef BVP_DUAL_NOINLINE
+#define BVP_DUAL_NOINLINE 0
+#endif
+#if BVP_F64_NOINLINE
+__device__ __noinline__ void call_f64(double* du, const double* u, const double* p, double t) {
+    bvp_f<double, double>(du, u, p, t);
+}
+#endif
+#if BVP_F32_NOINLINE
+__device__ __noinline__ void call_f32(float* du, const float* u, const float* p, float t) {
+    bvp_f<float, float>(du, u, p, t);
+}
+#endif
+#if BVP_DUAL_NOINLINE
+__device__ __noinline__ void call_fdual(Dual<JT, D>* du, const Dual<JT, D>* u, const JT* p, JT t) {
+    bvp_f<Dual<JT, D>, JT>(du, u, p, t);
+}
+#endif
+template <class A, class B> struct same_t { static constexpr bool value = false; };
+template <class A> struct same_t<A, A> { static constexpr bool value = true; };
+template <class T, class PT> BVP_DEV void call_f(T* du, const T* u, const PT* p, PT t) {
+#if BVP_F64_NOINLINE
+    if constexpr (same_t<T, double>::value && same_t<PT, double>::value) { call_f64(du, u, p, t); return; }
+#endif
+#if BVP_F32_NOINLINE
+    if constexpr (same_t<T, float>::value && same_t<PT, float>::value) { call_f32(du, u, p, t); return; }
+#endif
+#if BVP_DUAL_NOINLINE
+    if constexpr (same_t<T, Dual<JT, D>>::value && same_t<PT, JT>::value) { call_fdual(du, u, p, t); return; }
+#endif
+    bvp_f<T, PT>(du, u, p, t);
 }
 
 // MIRK4/5/6 put their first two stages on the mesh nodes (c = v = 0 and c = v = 1, no x
@@ -171,7 +215,7 @@ BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, 
             continue;
         }
         if (NODE_SHARE && r == 1 && node) {
-            bvp_f<T, PT>(&Ki[M], yi1, p, PT(ti1));
+            call_f<T, PT>(&Ki[M], yi1, p, PT(ti1));
 #pragma unroll
             for (int m = 0; m < M; ++m) node[m] = Ki[M + m];
             continue;
@@ -185,7 +229,7 @@ BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, 
                 for (int m = 0; m < M; ++m) Y[m] = Y[m] + hi * (Ki[j * M + m] * PT(tab_x(r, j)));
             }
         }
-        bvp_f<T, PT>(&Ki[r * M], Y, p, PT(ti + TT(tab_c(r)) * hi_d));
+        call_f<T, PT>(&Ki[r * M], Y, p, PT(ti + TT(tab_c(r)) * hi_d));
     }
 #pragma unroll
     for (int m = 0; m < M; ++m) {
@@ -213,7 +257,7 @@ BVP_DEV void interp_stages(const T* yi, const T* yi1, const T* Ki, T* KIi, const
             for (int qq = 0; qq < r; ++qq) acc = acc + KIi[qq * M + m] * PT(tab_xs(r, S + qq));
             Y[m] = acc * hi + PT(1.0 - tab_vs(r)) * yi[m] + PT(tab_vs(r)) * yi1[m];
         }
-        bvp_f<T, PT>(&KIi[r * M], Y, p, PT(ti + tab_cs(r) * hi_d));
+        call_f<T, PT>(&KIi[r * M], Y, p, PT(ti + tab_cs(r) * hi_d));
     }
 }
 
@@ -333,7 +377,7 @@ BVP_DEV double residual(const Args& a, const Inst& I) {
         R y0v[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) y0v[m] = y_at<R>(a, I, i0 * M + m);
-        bvp_f<R, R>(node, y0v, pr, sizeof(R) == 8 ? R(mesh[i0]) : R(a.tj[I.nb + i0]));
+        call_f<R, R>(node, y0v, pr, sizeof(R) == 8 ? R(mesh[i0]) : R(a.tj[I.nb + i0]));
     }
     const double* y64 = y_of(a, I, I.cur);
     // interior BC points: the lane whose block holds the interval evaluates the
@@ -726,84 +770,88 @@ BVP_DEV bool dense_solve(int n, R* A, R* b) {
     return true;
 }
 
-// The separator system on the whole warp: lane r holds row r (n = nk M rows, at most
-// NDENSE <= 16) and its right-hand side in registers. Gaussian elimination with partial
-// pivoting: the pivot row (largest |a_rk|, the first on ties, as dense_solve picks it) is
-// found by a warp reduction and exchanged with row k by shuffles; then back substitution by
-// broadcasts. Writes δ at the separator nodes.
-constexpr bool WARP_DENSE = NDENSE <= 16;
+// The separator system on the whole warp, in shared memory (n = nk M <= NDENSE <= 32 rows
+// of DLD entries, the right-hand side in column n): lane r assembles and updates row r.
+// Gaussian elimination with partial pivoting (the pivot row, largest |a_rk| and the first
+// on ties as dense_solve picks it, found by a warp reduction; the exchange done across the
+// columns), then back substitution by columns. Loops rather than unrolled code: the solve
+// runs once per Newton step and stays small in the instruction cache. Writes δ at the
+// separator nodes.
+constexpr bool SMEM_DENSE = NDENSE <= 32;
+constexpr int DLD = NDENSE + 1 + ((NDENSE + 1) % 2 == 0 ? 1 : 0);   // odd row stride
 BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
     const int lane = lane_id();
     const int n = nk * M;
     const int row0 = (nk - 1) * M;
-    JT row[NDENSE];
-    JT rhs = JT(0);
-#pragma unroll
-    for (int c = 0; c < NDENSE; ++c) row[c] = JT(0);
-    if (lane < row0) {
-        // segment relation j: A δ_{kept j} + B δ_{kept j+1} = g
-        const int j = lane / M, r = lane - j * M;
-        const JT* seg = seg_of(I, j);
-#pragma unroll
-        for (int c = 0; c < NDENSE; ++c) {
-            const int cj = c - j * M;
-            if (cj >= 0 && cj < M) row[c] = seg[r * M + cj];
-            else if (cj >= M && cj < 2 * M) row[c] = seg[M * M + r * M + cj - M];
-        }
-        rhs = seg[2 * M * M + r];
-    } else if (lane < n) {
-        // BC row r: the blocks of every BC contribution, added at their separator columns
-        const int r = lane - row0;
-        const int nb = I.iscr[ISCR_NB];
-        for (int k = 0; k < nb; ++k) {
-            const int node = I.iscr[ISCR_BNODE + k];
-            int kj = 0;
-            while (kj < nk - 1 && I.iscr[ISCR_KEPT + kj] != node) ++kj;
-            const double* G = I.scr + SCR_BCBLK + k * M * M + r * M;
-#pragma unroll
-            for (int c = 0; c < NDENSE; ++c) {
-                const int cj = c - kj * M;
-                if (cj >= 0 && cj < M) row[c] += JT(G[cj]);
+    JT* A = I.dns;
+    if (lane < n) {
+        JT* ar = A + lane * DLD;
+        for (int c = 0; c <= n; ++c) ar[c] = JT(0);
+        if (lane < row0) {
+            // segment relation j: A δ_{kept j} + B δ_{kept j+1} = g
+            const int j = lane / M, r = lane - j * M;
+            const JT* seg = seg_of(I, j);
+            for (int c = 0; c < M; ++c) {
+                ar[j * M + c] = seg[r * M + c];
+                ar[(j + 1) * M + c] = seg[M * M + r * M + c];
             }
-        }
-        rhs = JT(-I.scr[SCR_BCRES + r]);
-    }
-    bool ok = true;
-#pragma unroll
-    for (int k = 0; k < NDENSE; ++k) {
-        if (k < n) {
-            JT v = (lane >= k && lane < n) ? fabs(row[k]) : JT(-1);
-            int pr = lane;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const JT v2 = __shfl_xor_sync(FULL, v, o);
-                const int p2 = __shfl_xor_sync(FULL, pr, o);
-                if (v2 > v || (v2 == v && p2 < pr)) { v = v2; pr = p2; }
+            ar[n] = seg[2 * M * M + r];
+        } else {
+            // BC row r: every BC contribution's block, added at its separator's columns
+            const int r = lane - row0;
+            const int nb = I.iscr[ISCR_NB];
+            for (int k = 0; k < nb; ++k) {
+                const int node = I.iscr[ISCR_BNODE + k];
+                int kj = 0;
+                while (kj < nk - 1 && I.iscr[ISCR_KEPT + kj] != node) ++kj;
+                const double* G = I.scr + SCR_BCBLK + k * M * M + r * M;
+                for (int c = 0; c < M; ++c) ar[kj * M + c] += JT(G[c]);
             }
-            ok = ok && v > JT(0) && isfinite(v);
-            const int src = lane == k ? pr : (lane == pr ? k : lane);
-#pragma unroll
-            for (int c = 0; c < NDENSE; ++c) row[c] = __shfl_sync(FULL, row[c], src);
-            rhs = __shfl_sync(FULL, rhs, src);
-            const JT inv = JT(1) / __shfl_sync(FULL, row[k], k);
-            const JT mlt = (lane > k && lane < n) ? row[k] * inv : JT(0);
-#pragma unroll
-            for (int c = k + 1; c < NDENSE; ++c) row[c] -= mlt * __shfl_sync(FULL, row[c], k);
-            rhs -= mlt * __shfl_sync(FULL, rhs, k);
+            ar[n] = JT(-I.scr[SCR_BCRES + r]);
         }
     }
-    JT x = JT(0);
+    __syncwarp();
+    for (int k = 0; k < n; ++k) {
+        JT v = (lane >= k && lane < n) ? fabs(A[lane * DLD + k]) : JT(-1);
+        int pr = lane;
 #pragma unroll
-    for (int k = NDENSE - 1; k >= 0; --k) {
-        if (k < n) {
-            const JT xk = __shfl_sync(FULL, rhs / row[k], k);
-            if (lane == k) x = xk;
-            if (lane < k) rhs -= row[k] * xk;
+        for (int o = 16; o > 0; o >>= 1) {
+            const JT v2 = __shfl_xor_sync(FULL, v, o);
+            const int p2 = __shfl_xor_sync(FULL, pr, o);
+            if (v2 > v || (v2 == v && p2 < pr)) { v = v2; pr = p2; }
         }
+        if (!(v > JT(0)) || !isfinite(v)) return false;   // uniform across the warp
+        if (pr != k) {
+            for (int c = lane; c <= n; c += 32) {
+                const JT t = A[k * DLD + c];
+                A[k * DLD + c] = A[pr * DLD + c];
+                A[pr * DLD + c] = t;
+            }
+            __syncwarp();
+        }
+        if (lane > k && lane < n) {
+            JT* ar = A + lane * DLD;
+            const JT* ak = A + k * DLD;
+            const JT mlt = ar[k] * (JT(1) / ak[k]);
+            for (int c = k + 1; c <= n; ++c) ar[c] -= mlt * ak[c];
+        }
+        __syncwarp();
     }
-    if (ok && lane < n) a.delta[(I.nb + I.iscr[ISCR_KEPT + lane / M]) * M + lane % M] = x;
-    return ok;
+    for (int k = n - 1; k >= 0; --k) {
+        if (lane == k) A[k * DLD + n] = A[k * DLD + n] / A[k * DLD + k];
+        __syncwarp();
+        if (lane < k) A[lane * DLD + n] -= A[lane * DLD + k] * A[k * DLD + n];
+        __syncwarp();
+    }
+    if (lane < n) a.delta[(I.nb + I.iscr[ISCR_KEPT + lane / M]) * M + lane % M] = A[lane * DLD + n];
+    __syncwarp();
+    return true;
 }
+
+#ifndef BVP_TREE_UNROLL
+#define BVP_TREE_UNROLL 1
+#endif
+constexpr int TREE_UNROLL = BVP_TREE_UNROLL;  // shuffle-tree levels unrolled (1: one copy of each step)
 
 // Newton direction δ (in a.delta) for J δ = -F. Returns false if singular.
 BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
@@ -835,7 +883,7 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     // 2. shuffle tree over the block relations of each lane group
     int bnode = bhi;
     int xs[5];
-#pragma unroll
+#pragma unroll TREE_UNROLL
     for (int s = 0; s < 5; ++s) {
         const int step = 1 << s;
         JT Ap[M * M], Bp[M * M], gp[M];
@@ -857,7 +905,7 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     __syncwarp();
     // 3. separator system
     int dense_ok = 1;
-    if constexpr (WARP_DENSE) {
+    if constexpr (SMEM_DENSE) {
         dense_ok = separator_solve_warp(a, I, nk) ? 1 : 0;
     } else if (lane == 0) {
         // in thread-local storage (L1-resident), not the global scratch: the elimination
@@ -906,7 +954,7 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
             db[m] = a.delta[(I.nb + nbk) * M + m];
         }
     }
-#pragma unroll
+#pragma unroll TREE_UNROLL
     for (int s = 4; s >= 0; --s) {
         const int step = 1 << s;
         const bool comb = active && (t % (2 * step)) == 0 && t + step < L;
@@ -1126,7 +1174,7 @@ BVP_DEV double defect(const Args& a, const Inst& I) {
                 for (int qq = 0; qq < NSX; ++qq) acc += KIi[qq * M + m] * wp[S + qq];
                 zp[m] = acc;
             }
-            bvp_f<double, double>(fz, z, I.p, mesh[i] + (smp ? 1.0 - tau_star() : tau_star()) * h[i]);
+            call_f<double, double>(fz, z, I.p, mesh[i] + (smp ? 1.0 - tau_star() : tau_star()) * h[i]);
             double e = 0.0;
 #pragma unroll
             for (int m = 0; m < M; ++m) e = fmax(e, fabs((zp[m] - fz[m]) / (fabs(fz[m]) + 1.0)));
@@ -1413,6 +1461,7 @@ BVP_DEV Inst make_inst(const Args& a, int q) {
     I.pj = a.params_j + (long long)q * a.n_params;
     I.scr = a.scr + (long long)q * SCRW;
     I.iscr = a.iscr + (long long)q * ISCRW;
+    I.dns = nullptr;
     I.N = 0;
     I.cur = 0;
     return I;
@@ -1430,6 +1479,7 @@ constexpr int WARPS_PER_BLOCK = 4;
 constexpr bool SCR_SMEM = WARPS_PER_BLOCK * (SCRW * 8 + ISCRW * 4) <= 40 * 1024;
 constexpr int SM_SCRW = SCR_SMEM ? SCRW : 1;
 constexpr int SM_ISCRW = SCR_SMEM ? ISCRW : 1;
+constexpr int SM_DNS = SMEM_DENSE ? NDENSE * DLD : 1;
 }  // namespace bvp
 
 // Persistent fused solve: each warp repeatedly takes the next instance from the work
@@ -1437,6 +1487,7 @@ constexpr int SM_ISCRW = SCR_SMEM ? ISCRW : 1;
 extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::Args a) {
     __shared__ double s_scr[bvp::WARPS_PER_BLOCK][bvp::SM_SCRW];
     __shared__ int s_iscr[bvp::WARPS_PER_BLOCK][bvp::SM_ISCRW];
+    __shared__ bvp::JT s_dns[bvp::WARPS_PER_BLOCK][bvp::SM_DNS];
     const int lane = bvp::lane_id();
     const int w = threadIdx.x >> 5;
     while (true) {
@@ -1446,6 +1497,7 @@ extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::
         if (k >= a.n_inst) break;
         bvp::Inst I = bvp::make_inst(a, a.order[k]);
         if (bvp::SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
+        I.dns = s_dns[w];
         bvp::solve_instance(a, I);
     }
 }
@@ -1457,6 +1509,7 @@ extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::
 extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, int stage, double* out_norm) {
     __shared__ double s_scr[bvp::WARPS_PER_BLOCK][bvp::SM_SCRW];
     __shared__ int s_iscr[bvp::WARPS_PER_BLOCK][bvp::SM_ISCRW];
+    __shared__ bvp::JT s_dns[bvp::WARPS_PER_BLOCK][bvp::SM_DNS];
     const int lane = bvp::lane_id();
     const int w = threadIdx.x >> 5;
     while (true) {
@@ -1468,6 +1521,7 @@ extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, i
         double* g_scr = I.scr;
         int* g_iscr = I.iscr;
         if (bvp::SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
+        I.dns = s_dns[w];
         I.N = a.st[I.q].N;
         I.cur = 0;
         bvp::mesh_setup(a, I);
