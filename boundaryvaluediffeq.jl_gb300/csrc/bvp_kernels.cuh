@@ -284,60 +284,71 @@ BVP_DEV void sum_stages(const W* w, const T* yi, const T* Ki, const T* KIi, W hi
 //  * the separator nodes of the partition solve: 0, N-1 and every node a BC row touches;
 //  * the lanes per separator segment: a power of two no larger than the segment,
 //    proportional to its share of the mesh, at least one, 32 in all.
+// interpolant weights at a run-time τ: one out-of-line copy for the mesh setup, the
+// transfer and dense output (the defect's constant τ* fold at compile time)
+__device__ __noinline__ void interp_weights_rt(double t, double* w, double* wp) { interp_weights<double>(t, w, wp); }
+
+// the lane-0 part of mesh_setup, out of line: it runs once per mesh round and its straight
+// code is better kept out of the hot loop's instruction stream
+__device__ __noinline__ void mesh_setup_lane0(const double* mesh, const double* h, int N, const double* bc_t,
+                                              int bc_jac_exact, double* scr, int* iscr) {
+    int kept[KMAX];
+    int nk = 0;
+    kept[nk++] = 0;
+    kept[nk++] = N - 1;
+    if (TWOPOINT) {
+        iscr[ISCR_UNODE] = 0; iscr[ISCR_UNODE + 1] = N - 1;
+        iscr[ISCR_UIN] = 0; iscr[ISCR_UIN + 1] = 0;
+    } else {
+        for (int k = 0; k < NBC; ++k) {
+            const double t = bc_t[k];
+            int node, in = 0;
+            if (t == mesh[0]) node = 0;
+            else if (t == mesh[N - 1]) node = N - 1;
+            else {
+                node = interval_of(mesh, N, t);
+                in = 1;
+                double w[SS], wp[SS];
+                interp_weights_rt((t - mesh[node]) / h[node], w, wp);
+                for (int s2 = 0; s2 < SS; ++s2) scr[SCR_BCW + k * SS + s2] = w[s2];
+            }
+            iscr[ISCR_UNODE + k] = node;
+            iscr[ISCR_UIN + k] = in;
+            kept[nk++] = node;
+            if (in && bc_jac_exact) kept[nk++] = node + 1;
+        }
+    }
+    for (int u = 1; u < nk; ++u) {
+        const int v = kept[u];
+        int w2 = u - 1;
+        while (w2 >= 0 && kept[w2] > v) { kept[w2 + 1] = kept[w2]; --w2; }
+        kept[w2 + 1] = v;
+    }
+    int nu = 0;
+    for (int u = 0; u < nk; ++u)
+        if (nu == 0 || kept[u] != kept[nu - 1]) kept[nu++] = kept[u];
+    iscr[ISCR_NK] = nu;
+    for (int u = 0; u < nu; ++u) iscr[ISCR_KEPT + u] = kept[u];
+    const int ns = nu - 1, m = N - 1;
+    int o = 0;
+    for (int j = 0; j < ns; ++j) {
+        const int len = kept[j + 1] - kept[j];
+        int want = 1 + ((32 - ns) * len) / m;
+        want = want < len ? want : len;
+        int L = 1;
+        while (2 * L <= want) L *= 2;
+        iscr[ISCR_LOFF + j] = o;
+        o += L;
+    }
+    iscr[ISCR_LOFF + ns] = o;
+}
+
 BVP_DEV void mesh_setup(const Args& a, const Inst& I) {
     if (lane_id() == 0) {
-        const double* mesh = mesh_of(a, I, I.cur);
-        const double* h = h_of(a, I, I.cur);
-        const int N = I.N;
-        int kept[KMAX];
-        int nk = 0;
-        kept[nk++] = 0;
-        kept[nk++] = N - 1;
-        if (TWOPOINT) {
-            I.iscr[ISCR_UNODE] = 0; I.iscr[ISCR_UNODE + 1] = N - 1;
-            I.iscr[ISCR_UIN] = 0; I.iscr[ISCR_UIN + 1] = 0;
-        } else {
-            for (int k = 0; k < NBC; ++k) {
-                const double t = a.bc_t[k];
-                int node, in = 0;
-                if (t == mesh[0]) node = 0;
-                else if (t == mesh[N - 1]) node = N - 1;
-                else {
-                    node = interval_of(mesh, N, t);
-                    in = 1;
-                    double w[SS], wp[SS];
-                    interp_weights<double>((t - mesh[node]) / h[node], w, wp);
-                    for (int s = 0; s < SS; ++s) I.scr[SCR_BCW + k * SS + s] = w[s];
-                }
-                I.iscr[ISCR_UNODE + k] = node;
-                I.iscr[ISCR_UIN + k] = in;
-                kept[nk++] = node;
-                if (in && a.bc_jac_exact) kept[nk++] = node + 1;
-            }
-        }
-        for (int u = 1; u < nk; ++u) {
-            const int v = kept[u];
-            int w2 = u - 1;
-            while (w2 >= 0 && kept[w2] > v) { kept[w2 + 1] = kept[w2]; --w2; }
-            kept[w2 + 1] = v;
-        }
-        int nu = 0;
-        for (int u = 0; u < nk; ++u)
-            if (nu == 0 || kept[u] != kept[nu - 1]) kept[nu++] = kept[u];
-        I.iscr[ISCR_NK] = nu;
-        for (int u = 0; u < nu; ++u) I.iscr[ISCR_KEPT + u] = kept[u];
-        const int ns = nu - 1, m = N - 1;
-        int o = 0;
-        for (int j = 0; j < ns; ++j) {
-            const int len = kept[j + 1] - kept[j];
-            int want = 1 + ((32 - ns) * len) / m;
-            want = want < len ? want : len;
-            int L = 1;
-            while (2 * L <= want) L *= 2;
-            I.iscr[ISCR_LOFF + j] = o;
-            o += L;
-        }
-        I.iscr[ISCR_LOFF + ns] = o;
+        double bt[NBC];
+#pragma unroll
+        for (int k = 0; k < NBC; ++k) bt[k] = a.bc_t[k];
+        mesh_setup_lane0(mesh_of(a, I, I.cur), h_of(a, I, I.cur), I.N, bt, a.bc_jac_exact, I.scr, I.iscr);
     }
     {
         // the mesh in the Jacobian precision (FP32 stage times without FP64 conversions)
@@ -400,7 +411,7 @@ BVP_DEV double residual(const Args& a, const Inst& I) {
             phi_interval<R, R, R>(yi, yi1, Ki, ri, pr, R(tj[i]), R(hj[i]), NODE_SHARE ? node : nullptr, R(tj[i + 1]),
                                   dy);
         }
-#pragma unroll
+#pragma unroll 1
         for (int k = 0; k < NBCP; ++k) {
             if (bc_iv[k] == i) {
                 R KIi[NSXA * M], w[SS], z[M];
@@ -786,6 +797,7 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
     JT* A = I.dns;
     if (lane < n) {
         JT* ar = A + lane * DLD;
+#pragma unroll 1
         for (int c = 0; c <= n; ++c) ar[c] = JT(0);
         if (lane < row0) {
             // segment relation j: A δ_{kept j} + B δ_{kept j+1} = g
@@ -800,6 +812,7 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
             // BC row r: every BC contribution's block, added at its separator's columns
             const int r = lane - row0;
             const int nb = I.iscr[ISCR_NB];
+#pragma unroll 1
             for (int k = 0; k < nb; ++k) {
                 const int node = I.iscr[ISCR_BNODE + k];
                 int kj = 0;
@@ -811,6 +824,7 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
         }
     }
     __syncwarp();
+#pragma unroll 1
     for (int k = 0; k < n; ++k) {
         JT v = (lane >= k && lane < n) ? fabs(A[lane * DLD + k]) : JT(-1);
         int pr = lane;
@@ -822,6 +836,7 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
         }
         if (!(v > JT(0)) || !isfinite(v)) return false;   // uniform across the warp
         if (pr != k) {
+#pragma unroll 1
             for (int c = lane; c <= n; c += 32) {
                 const JT t = A[k * DLD + c];
                 A[k * DLD + c] = A[pr * DLD + c];
@@ -833,10 +848,12 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
             JT* ar = A + lane * DLD;
             const JT* ak = A + k * DLD;
             const JT mlt = ar[k] * (JT(1) / ak[k]);
+#pragma unroll 1
             for (int c = k + 1; c <= n; ++c) ar[c] -= mlt * ak[c];
         }
         __syncwarp();
     }
+#pragma unroll 1
     for (int k = n - 1; k >= 0; --k) {
         if (lane == k) A[k * DLD + n] = A[k * DLD + n] / A[k * DLD + k];
         __syncwarp();
@@ -1297,7 +1314,7 @@ BVP_DEV void transfer(const Args& a, Inst& I, int newN) {
         const double dt = oh[i];
         const double tau = (t - om[i]) / dt;
         double w[SS], wp[SS];
-        interp_weights<double>(tau, w, wp);
+        interp_weights_rt(tau, w, wp);
         const double* Kg = a.K + (I.nb + i) * (S * M);
         const double* KIg = a.KI + (I.nb + i) * (NSXA * M);
 #pragma unroll
@@ -1580,7 +1597,7 @@ extern "C" __global__ void bvp_dense(const bvp::Args a, int nq, const double* tq
         const int i = interval_of(mesh, N, t);
         const double dt = a.h[nb + i];
         double w[SS], wp[SS];
-        interp_weights<double>((t - mesh[i]) / dt, w, wp);
+        interp_weights_rt((t - mesh[i]) / dt, w, wp);
         const double* wv = deriv ? wp : w;
         const double* Kg = a.K + (nb + i) * (S * M);
         const double* KIg = a.KI + (nb + i) * (NSXA * M);
