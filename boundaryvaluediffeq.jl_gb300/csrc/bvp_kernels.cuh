@@ -520,11 +520,11 @@ BVP_DEV void write_bc_block(const Inst& I, int slot, int node, const double* G) 
     for (int q = 0; q < M * M; ++q) dst[q] = G[q];
 }
 
-BVP_DEV void jacobian(const Args& a, const Inst& I) {
+// the collocation blocks of every interval into Sb / Rb (the Newton solve computes them inside
+// its block elimination instead; this pass serves the per-kernel tests)
+BVP_DEV void jacobian_blocks(const Args& a, const Inst& I) {
     using DI = Dual<JT, D>;
     const int lane = lane_id();
-    const double* mesh = mesh_of(a, I, I.cur);
-    const double* h = h_of(a, I, I.cur);
     const JT* yj = yj_of(a, I);
     const JT* tj = a.tj + I.nb;
     const JT* hj = a.hj + I.nb;
@@ -546,6 +546,16 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
                 Rg[r * M + c] = ri[r].d[M + c];
             }
     }
+    __syncwarp();
+}
+
+// the BC rows' Jacobian blocks (scratch), from u at the BC points cached by the last residual
+BVP_DEV void bc_jacobian(const Args& a, const Inst& I) {
+    using DI = Dual<JT, D>;
+    const int lane = lane_id();
+    const double* mesh = mesh_of(a, I, I.cur);
+    const double* h = h_of(a, I, I.cur);
+    const JT* yj = yj_of(a, I);
     using DU = Dual<JT, M>;
     const double* ua_c = I.scr + SCR_UA;
     double G[M * M];
@@ -630,6 +640,11 @@ BVP_DEV void jacobian(const Args& a, const Inst& I) {
         if (lane == 0) I.iscr[ISCR_NB] = a.bc_jac_exact ? 2 * NBC : NBC;
     }
     __syncwarp();
+}
+
+BVP_DEV void jacobian(const Args& a, const Inst& I) {
+    jacobian_blocks(a, I);
+    bc_jacobian(a, I);
 }
 
 // ---- K3: structured factorisation + solve (warp) -----------------------------------------
@@ -870,6 +885,35 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
 #endif
 constexpr int TREE_UNROLL = BVP_TREE_UNROLL;  // shuffle-tree levels unrolled (1: one copy of each step)
 
+// S_c = ∂r_c/∂y_c and R_c = ∂r_c/∂y_{c+1} of interval c by forward mode (2M tangents), the same
+// blocks jacobian_blocks writes. With NODE_SHARE, node holds f at y_c with its tangents in the
+// y_c slots on entry, and f at y_{c+1} with its tangents moved to the y_{c+1}-as-left-node
+// slots on return (the next interval's first stage).
+BVP_DEV void block_jacobian(const JT* yj, const JT* tj, const JT* hj, const JT* pj, int c, Dual<JT, D>* node,
+                            JT* Sr, JT* Rr) {
+    using DI = Dual<JT, D>;
+    DI yi[M], yi1[M], Ki[S * M], ri[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        yi[m] = DI(yj[c * M + m]); yi[m].d[m] = JT(1);
+        yi1[m] = DI(yj[(c + 1) * M + m]); yi1[m].d[M + m] = JT(1);
+    }
+    phi_interval<DI, JT, JT>(yi, yi1, Ki, ri, pj, tj[c], hj[c], NODE_SHARE ? node : nullptr, tj[c + 1]);
+    if (NODE_SHARE) {
+#pragma unroll
+        for (int m = 0; m < M; ++m)
+#pragma unroll
+            for (int k = 0; k < M; ++k) { node[m].d[k] = node[m].d[M + k]; node[m].d[M + k] = JT(0); }
+    }
+#pragma unroll
+    for (int r = 0; r < M; ++r)
+#pragma unroll
+        for (int cc = 0; cc < M; ++cc) {
+            Sr[r * M + cc] = ri[r].d[cc];
+            Rr[r * M + cc] = ri[r].d[M + cc];
+        }
+}
+
 // Newton direction δ (in a.delta) for J δ = -F. Returns false if singular.
 BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     const int lane = lane_id();
@@ -887,14 +931,36 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     const int blo = na + (t * len) / L;            // block [blo, bhi)
     const int bhi = na + ((t + 1) * len) / L;
     bool bad = false;
-    // 1. sequential elimination inside the block
+    // 1. sequential elimination inside the block, each interval's Jacobian blocks computed
+    //    where they are used (block_jacobian) instead of read back from memory
     JT A[M * M], B[M * M], g[M];
     if (active) {
-        load_eq0(a, I, blo, A, B, g);
-        for (int c = blo + 1; c < bhi; ++c) {
-            JT Ar[M * M], Br[M * M], gr[M];
-            load_eq0(a, I, c, Ar, Br, gr);
-            bad |= !eliminate_pair(A, B, g, Ar, Br, gr, a.rec + (I.nb + c) * RECW, A, B, g);
+        using DI = Dual<JT, D>;
+        const JT* yj = yj_of(a, I);
+        const JT* tj = a.tj + I.nb;
+        const JT* hj = a.hj + I.nb;
+        const JT* Fj = a.Fj + I.nb * M;
+        DI node[M];
+        {
+            DI y0v[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) { y0v[m] = DI(yj[blo * M + m]); y0v[m].d[m] = JT(1); }
+            if (NODE_SHARE) call_f<DI, JT>(node, y0v, I.pj, tj[blo]);
+        }
+#pragma unroll 1
+        for (int c = blo; c < bhi; ++c) {
+            JT Sr[M * M], Rr[M * M], gr[M];
+            block_jacobian(yj, tj, hj, I.pj, c, node, Sr, Rr);
+#pragma unroll
+            for (int m = 0; m < M; ++m) gr[m] = -Fj[c * M + m];
+            if (c == blo) {
+#pragma unroll
+                for (int q = 0; q < M * M; ++q) { A[q] = Sr[q]; B[q] = Rr[q]; }
+#pragma unroll
+                for (int m = 0; m < M; ++m) g[m] = gr[m];
+            } else {
+                bad |= !eliminate_pair(A, B, g, Sr, Rr, gr, a.rec + (I.nb + c) * RECW, A, B, g);
+            }
         }
     }
     // 2. shuffle tree over the block relations of each lane group
@@ -1006,12 +1072,36 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
         JT dn[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) dn[m] = db[m];
-        for (int c = bhi - 1; c > blo; --c) {
-            JT dc[M];
-            back_solve(a.rec + (I.nb + c) * RECW, da, dn, dc);
-            JT* dg = a.delta + (I.nb + c) * M;
+        if constexpr (RECW <= 32) {
+            // records in registers, the next one loaded while this one is applied
+            const JT* rbase = a.rec + I.nb * RECW;
+            JT rc[RECW], rn[RECW];
+            if (bhi - 1 > blo) {
 #pragma unroll
-            for (int m = 0; m < M; ++m) { dg[m] = dc[m]; dn[m] = dc[m]; bad |= !isfinite(dc[m]); }
+                for (int q = 0; q < RECW; ++q) rc[q] = rbase[(bhi - 1) * RECW + q];
+            }
+#pragma unroll 1
+            for (int c = bhi - 1; c > blo; --c) {
+                if (c - 1 > blo) {
+#pragma unroll
+                    for (int q = 0; q < RECW; ++q) rn[q] = rbase[(c - 1) * RECW + q];
+                }
+                JT dc[M];
+                back_solve(rc, da, dn, dc);
+                JT* dg = a.delta + (I.nb + c) * M;
+#pragma unroll
+                for (int m = 0; m < M; ++m) { dg[m] = dc[m]; dn[m] = dc[m]; bad |= !isfinite(dc[m]); }
+#pragma unroll
+                for (int q = 0; q < RECW; ++q) rc[q] = rn[q];
+            }
+        } else {
+            for (int c = bhi - 1; c > blo; --c) {
+                JT dc[M];
+                back_solve(a.rec + (I.nb + c) * RECW, da, dn, dc);
+                JT* dg = a.delta + (I.nb + c) * M;
+#pragma unroll
+                for (int m = 0; m < M; ++m) { dg[m] = dc[m]; dn[m] = dc[m]; bad |= !isfinite(dc[m]); }
+            }
         }
 #pragma unroll
         for (int m = 0; m < M; ++m) bad |= !isfinite(da[m]) || !isfinite(db[m]);
@@ -1103,7 +1193,7 @@ BVP_DEV bool newton_attempt(const Args& a, Inst& I, bool linesearch, int& iters,
             else if (++stall >= a.stall_steps) return false;
         }
         if (iters >= a.max_newton) return false;
-        jacobian(a, I);
+        bc_jacobian(a, I);
         if (!linear_solve(a, I)) return false;
         ++iters;
         if (!linesearch) {
@@ -1544,7 +1634,7 @@ extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, i
         bvp::mesh_setup(a, I);
         bvp::refresh_yj(a, I);
         double v = bvp::residual<double>(a, I);
-        if (stage >= 1 && stage <= 2) bvp::jacobian(a, I);
+        if (stage >= 1 && stage <= 2) bvp::jacobian(a, I);  // stage 2's solve recomputes the same blocks
         if (stage == 2) v = bvp::linear_solve(a, I) ? 0.0 : 1.0;
         if (stage == 3) v = bvp::defect(a, I);
         if (lane == 0) out_norm[I.q] = v;
