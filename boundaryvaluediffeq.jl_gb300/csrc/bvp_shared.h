@@ -33,7 +33,7 @@ struct BvpArgs {
     double abstol, defect_threshold, divergence_factor;
     double bc_t[16];
     bvp_i64 tot;                   // total node capacity (sum over instances)
-    const int* order;              // work order (instance ids, costliest first)
+    const int* order;              // work order (instance ids, coarsest initial mesh first)
     int* work_counter;
     const double* params;          // n_inst x n_params
     const BVP_JT_PTR* params_j;    // same, in the Jacobian precision
