@@ -206,6 +206,11 @@ def run_reference(args):
     return 0
 
 
+# DRAM bytes (read + write) of one bvp_solve_fused launch per instance, from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum) of the surrogate-warm solve of the
+# 2048-instance pendulum batch: 54.56 MB / 2048. Traffic grows with the instance count, so
+# the roofline's traffic is this figure times the batch size.
+FUSED_DRAM_BYTES_PER_INSTANCE = 54.56e6 / 2048
 N_TRAIN = 50000
 TRAIN_SEED = SEED + 10_000      # training instances are disjoint from the timed batch
 GRID = 64
@@ -378,9 +383,10 @@ def main():
     warm_fallback_e2e = int(nfb[0])
     warm_fail = int((out["retcode"] != 0).sum())
     h2d_plain = pa.nbytes + na.nbytes + ta.nbytes + ya.nbytes
-    h2d_warm = pa.nbytes + na.nbytes + ta.nbytes + fa.nbytes + (n + 1) * 8
-    d2h_plain = n * 40 + plain_nodes * 8 * 3   # per-instance state + packed mesh and solution
-    d2h_warm = n * 40 + warm_nodes * 8 * 3
+    h2d_warm = pa.nbytes + na.nbytes + ta.nbytes + fa.nbytes
+    # per-instance state (40 B), packed offsets, packed mesh and solution (M = 2)
+    d2h_plain = n * 40 + (n + 1) * 8 + plain_nodes * 8 * 3
+    d2h_warm = n * 40 + (n + 1) * 8 + warm_nodes * 8 * 3
 
     if rank != 0:
         if ws > 1:
@@ -421,7 +427,9 @@ def main():
                   "fused_ms_mean": statistics.mean(plain_fused)},
         "gpu_launches": launches_warm * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                     "frac": achieved / peaks.get("hbm_gbs", 1.0), "traffic": None,
+                     "frac": achieved / peaks.get("hbm_gbs", 1.0),
+                     "traffic": FUSED_DRAM_BYTES_PER_INSTANCE * n_inst,
+                     "algorithmic_bytes": alg_bytes,
                      "kernel": "bvp_solve_fused", "peak_source": src,
                      "note": "algorithmic bytes of K1-K4 per interval x Newton iterations / fused kernel time "
                              "(surrogate-warm solve)"},

@@ -1648,11 +1648,13 @@ extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, i
 }
 
 // Copy the results of every instance (buffer 0) into packed host-bound arrays.
-extern "C" __global__ void bvp_pack(const bvp::Args a, const long long* out_off, double* mesh_out,
+// out_off has n_inst + 1 entries (bvp_out_offsets); the outputs hold cap points: a batch
+// whose packed size exceeds cap writes nothing (the host grows the outputs and packs again).
+extern "C" __global__ void bvp_pack(const bvp::Args a, const long long* out_off, long long cap, double* mesh_out,
                                     double* y_out, int want_stages, double* K_out, double* KI_out) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = bvp::lane_id();
-    if (warp >= a.n_inst) return;
+    if (warp >= a.n_inst || out_off[a.n_inst] > cap) return;
     const int q = warp;
     const long long nb = a.node_off[q];
     const int N = a.st[q].N;
@@ -1666,6 +1668,51 @@ extern "C" __global__ void bvp_pack(const bvp::Args a, const long long* out_off,
         for (int k = lane; k < (N - 1) * bvp::NSXA * bvp::M; k += 32)
             KI_out[o * bvp::NSXA * bvp::M + k] = a.KI[nb * bvp::NSXA * bvp::M + k];
     }
+}
+
+// Packed-output offsets of the last solve: the exclusive prefix sum of every instance's final
+// point count (n + 1 entries, into d_off and the host-mapped h_off) and a copy of the
+// per-instance states into host-mapped h_st. One block.
+extern "C" __global__ void __launch_bounds__(1024) bvp_out_offsets(int n, const BvpInstState* st, long long* d_off,
+                                                                   long long* h_off, BvpInstState* h_st) {
+    __shared__ long long wsum[32];
+    __shared__ long long carry;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int q = base + tid;
+        long long c = 0;
+        if (q < n) {
+            const BvpInstState sq = st[q];
+            h_st[q] = sq;
+            c = sq.N;
+        }
+        long long v = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long t = __shfl_up_sync(bvp::FULL, v, o);
+            if (lane >= o) v += t;
+        }
+        if (lane == 31) wsum[warp] = v;
+        __syncthreads();
+        if (warp == 0) {
+            long long w = (lane < int(blockDim.x >> 5)) ? wsum[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long t = __shfl_up_sync(bvp::FULL, w, o);
+                if (lane >= o) w += t;
+            }
+            wsum[lane] = w;
+        }
+        __syncthreads();
+        const long long excl = carry + (warp > 0 ? wsum[warp - 1] : 0) + v - c;
+        if (q < n) { d_off[q] = excl; h_off[q] = excl; }
+        __syncthreads();
+        if (tid == 0) carry += wsum[31];
+        __syncthreads();
+    }
+    if (tid == 0) { d_off[n] = carry; h_off[n] = carry; }
 }
 
 // Dense output of the last solve (needs want_stages): u(t) or u'(t) at nq query times per

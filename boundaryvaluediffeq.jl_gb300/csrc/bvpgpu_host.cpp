@@ -51,7 +51,7 @@ struct bvp_handle_s {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaLibrary_t lib = nullptr;
-    cudaKernel_t k_fused = nullptr, k_stage = nullptr, k_pack = nullptr, k_probe = nullptr,
+    cudaKernel_t k_fused = nullptr, k_stage = nullptr, k_pack = nullptr, k_probe = nullptr, k_offsets = nullptr,
                  k_convert = nullptr, k_prep = nullptr, k_dense = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     // device arrays
@@ -61,6 +61,7 @@ struct bvp_handle_s {
         d_out_y, d_out_K, d_out_KI, d_norm, d_feat, d_grid;
     // pinned host staging
     HostBuf h_in, h_st, h_off, h_mesh, h_y, h_K, h_KI;
+    long long out_cap = 0;   // points the packed host outputs hold
     // last batch
     int last_n = 0;
     long long last_tot = 0;
@@ -227,6 +228,7 @@ static bvp_status compile_and_load(bvp_handle* h) {
     CU(cudaLibraryGetKernel(&h->k_fused, h->lib, "bvp_solve_fused"));
     CU(cudaLibraryGetKernel(&h->k_stage, h->lib, "bvp_stage"));
     CU(cudaLibraryGetKernel(&h->k_pack, h->lib, "bvp_pack"));
+    CU(cudaLibraryGetKernel(&h->k_offsets, h->lib, "bvp_out_offsets"));
     CU(cudaLibraryGetKernel(&h->k_probe, h->lib, "bvp_layout_probe"));
     CU(cudaLibraryGetKernel(&h->k_convert, h->lib, "bvp_convert_params"));
     CU(cudaLibraryGetKernel(&h->k_prep, h->lib, "bvp_prep"));
@@ -418,14 +420,78 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
     return BVP_OK;
 }
 
-// Brings per-instance state and packed solutions of the last solve to the host.
+// host pointer of pinned memory as the device sees it (the same pointer under unified addressing)
+static void* dev_view_raw(void* p) {
+    void* d = nullptr;
+    if (cudaHostGetDevicePointer(&d, p, 0) != cudaSuccess) return nullptr;
+    return d;
+}
+#define dev_view_d(p) static_cast<double*>(dev_view_raw(p))
+
+static bvp_status grow_outputs(bvp_handle* h, long long pts) {
+    const int M = h->L.M;
+    const bool stages = h->opt.want_stages != 0;
+    if (!ensure_host(h->h_mesh, size_t(pts) * 8) || !ensure_host(h->h_y, size_t(pts) * M * 8) ||
+        (stages && (!ensure_host(h->h_K, size_t(pts) * h->L.S * M * 8) ||
+                    !ensure_host(h->h_KI, size_t(pts) * h->L.NSXA * M * 8))))
+        return fail(h, BVP_ERR_NOMEM, "output allocation failed");
+    h->out_cap = pts;
+    return BVP_OK;
+}
+
+static bvp_status launch_pack(bvp_handle* h, int n) {
+    BvpArgs a;
+    fill_args(h, a, n, h->last_tot, 0, static_cast<const double*>(h->d_params.p), nullptr, nullptr, nullptr, nullptr);
+    const long long* oo = static_cast<const long long*>(h->d_out_off.p);
+    long long cap = h->out_cap;
+    double* om = dev_view_d(h->h_mesh.p);
+    double* oy = dev_view_d(h->h_y.p);
+    const bool stages = h->opt.want_stages != 0;
+    int ws = stages ? 1 : 0;
+    double* oK = stages ? dev_view_d(h->h_K.p) : nullptr;
+    double* oKI = stages ? dev_view_d(h->h_KI.p) : nullptr;
+    if (!om || !oy || (stages && (!oK || !oKI))) return fail(h, BVP_ERR_CUDA, "host output not mapped");
+    void* args[] = {&a, &oo, &cap, &om, &oy, &ws, &oK, &oKI};
+    const int blocks = (n * 32 + 255) / 256;
+    CU(cudaLaunchKernel((const void*)h->k_pack, dim3(std::max(1, blocks)), dim3(256), args, 0, h->stream));
+    return BVP_OK;
+}
+
+// Brings per-instance state and packed solutions of the last solve to the host: the offsets
+// and the packing run on the device right behind the solve and write into pinned host memory
+// the device maps (no separate copies, one synchronisation); a batch larger than the outputs
+// hold grows them and packs once more.
 static bvp_status finish(bvp_handle* h, bvp_results* out) {
     const int n = h->last_n;
-    const int M = h->L.M;
-    if (!ensure_host(h->h_st, size_t(n) * sizeof(BvpInstState)))
+    if (!ensure_host(h->h_st, size_t(n) * sizeof(BvpInstState)) || !ensure_host(h->h_off, size_t(n + 1) * 8) ||
+        !ensure_dev(h->d_out_off, size_t(n + 1) * 8))
         return fail(h, BVP_ERR_NOMEM, "pinned allocation failed");
-    CU(cudaMemcpyAsync(h->h_st.p, h->d_st.p, size_t(n) * sizeof(BvpInstState), cudaMemcpyDeviceToHost, h->stream));
+    if (h->out_cap == 0) {
+        bvp_status s0 = grow_outputs(h, 1024);
+        if (s0 != BVP_OK) return s0;
+    }
+    {
+        int nn = n;
+        const BvpInstState* dst_ = static_cast<const BvpInstState*>(h->d_st.p);
+        long long* doff = static_cast<long long*>(h->d_out_off.p);
+        long long* hoff = static_cast<long long*>(dev_view_raw(h->h_off.p));
+        BvpInstState* hst = static_cast<BvpInstState*>(dev_view_raw(h->h_st.p));
+        if (!hoff || !hst) return fail(h, BVP_ERR_CUDA, "host output not mapped");
+        void* args[] = {&nn, &dst_, &doff, &hoff, &hst};
+        CU(cudaLaunchKernel((const void*)h->k_offsets, dim3(1), dim3(1024), args, 0, h->stream));
+    }
+    bvp_status s = launch_pack(h, n);
+    if (s != BVP_OK) return s;
     CU(cudaStreamSynchronize(h->stream));
+    const int64_t* off = static_cast<const int64_t*>(h->h_off.p);
+    const long long tot_out = off[n];
+    if (tot_out > h->out_cap) {
+        s = grow_outputs(h, tot_out + tot_out / 4);
+        if (s != BVP_OK) return s;
+        s = launch_pack(h, n);
+        if (s != BVP_OK) return s;
+        CU(cudaStreamSynchronize(h->stream));
+    }
     float ms0 = 0, ms1 = 0;
     cudaEventElapsedTime(&ms0, h->ev[0], h->ev[2]);
     cudaEventElapsedTime(&ms1, h->ev[1], h->ev[2]);
@@ -433,42 +499,7 @@ static bvp_status finish(bvp_handle* h, bvp_results* out) {
     h->timing_ms[1] = ms1;
     const BvpInstState* st = static_cast<const BvpInstState*>(h->h_st.p);
     h->st.assign(st, st + n);
-    if (!ensure_host(h->h_off, size_t(n + 1) * 8)) return fail(h, BVP_ERR_NOMEM, "pinned allocation failed");
-    int64_t* off = static_cast<int64_t*>(h->h_off.p);
-    off[0] = 0;
-    for (int q = 0; q < n; ++q) off[q + 1] = off[q] + st[q].N;
-    const long long tot_out = off[n];
     h->offsets.assign(off, off + n + 1);
-    const bool stages = h->opt.want_stages != 0;
-    if (!ensure_dev(h->d_out_mesh, size_t(tot_out) * 8) || !ensure_dev(h->d_out_y, size_t(tot_out) * M * 8) ||
-        !ensure_host(h->h_mesh, size_t(tot_out) * 8) || !ensure_host(h->h_y, size_t(tot_out) * M * 8))
-        return fail(h, BVP_ERR_NOMEM, "output allocation failed");
-    if (stages && (!ensure_dev(h->d_out_K, size_t(tot_out) * h->L.S * M * 8) ||
-                   !ensure_dev(h->d_out_KI, size_t(tot_out) * h->L.NSXA * M * 8) ||
-                   !ensure_host(h->h_K, size_t(tot_out) * h->L.S * M * 8) ||
-                   !ensure_host(h->h_KI, size_t(tot_out) * h->L.NSXA * M * 8)))
-        return fail(h, BVP_ERR_NOMEM, "output allocation failed");
-    CU(cudaMemcpyAsync(h->d_out_off.p, off, size_t(n + 1) * 8, cudaMemcpyHostToDevice, h->stream));
-    {
-        BvpArgs a;
-        fill_args(h, a, n, h->last_tot, 0, static_cast<const double*>(h->d_params.p), nullptr, nullptr, nullptr, nullptr);
-        const long long* oo = static_cast<const long long*>(h->d_out_off.p);
-        double* om = static_cast<double*>(h->d_out_mesh.p);
-        double* oy = static_cast<double*>(h->d_out_y.p);
-        int ws = stages ? 1 : 0;
-        double* oK = static_cast<double*>(h->d_out_K.p);
-        double* oKI = static_cast<double*>(h->d_out_KI.p);
-        void* args[] = {&a, &oo, &om, &oy, &ws, &oK, &oKI};
-        const int blocks = (n * 32 + 255) / 256;
-        CU(cudaLaunchKernel((const void*)h->k_pack, dim3(std::max(1, blocks)), dim3(256), args, 0, h->stream));
-    }
-    CU(cudaMemcpyAsync(h->h_mesh.p, h->d_out_mesh.p, size_t(tot_out) * 8, cudaMemcpyDeviceToHost, h->stream));
-    CU(cudaMemcpyAsync(h->h_y.p, h->d_out_y.p, size_t(tot_out) * M * 8, cudaMemcpyDeviceToHost, h->stream));
-    if (stages) {
-        CU(cudaMemcpyAsync(h->h_K.p, h->d_out_K.p, size_t(tot_out) * h->L.S * M * 8, cudaMemcpyDeviceToHost, h->stream));
-        CU(cudaMemcpyAsync(h->h_KI.p, h->d_out_KI.p, size_t(tot_out) * h->L.NSXA * M * 8, cudaMemcpyDeviceToHost, h->stream));
-    }
-    CU(cudaStreamSynchronize(h->stream));
     if (out) {
         for (int q = 0; q < n; ++q) {
             if (out->retcode) out->retcode[q] = st[q].retcode;
@@ -546,31 +577,26 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
         tot += std::max(ni, h->opt.max_subintervals) + 1;
         y0_vals += (long long)(ni + 1) * M;
     }
-    bvp_status s = ensure_arena(h, tot, n, y0_vals);
+    (void)y0_vals;
+    bvp_status s = ensure_arena(h, tot, n, 1);
     if (s != BVP_OK) return s;
+    // inputs staged through pinned memory: parameters, tspans, interval counts, features
     const int P = h->desc.n_params;
-    const size_t b_params = size_t(n) * P * 8, b_ni = size_t(n) * 4, b_ts = size_t(n) * 16,
-                 b_off = size_t(n + 1) * 8;
-    if (!ensure_host(h->h_in, b_params + b_ni + b_ts + b_off + 64)) return fail(h, BVP_ERR_NOMEM, "pinned allocation failed");
+    const int nfeat = n_features;
+    const size_t b_params = size_t(n) * P * 8, b_ts = size_t(n) * 16, b_ni = size_t(n) * 4,
+                 b_feat = size_t(n) * nfeat * 4;
+    if (!ensure_host(h->h_in, b_params + b_ts + b_ni + b_feat + 64)) return fail(h, BVP_ERR_NOMEM, "pinned allocation failed");
+    if (!ensure_dev(h->d_feat, b_feat) || !ensure_dev(h->d_grid, size_t(n) * n_grid * M * 4))
+        return fail(h, BVP_ERR_NOMEM, "device allocation failed");
     char* hp = static_cast<char*>(h->h_in.p);
     std::memcpy(hp, params, b_params);
-    std::memcpy(hp + b_params, n_intervals, b_ni);
-    std::memcpy(hp + b_params + b_ni, tspans, b_ts);
-    int64_t* yoff = reinterpret_cast<int64_t*>(hp + b_params + b_ni + b_ts);
-    {
-        long long acc = 0;
-        for (int q = 0; q < n; ++q) { yoff[q] = acc; acc += n_intervals[q] + 1; }
-        yoff[n] = acc;
-    }
+    std::memcpy(hp + b_params, tspans, b_ts);
+    std::memcpy(hp + b_params + b_ts, n_intervals, b_ni);
+    std::memcpy(hp + b_params + b_ts + b_ni, features, b_feat);
     if (b_params) CU(cudaMemcpyAsync(h->d_params.p, hp, b_params, cudaMemcpyHostToDevice, h->stream));
-    CU(cudaMemcpyAsync(h->d_n_init.p, hp + b_params, b_ni, cudaMemcpyHostToDevice, h->stream));
-    CU(cudaMemcpyAsync(h->d_tspans.p, hp + b_params + b_ni, b_ts, cudaMemcpyHostToDevice, h->stream));
-    CU(cudaMemcpyAsync(h->d_y0_off.p, yoff, b_off, cudaMemcpyHostToDevice, h->stream));
-    // features and the network's grid output
-    const int nfeat = n_features;
-    if (!ensure_dev(h->d_feat, size_t(n) * nfeat * 4) || !ensure_dev(h->d_grid, size_t(n) * n_grid * M * 4))
-        return fail(h, BVP_ERR_NOMEM, "device allocation failed");
-    CU(cudaMemcpyAsync(h->d_feat.p, features, size_t(n) * nfeat * 4, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_tspans.p, hp + b_params, b_ts, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_n_init.p, hp + b_params + b_ts, b_ni, cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_feat.p, hp + b_params + b_ts + b_ni, b_feat, cudaMemcpyHostToDevice, h->stream));
     if (bvp_mlp_forward_device(net, n, static_cast<const float*>(h->d_feat.p), static_cast<float*>(h->d_grid.p),
                                h->stream) != BVP_OK)
         return fail(h, BVP_ERR_CUDA, "surrogate forward failed");
