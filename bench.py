@@ -355,12 +355,15 @@ def main():
     fa = np.ascontiguousarray(feats)
     nfb = np.zeros(1, np.int32)
 
+    # the host buffers' pointers are taken once, as a C caller holds them
+    p_pa, p_na, p_ta, p_ya, p_fa = f64(pa), i32(na), f64(ta), f64(ya), fa.ctypes.data_as(C.POINTER(C.c_float))
+    p_cr, p_nfb = C.byref(cr), i32(nfb)
+
     def e2e_plain():
-        return lib.bvp_solve_batch(sv.h, n, f64(pa), i32(na), f64(ta), 0, f64(ya), C.byref(cr))
+        return lib.bvp_solve_batch(sv.h, n, p_pa, p_na, p_ta, 0, p_ya, p_cr)
 
     def e2e_warm():
-        return lib.bvp_solve_batch_warm(sv.h, net.h, n, fa.shape[1], fa.ctypes.data_as(C.POINTER(C.c_float)), GRID,
-                                        f64(pa), i32(na), f64(ta), f64(ya), C.byref(cr), i32(nfb))
+        return lib.bvp_solve_batch_warm(sv.h, net.h, n, fa.shape[1], p_fa, GRID, p_pa, p_na, p_ta, p_ya, p_cr, p_nfb)
 
     def run_e2e(call):
         for _ in range(2):

@@ -1556,6 +1556,30 @@ BVP_DEV void solve_instance(const Args& a, Inst& I) {
     s.N = I.N;
     s.cur = 0;
     if (lane_id() == 0) a.st[I.q] = s;
+    if (a.host_mesh) {
+        // results to the host while the rest of the batch still runs: room from the cursor,
+        // so the host's packed arrays hold instances in completion order
+        unsigned long long start = 0;
+        if (lane_id() == 0) start = atomicAdd(a.out_cursor, (unsigned long long)I.N);
+        start = __shfl_sync(FULL, start, 0);
+        const bool fits = (long long)start + I.N <= a.host_cap;
+        if (fits) {
+            const double* m0 = mesh_of(a, I, 0);
+            const double* y0 = y_of(a, I, 0);
+            for (int k = lane_id(); k < I.N; k += 32) a.host_mesh[start + k] = m0[k];
+            for (int k = lane_id(); k < I.N * M; k += 32) a.host_y[start * M + k] = y0[k];
+            if (a.want_stages && a.host_K) {
+                for (int k = lane_id(); k < (I.N - 1) * S * M; k += 32)
+                    a.host_K[start * S * M + k] = a.K[I.nb * S * M + k];
+                for (int k = lane_id(); k < (I.N - 1) * NSXA * M; k += 32)
+                    a.host_KI[start * NSXA * M + k] = a.KI[I.nb * NSXA * M + k];
+            }
+        }
+        if (lane_id() == 0) {
+            a.host_start[I.q] = fits ? (long long)start : -1;
+            a.host_st[I.q] = s;
+        }
+    }
     __syncwarp();
 }
 

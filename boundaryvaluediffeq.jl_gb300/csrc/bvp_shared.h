@@ -67,6 +67,16 @@ struct BvpArgs {
     double* scr;                   // per-instance scratch, SCRW doubles each
     int* iscr;                     // per-instance int scratch, ISCRW ints each
     BvpInstState* st;
+    // results straight to pinned host memory the device maps (null: results stay on the device):
+    // each instance takes host_cap-bounded room from out_cursor when it finishes
+    double* host_mesh;
+    double* host_y;
+    double* host_K;
+    double* host_KI;
+    bvp_i64* host_start;           // per instance: first point of its results, -1 when it did not fit
+    BvpInstState* host_st;
+    unsigned long long* out_cursor;
+    bvp_i64 host_cap;              // points the host arrays hold
 };
 
 // Scratch layout as a function of (M, order, BC evaluation points, two-point).

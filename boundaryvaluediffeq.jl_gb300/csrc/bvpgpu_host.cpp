@@ -382,13 +382,20 @@ static int fused_grid(bvp_handle* h, int n) {
 }
 
 // Launches prep + conversion + fused solve on the handle's stream.
+static bvp_status prepare_host_outputs(bvp_handle* h, int n, long long pts_guess, BvpArgs& a);
+
 static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode, const double* d_params,
                                const int* d_n_init, const double* d_tspans, const double* d_y0,
-                               const long long* d_y0_off, const float* d_grid = nullptr, int n_grid = 0) {
+                               const long long* d_y0_off, const float* d_grid = nullptr, int n_grid = 0,
+                               long long host_pts = 0) {
     BvpArgs a;
     fill_args(h, a, n, tot, y0_mode, d_params, d_n_init, d_tspans, d_y0, d_y0_off);
     a.y0_grid = d_grid;
     a.n_grid = n_grid;
+    if (host_pts > 0) {
+        bvp_status s = prepare_host_outputs(h, n, host_pts, a);
+        if (s != BVP_OK) return s;
+    }
     CU(cudaEventRecord(h->ev[0], h->stream));
     {
         long long np = (long long)n * h->desc.n_params;
@@ -515,6 +522,70 @@ static bvp_status finish(bvp_handle* h, bvp_results* out) {
     return BVP_OK;
 }
 
+// Host outputs for a solve whose kernel writes its results to pinned host memory as each
+// instance finishes (the host calls: bvp_solve_batch, bvp_solve_batch_warm). pts_guess sizes
+// the arrays on first use; later calls keep the largest size seen.
+static bvp_status prepare_host_outputs(bvp_handle* h, int n, long long pts_guess, BvpArgs& a) {
+    if (!ensure_host(h->h_st, size_t(n) * sizeof(BvpInstState)) || !ensure_host(h->h_off, size_t(n + 1) * 8) ||
+        !ensure_dev(h->d_out_off, size_t(n + 1) * 8))
+        return fail(h, BVP_ERR_NOMEM, "pinned allocation failed");
+    if (h->out_cap < pts_guess) {
+        bvp_status s = grow_outputs(h, pts_guess + pts_guess / 4);
+        if (s != BVP_OK) return s;
+    }
+    const bool stages = h->opt.want_stages != 0;
+    a.host_mesh = dev_view_d(h->h_mesh.p);
+    a.host_y = dev_view_d(h->h_y.p);
+    a.host_K = stages ? dev_view_d(h->h_K.p) : nullptr;
+    a.host_KI = stages ? dev_view_d(h->h_KI.p) : nullptr;
+    a.host_start = static_cast<bvp_i64*>(dev_view_raw(h->h_off.p));
+    a.host_st = static_cast<BvpInstState*>(dev_view_raw(h->h_st.p));
+    a.out_cursor = reinterpret_cast<unsigned long long*>(static_cast<char*>(h->d_counter.p) + 8);
+    a.host_cap = h->out_cap;
+    if (!a.host_mesh || !a.host_y || !a.host_start || !a.host_st || (stages && (!a.host_K || !a.host_KI)))
+        return fail(h, BVP_ERR_CUDA, "host output not mapped");
+    CU(cudaMemsetAsync(a.out_cursor, 0, 8, h->stream));
+    return BVP_OK;
+}
+
+// Completes a solve launched with host outputs: one synchronisation; the offsets are the
+// instances' starts (completion order) and offsets[n] the total. Instances that did not fit
+// are packed again, in instance order, after the arrays grow.
+static bvp_status finish_host(bvp_handle* h, bvp_results* out) {
+    const int n = h->last_n;
+    CU(cudaStreamSynchronize(h->stream));
+    const BvpInstState* st = static_cast<const BvpInstState*>(h->h_st.p);
+    int64_t* off = static_cast<int64_t*>(h->h_off.p);
+    long long total = 0;
+    bool overflow = false;
+    for (int q = 0; q < n; ++q) {
+        total += st[q].N;
+        overflow |= off[q] < 0;
+    }
+    if (overflow) return finish(h, out);
+    off[n] = total;
+    float ms0 = 0, ms1 = 0;
+    cudaEventElapsedTime(&ms0, h->ev[0], h->ev[2]);
+    cudaEventElapsedTime(&ms1, h->ev[1], h->ev[2]);
+    h->timing_ms[0] = ms0;
+    h->timing_ms[1] = ms1;
+    h->st.assign(st, st + n);
+    h->offsets.assign(off, off + n + 1);
+    if (out) {
+        for (int q = 0; q < n; ++q) {
+            if (out->retcode) out->retcode[q] = st[q].retcode;
+            if (out->n_nodes) out->n_nodes[q] = st[q].N;
+            if (out->newton_iters) out->newton_iters[q] = st[q].newton_iters;
+            if (out->rounds) out->rounds[q] = st[q].rounds;
+            if (out->defect) out->defect[q] = st[q].defect;
+            if (out->resid) out->resid[q] = st[q].resid;
+        }
+    }
+    h->have_results = true;
+    h->pending_device = false;
+    return BVP_OK;
+}
+
 bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const int32_t* n_intervals,
                            const double* tspans, int32_t y0_mode, const double* y0, bvp_results* out) {
     if (!h) return BVP_ERR_INVALID;
@@ -522,11 +593,12 @@ bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const
         (y0_mode != 0 && y0_mode != 1))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
     const int M = h->L.M;
-    long long tot = 0, y0_vals = 0;
+    long long tot = 0, y0_vals = 0, pts = 0;
     for (int q = 0; q < n; ++q) {
         const int ni = n_intervals[q];
         if (ni < 1) return fail(h, BVP_ERR_INVALID, "n_intervals must be >= 1");
         if (!(tspans[2 * q + 1] > tspans[2 * q])) return fail(h, BVP_ERR_INVALID, "tspan must satisfy t0 < t1");
+        pts += ni + 1;
         tot += std::max(ni, h->opt.max_subintervals) + 1;
         y0_vals += (y0_mode == 1) ? (long long)(ni + 1) * M : M;
     }
@@ -555,9 +627,10 @@ bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const
     if (y0_mode == 1) CU(cudaMemcpyAsync(h->d_y0_off.p, yoff, b_off, cudaMemcpyHostToDevice, h->stream));
     s = launch_solve(h, n, tot, y0_mode, static_cast<const double*>(h->d_params.p),
                      static_cast<const int*>(h->d_n_init.p), static_cast<const double*>(h->d_tspans.p),
-                     static_cast<const double*>(h->d_y0.p), static_cast<const long long*>(h->d_y0_off.p));
+                     static_cast<const double*>(h->d_y0.p), static_cast<const long long*>(h->d_y0_off.p), nullptr,
+                     0, pts);
     if (s != BVP_OK) return s;
-    return finish(h, out);
+    return finish_host(h, out);
 }
 
 bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t n_features, const float* features,
@@ -569,11 +642,12 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
     if (!net || n < 1 || n_features < 1 || !features || n_grid < 2 || !n_intervals || !tspans || !y0_plain ||
         (h->desc.n_params > 0 && !params))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
-    long long tot = 0, y0_vals = 0;
+    long long tot = 0, y0_vals = 0, pts = 0;
     for (int q = 0; q < n; ++q) {
         const int ni = n_intervals[q];
         if (ni < 1) return fail(h, BVP_ERR_INVALID, "n_intervals must be >= 1");
         if (!(tspans[2 * q + 1] > tspans[2 * q])) return fail(h, BVP_ERR_INVALID, "tspan must satisfy t0 < t1");
+        pts += ni + 1;
         tot += std::max(ni, h->opt.max_subintervals) + 1;
         y0_vals += (long long)(ni + 1) * M;
     }
@@ -603,9 +677,10 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
     // the solve resamples the grid guesses onto the initial meshes itself (y0_mode 2)
     s = launch_solve(h, n, tot, 2, static_cast<const double*>(h->d_params.p), static_cast<const int*>(h->d_n_init.p),
                      static_cast<const double*>(h->d_tspans.p), static_cast<const double*>(h->d_y0.p),
-                     static_cast<const long long*>(h->d_y0_off.p), static_cast<const float*>(h->d_grid.p), n_grid);
+                     static_cast<const long long*>(h->d_y0_off.p), static_cast<const float*>(h->d_grid.p), n_grid,
+                     pts);
     if (s != BVP_OK) return s;
-    s = finish(h, nullptr);
+    s = finish_host(h, nullptr);
     if (s != BVP_OK) return s;
     // plain-guess fallback for the instances the warm start did not bring to convergence
     std::vector<int> bad;
@@ -774,7 +849,7 @@ bvp_status bvp_get_solution(bvp_handle* h, int32_t inst, double* mesh, double* y
     if (!h->have_results) return fail(h, BVP_ERR_STATE, "no results");
     if (inst < 0 || inst >= h->last_n) return fail(h, BVP_ERR_INVALID, "instance out of range");
     const int64_t o = h->offsets[inst];
-    const int N = int(h->offsets[inst + 1] - o);
+    const int N = h->st[inst].N;
     if (n_nodes) *n_nodes = N;
     if (cap < N) return fail(h, BVP_ERR_INVALID, "capacity too small");
     const int M = h->L.M;

@@ -33,7 +33,7 @@ class BatchResult:
     rounds: np.ndarray
     defect: np.ndarray
     resid: np.ndarray
-    offsets: np.ndarray          # packed layout: instance i at [offsets[i], offsets[i+1])
+    offsets: np.ndarray          # packed layout: instance i at [offsets[i], offsets[i] + n_nodes[i])
     mesh_packed: np.ndarray
     y_packed: np.ndarray         # (total, M)
     K_packed: np.ndarray | None = None
@@ -54,16 +54,19 @@ class BatchResult:
         nmax = int(self.n_nodes.max())
         out = np.full((n, nmax) + packed.shape[1:], np.nan)
         for i in range(n):
-            a, b = self.offsets[i], self.offsets[i + 1]
-            out[i, : b - a] = packed[a:b]
+            a = self.offsets[i]
+            k = int(self.n_nodes[i])
+            out[i, :k] = packed[a:a + k]
         return out
 
     def solution(self, i):
-        a, b = self.offsets[i], self.offsets[i + 1]
+        a = self.offsets[i]
+        b = a + int(self.n_nodes[i])
         return self.mesh_packed[a:b], self.y_packed[a:b]
 
     def stages(self, i):
-        a, b = self.offsets[i], self.offsets[i + 1]
+        a = self.offsets[i]
+        b = a + int(self.n_nodes[i])
         return self.K_packed[a:b - 1], self.KI_packed[a:b - 1]
 
 

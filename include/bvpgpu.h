@@ -132,9 +132,11 @@ bvp_status bvp_get_solution(bvp_handle* h, int32_t inst, double* mesh, double* y
                             int32_t* n_nodes);
 
 /* Pointers to the packed results of the last batch (valid until the next solve):
- * instance i occupies points offsets[i] .. offsets[i+1]-1 of mesh / y (x M); with
- * want_stages, K (s x M per interval) and KI (extra stages x M per interval) use the same
- * offsets (interval i of instance q at offsets[q] + i). */
+ * instance i occupies points offsets[i] .. offsets[i] + n_nodes[i] - 1 of mesh / y (x M),
+ * offsets[n_inst] is the total; with want_stages, K (s x M per interval) and KI (extra
+ * stages x M per interval) use the same offsets (interval k of instance q at offsets[q] + k).
+ * The host calls write each instance's results as it finishes, so the instances' ranges
+ * are in completion order, not instance order. */
 bvp_status bvp_get_packed(bvp_handle* h, const int64_t** offsets, const double** mesh,
                           const double** y, const double** K, const double** KI);
 
