@@ -221,12 +221,13 @@ int grid1d(long long n) { return int(std::min<long long>((n + 255) / 256, 4096))
 
 // ---- fused inference: every layer of the network in one kernel --------------------------
 // A CTA takes FR rows of the batch through all layers: the activations stay in shared
-// memory (BF16, two buffers used in turn), each warp computes 8-column tiles of the layer
-// output with mma.m16n8k16 (FP32 accumulation over k16 steps in order, as gemm_bf16 does),
-// reading the weights from a transposed BF16 copy [N][Kp] (k contiguous: the B-fragment
-// pairs are single 32-bit loads, L1/L2-resident across CTAs). The epilogue adds the bias and
-// applies GELU (hidden layers) or the output de-normalisation (last layer), with the same
-// operations as k_bias_act, so the result equals the layer-by-layer forward.
+// memory (BF16, two buffers used in turn); each layer's weights, kept in a transposed BF16
+// copy [N][Kp] (k contiguous), are staged into shared memory with 16-byte loads (rows padded
+// by 8 elements: the B-fragment reads are bank-conflict free), and each warp computes
+// 8-column tiles of the layer output with mma.m16n8k16 (FP32 accumulation over k16 steps in
+// order, as gemm_bf16 does). The epilogue adds the bias and applies GELU (hidden layers) or
+// the output de-normalisation (last layer), with the same operations as k_bias_act, so the
+// result equals the layer-by-layer forward.
 constexpr int FR = 32;            // rows per CTA
 constexpr int FWMAX = 256;        // widest layer the fused kernel takes
 constexpr int FLD = FWMAX + 8;    // shared row stride (bf16): conflict-free fragment loads
@@ -255,10 +256,15 @@ __global__ void k_build_wt(int L, FusedNet fn, const long long* offW, const bf16
     }
 }
 
+constexpr int FWLD = FWMAX + 8;   // staged weight row stride (bf16)
+constexpr size_t FUSED_SMEM = size_t(2) * FR * FLD * 2 + size_t(FWMAX) * FWLD * 2;
+
 __global__ void __launch_bounds__(128) k_mlp_forward_fused(const FusedNet fn, int B, const float* __restrict__ x,
                                                            const bf16* __restrict__ wt, const float* __restrict__ p,
                                                            const float* __restrict__ nrm, float* __restrict__ y) {
-    __shared__ __align__(16) bf16 act[2][FR][FLD];
+    extern __shared__ __align__(16) unsigned char fsm[];
+    bf16 (*act)[FR][FLD] = reinterpret_cast<bf16 (*)[FR][FLD]>(fsm);
+    bf16* wsm = reinterpret_cast<bf16*>(fsm + size_t(2) * FR * FLD * 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int g = lane >> 2, t = lane & 3;
     const int r0 = blockIdx.x * FR;
@@ -277,7 +283,21 @@ __global__ void __launch_bounds__(128) k_mlp_forward_fused(const FusedNet fn, in
     for (int l = 0; l < fn.L; ++l) {
         const int K = fn.kp[l], N = fn.w[l + 1];
         const int ntiles = N / 8;
-        const bf16* W = wt + fn.offWt[l];
+        const int WLD = K + 8;
+        {
+            // stage the layer's [N][K] weights with asynchronous 16-byte copies, all in flight
+            // at once (rows 16-byte aligned: K is a multiple of 16)
+            const bf16* src = wt + fn.offWt[l];
+            const int per_row = K / 8;
+            for (int e = tid; e < N * per_row; e += 128) {
+                const int nn = e / per_row, c = e - nn * per_row;
+                const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(wsm + nn * WLD + c * 8));
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src + size_t(e) * 8));
+            }
+            asm volatile("cp.async.wait_all;\n" ::: "memory");
+        }
+        __syncthreads();
+        const bf16* W = wsm;
         float acc[FQ][2][4];
 #pragma unroll
         for (int q = 0; q < FQ; ++q)
@@ -299,7 +319,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_fused(const FusedNet fn, in
             for (int q = 0; q < FQ; ++q) {
                 const int j = warp + 4 * q;
                 if (j < ntiles) {
-                    const bf16* wr = W + (long long)(j * 8 + g) * K + k0 + 2 * t;
+                    const bf16* wr = W + (j * 8 + g) * WLD + k0 + 2 * t;
                     uint32_t bfr[2];
                     bfr[0] = *reinterpret_cast<const uint32_t*>(wr);
                     bfr[1] = *reinterpret_cast<const uint32_t*>(wr + 8);
@@ -445,7 +465,7 @@ void refresh_wt(bvp_mlp* n) {
 // inference on device pointers: the fused kernel when the network fits it, else layer by layer
 void infer(bvp_mlp* n, int B, const float* d_x, float* d_y, cudaStream_t s) {
     if (n->fused) {
-        k_mlp_forward_fused<<<(B + FR - 1) / FR, 128, 0, s>>>(n->fn, B, d_x, n->d_wt, n->d_p, n->d_norm, d_y);
+        k_mlp_forward_fused<<<(B + FR - 1) / FR, 128, FUSED_SMEM, s>>>(n->fn, B, d_x, n->d_wt, n->d_p, n->d_norm, d_y);
     } else {
         cudaStream_t prev = n->stream;
         n->stream = s;
@@ -495,7 +515,9 @@ bvp_status bvp_mlp_create(int32_t n_layers, const int32_t* widths, bvp_mlp** out
             ot += (long long)n->w[l + 1] * f.kp[l];
             f.offb[l] = n->offb[l];
         }
-        ok = cudaMalloc(&n->d_wt, ot * 2) == cudaSuccess && cudaMalloc(&n->d_offW, n_layers * 8) == cudaSuccess &&
+        ok = cudaFuncSetAttribute(k_mlp_forward_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FUSED_SMEM)) ==
+                 cudaSuccess &&
+             cudaMalloc(&n->d_wt, ot * 2) == cudaSuccess && cudaMalloc(&n->d_offW, n_layers * 8) == cudaSuccess &&
              cudaMemcpy(n->d_offW, n->offW.data(), n_layers * 8, cudaMemcpyHostToDevice) == cudaSuccess;
         if (!ok) { n->err = "allocation failed"; return BVP_ERR_CUDA; }
     }
