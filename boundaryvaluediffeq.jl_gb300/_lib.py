@@ -21,7 +21,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD = os.path.join(PKG_DIR, "_build")
 INCLUDE = os.path.join(os.path.dirname(PKG_DIR), "include")
 LIB_PATH = os.path.join(BUILD, "libbvpgpu.so")
-EMBED = ("bvp_prelude.cuh", "bvp_kernels.cuh", "bvp_shared.h", "bvp_tableau.cuh")
+EMBED = ("bvp_prelude.cuh", "bvp_kernels.cuh", "bvp_large.cuh", "bvp_shared.h", "bvp_tableau.cuh")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
@@ -79,7 +79,8 @@ def _run(cmd, log=None):
 
 def device_check_source(problem) -> str:
     """A translation unit with the problem inlined, for the nvcc sm_103a build check."""
-    return ("#include \"bvp_prelude.cuh\"\n" + problem.source + "\n#include \"bvp_kernels.cuh\"\n")
+    kernels = "bvp_large.cuh" if problem.M > 8 else "bvp_kernels.cuh"
+    return ("#include \"bvp_prelude.cuh\"\n" + problem.source + f"\n#include \"{kernels}\"\n")
 
 
 def build_library(verbose: bool = False, force: bool = False, check_problems=None) -> str:
@@ -99,7 +100,7 @@ def build_library(verbose: bool = False, force: bool = False, check_problems=Non
                     os.path.join(CSRC, "bvp_mlp.cu"), "-o", tmp, "-lnvrtc", "-ldl"]
         jobs.append(subprocess.Popen(host_cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
         checks = check_problems if check_problems is not None else [
-            (P.PENDULUM, 4, 0), (P.SINGULAR_PERTURBATION, 6, 0)]
+            (P.PENDULUM, 4, 0), (P.SINGULAR_PERTURBATION, 6, 0), (P.NONLINEAR32, 4, 0)]
         check_cmds = []
         for prob, order, nbc_dummy in checks:
             src = os.path.join(BUILD, f"check_{prob.name}_o{order}.cu")

@@ -79,6 +79,43 @@ struct BvpArgs {
     bvp_i64 host_cap;              // points the host arrays hold
 };
 
+// Launch arguments of the larger-state kernels (M > 8, bvp_large.cuh): one instance per CTA or
+// per grid row, the Newton and mesh rounds driven from the host.
+struct BvpLargeArgs {
+    int n_inst, n_params, n_active;
+    double alpha;                  // bl_update: y = ybase + alpha delta (alpha 0: y += delta)
+    const int* active;             // instance ids taking part in this launch
+    const double* params;
+    const BVP_JT_PTR* params_j;
+    const bvp_i64* node_off;
+    const int* N;                  // current point count per instance
+    double* mesh;                  // [2][tot]: current mesh in buffer 0, a new one in buffer 1
+    double* h;                     // [2][tot]
+    double* y;                     // [2][tot][M]
+    double* ybase;                 // [tot][M]
+    double* ybak;                  // [tot][M]
+    double* K;                     // [tot][S][M]
+    double* KI;                    // [tot][NSXA][M]
+    double* F;                     // [tot][M]
+    double* err;                   // [tot]
+    double* inc;                   // [tot][M]
+    int* iold;                     // [tot]
+    double* bcres;                 // [n_inst][M]: La rows at t0, then Lb rows at t1
+    BVP_JT_PTR* yj;                // [tot][M]
+    BVP_JT_PTR* Sb;                // [tot][M][M]
+    BVP_JT_PTR* Rb;                // [tot][M][M]
+    BVP_JT_PTR* G;                 // [n_inst][2][M][M]: dbca/dy0 (rows 0..La-1), dbcb/dyN (rows La..M-1)
+    BVP_JT_PTR* rec;               // [tot][3M^2 + M]
+    BVP_JT_PTR* delta;             // [tot][M]
+    unsigned long long* norm;      // [n_inst]: max |F| as the bits of a non-negative double
+    double* sq;                    // [n_inst]: sum of F^2
+    unsigned long long* dnorm;     // [n_inst]: defect norm bits
+    int* bad;                      // [n_inst]: singular block in the last solve
+    bvp_i64 tot;
+    int transfer_inplace;
+    const int* newN;               // bl_transfer: point count of the new mesh (buffer 1)
+};
+
 // Scratch layout as a function of (M, order, BC evaluation points, two-point).
 struct BvpLayout {
     int M, S, SS, NSX, NSXA, EQW, RECW, NBCB, KMAX, NDENSE;

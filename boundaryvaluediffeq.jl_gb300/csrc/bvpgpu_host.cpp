@@ -18,6 +18,8 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <cmath>
+#include <map>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -54,6 +56,13 @@ struct bvp_handle_s {
     cudaKernel_t k_fused = nullptr, k_stage = nullptr, k_pack = nullptr, k_probe = nullptr, k_offsets = nullptr,
                  k_convert = nullptr, k_prep = nullptr, k_dense = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    // larger-state path (M > 8, bvp_large.cuh)
+    bool large = false;
+    cudaKernel_t kl_res = nullptr, kl_jac = nullptr, kl_solve = nullptr, kl_update = nullptr, kl_copy = nullptr,
+                 kl_defect = nullptr, kl_transfer = nullptr, kl_convert = nullptr, kl_probe = nullptr;
+    int l_threads = 256;     // bl_linsolve block size (8 warps; 4 with FP64 blocks)
+    size_t l_smem = 0;
+    DevBuf d_bcres, d_G, d_lnorm, d_lsq, d_ldnorm, d_lbad, d_active, d_N, d_newN;
     // device arrays
     DevBuf d_mesh, d_h, d_y, d_ybak, d_ybase, d_K, d_KI, d_F, d_err, d_inc, d_iold, d_Sb, d_Rb,
         d_rec, d_tj, d_hj, d_delta, d_yj, d_Fj, d_scr, d_iscr, d_st, d_order, d_cap, d_node_off, d_counter,
@@ -192,8 +201,9 @@ static bvp_status compile_and_load(bvp_handle* h) {
         "-DBVP_LA=" + std::to_string(d.twopoint ? d.La : 0),
         std::string("-DBVP_JT=") + (o.jac_precision == 64 ? "double" : "float"),
     };
+    const bool large = d.M > 8;
     const std::string src = std::string("#include \"bvp_prelude.cuh\"\n#line 1 \"problem_source\"\n") +
-                            h->source + "\n#include \"bvp_kernels.cuh\"\n";
+                            h->source + (large ? "\n#include \"bvp_large.cuh\"\n" : "\n#include \"bvp_kernels.cuh\"\n");
     uint64_t key = fnv1a(kEmbedHash, std::strlen(kEmbedHash));
     key = fnv1a(src.data(), src.size(), key);
     for (auto& s : opts) key = fnv1a(s.data(), s.size() + 1, key);
@@ -225,6 +235,19 @@ static bvp_status compile_and_load(bvp_handle* h) {
         write_file_atomic(path, cubin);
     }
     CU(cudaLibraryLoadData(&h->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+    if (large) {
+        h->large = true;
+        CU(cudaLibraryGetKernel(&h->kl_res, h->lib, "bl_residual"));
+        CU(cudaLibraryGetKernel(&h->kl_jac, h->lib, "bl_jacobian"));
+        CU(cudaLibraryGetKernel(&h->kl_solve, h->lib, "bl_linsolve"));
+        CU(cudaLibraryGetKernel(&h->kl_update, h->lib, "bl_update"));
+        CU(cudaLibraryGetKernel(&h->kl_copy, h->lib, "bl_copy"));
+        CU(cudaLibraryGetKernel(&h->kl_defect, h->lib, "bl_defect"));
+        CU(cudaLibraryGetKernel(&h->kl_transfer, h->lib, "bl_transfer"));
+        CU(cudaLibraryGetKernel(&h->kl_convert, h->lib, "bl_convert_params"));
+        CU(cudaLibraryGetKernel(&h->kl_probe, h->lib, "bl_layout_probe"));
+        return BVP_OK;
+    }
     CU(cudaLibraryGetKernel(&h->k_fused, h->lib, "bvp_solve_fused"));
     CU(cudaLibraryGetKernel(&h->k_stage, h->lib, "bvp_stage"));
     CU(cudaLibraryGetKernel(&h->k_pack, h->lib, "bvp_pack"));
@@ -248,7 +271,8 @@ bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bv
     const bvp_problem_desc& d = h->desc;
     const bvp_options& o = h->opt;
     std::string why;
-    if (d.M < 1 || d.M > 8) why = "M must be in 1..8";
+    if (d.M < 1 || d.M > 32) why = "M must be in 1..32";
+    else if (d.M > 8 && !d.twopoint) why = "M > 8 takes two-point boundary conditions";
     else if (d.n_params < 0) why = "n_params must be >= 0";
     else if (!d.twopoint && (d.n_bc_pts < 1 || d.n_bc_pts > 16)) why = "n_bc_pts must be in 1..16";
     else if (d.twopoint && (d.La < 0 || d.Lb < 0 || d.La + d.Lb != d.M)) why = "La + Lb must equal M";
@@ -272,6 +296,24 @@ bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bv
     bvp_status s = compile_and_load(h);
     *out = h;
     if (s != BVP_OK) return s;
+    if (h->large) {
+        // host/device launch ABI of the larger-state kernels, and their shared memory
+        DevBuf probe;
+        if (!ensure_dev(probe, 16 * sizeof(int))) return fail(h, BVP_ERR_NOMEM, "probe alloc");
+        int* pp = static_cast<int*>(probe.p);
+        void* args[] = {&pp};
+        CU(cudaLaunchKernel((const void*)h->kl_probe, dim3(1), dim3(1), args, 0, h->stream));
+        int got[16] = {0};
+        CU(cudaMemcpyAsync(got, probe.p, sizeof(got), cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaStreamSynchronize(h->stream));
+        cudaFree(probe.p);
+        if (got[0] != int(sizeof(BvpLargeArgs)) || got[1] != h->L.RECW || got[4] != h->L.S || got[5] != h->L.NSXA)
+            return fail(h, BVP_ERR_STATE, "host/device layout mismatch (larger-state kernels)");
+        h->l_threads = h->js == 8 ? 128 : 256;
+        h->l_smem = size_t(h->l_threads / 32) * size_t(2 * d.M) * size_t(got[2]) * size_t(h->js);
+        CU(cudaFuncSetAttribute((const void*)h->kl_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, int(h->l_smem)));
+        return BVP_OK;
+    }
     // check that host and device agree on the launch ABI
     DevBuf probe;
     if (!ensure_dev(probe, 16 * sizeof(int))) return fail(h, BVP_ERR_NOMEM, "probe alloc");
@@ -586,12 +628,507 @@ static bvp_status finish_host(bvp_handle* h, bvp_results* out) {
     return BVP_OK;
 }
 
+// ---- larger-state path (M > 8): the bl_* kernels, Newton and mesh rounds driven here --------
+// The per-instance control flow is the one the fused kernel runs (solve_instance /
+// newton_attempt with the FP64 residual throughout): Newton on ||F||_inf <= abstol with the
+// stall and divergence tests, a backtracking retry from the same start, the defect, the
+// mesh selection (sequential per instance: here), the transfer and the halving restart.
+namespace {
+struct LargeInst {
+    int N = 0, cap = 0;
+    long long off = 0;
+    std::vector<double> mesh, h;
+    int rounds = 0, retcode = BVP_RET_FAILURE, flags = 0, newton_total = 0;
+    bool done = false;
+    double defect = 0.0, resid = 0.0;
+    // Newton attempt state
+    int attempt = 0, iters = 0, why = 0, stall = 0, ls = 0, status = 0;  // status 0 running, 1 ok, 2 failed
+    double nrm0 = 0, best = 0, f0 = 0, alpha = 1, sq = 0;
+};
+enum { LR_START = 0, LR_STEP = 1, LR_TRIAL = 2 };
+double bits_to_double(unsigned long long b) {
+    double v;
+    std::memcpy(&v, &b, 8);
+    return v;
+}
+}  // namespace
+
+static bvp_status large_run(bvp_handle* h, cudaKernel_t k, dim3 grid, dim3 block, size_t smem, BvpLargeArgs& a,
+                            int* mode = nullptr) {
+    void* args1[] = {&a};
+    void* args2[] = {&a, mode};
+    CU(cudaLaunchKernel((const void*)k, grid, block, mode ? args2 : args1, smem, h->stream));
+    return BVP_OK;
+}
+
+// uploads the active list and returns the grid rows
+static bvp_status large_active(bvp_handle* h, BvpLargeArgs& a, const std::vector<int>& ids) {
+    a.n_active = int(ids.size());
+    if (ids.empty()) return BVP_OK;
+    CU(cudaMemcpyAsync(h->d_active.p, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    return BVP_OK;
+}
+
+static bvp_status large_per_node(bvp_handle* h, BvpLargeArgs& a, cudaKernel_t k, int maxN, int mode = -1) {
+    if (a.n_active == 0) return BVP_OK;
+    const int M = h->L.M;
+    dim3 grid(unsigned((maxN * M + 255) / 256), unsigned(a.n_active));
+    return large_run(h, k, grid, dim3(256), 0, a, mode >= 0 ? &mode : nullptr);
+}
+
+static bvp_status solve_large(bvp_handle* h, int n, const double* params, const int32_t* n_intervals,
+                              const double* tspans, int y0_mode, const double* y0, bvp_results* out) {
+    const int M = h->L.M, P = h->desc.n_params;
+    const bvp_options& o = h->opt;
+    std::vector<LargeInst> I(n);
+    long long tot = 0;
+    for (int q = 0; q < n; ++q) {
+        const int ni = n_intervals[q];
+        if (ni < 1) return fail(h, BVP_ERR_INVALID, "n_intervals must be >= 1");
+        if (!(tspans[2 * q + 1] > tspans[2 * q])) return fail(h, BVP_ERR_INVALID, "tspan must satisfy t0 < t1");
+        I[q].cap = std::max(ni, o.max_subintervals) + 1;
+        I[q].off = tot;
+        tot += I[q].cap;
+    }
+    bvp_status s = ensure_arena(h, tot, n, 1);
+    if (s != BVP_OK) return s;
+    const int js = h->js;
+    if (!ensure_dev(h->d_bcres, size_t(n) * M * 8) || !ensure_dev(h->d_G, size_t(n) * 2 * M * M * js) ||
+        !ensure_dev(h->d_lnorm, size_t(n) * 8) || !ensure_dev(h->d_lsq, size_t(n) * 8) ||
+        !ensure_dev(h->d_ldnorm, size_t(n) * 8) || !ensure_dev(h->d_lbad, size_t(n) * 4) ||
+        !ensure_dev(h->d_active, size_t(n) * 4) || !ensure_dev(h->d_N, size_t(n) * 4) ||
+        !ensure_dev(h->d_newN, size_t(n) * 4))
+        return fail(h, BVP_ERR_NOMEM, "device allocation failed");
+    // inputs, meshes, initial guesses
+    std::vector<long long> offs(n);
+    std::vector<int> Ns(n);
+    if (P) CU(cudaMemcpyAsync(h->d_params.p, params, size_t(n) * P * 8, cudaMemcpyHostToDevice, h->stream));
+    {
+        long long np = (long long)n * P;
+        const double* src = static_cast<const double*>(h->d_params.p);
+        void* dst = h->d_params_j.p;
+        void* args[] = {&src, &dst, &np};
+        if (np) CU(cudaLaunchKernel((const void*)h->kl_convert, dim3(256), dim3(256), args, 0, h->stream));
+    }
+    std::vector<double> ybuf;
+    long long yoff = 0;
+    for (int q = 0; q < n; ++q) {
+        LargeInst& L = I[q];
+        const int ni = n_intervals[q];
+        const double t0 = tspans[2 * q], t1 = tspans[2 * q + 1];
+        const double hh = (t1 - t0) / ni;   // range(t0; stop = t1, length = n + 1) (Core/utils.jl:694-700)
+        L.N = ni + 1;
+        L.mesh.resize(ni + 1);
+        L.h.resize(ni);
+        for (int i = 0; i <= ni; ++i) L.mesh[i] = (i == ni) ? t1 : std::fma(double(i), hh, t0);
+        for (int i = 0; i < ni; ++i) L.h[i] = L.mesh[i + 1] - L.mesh[i];
+        ybuf.assign(size_t(L.N) * M, 0.0);
+        if (y0_mode == 0) {
+            for (int i = 0; i < L.N; ++i)
+                for (int m = 0; m < M; ++m) ybuf[size_t(i) * M + m] = y0[size_t(q) * M + m];
+        } else {
+            std::memcpy(ybuf.data(), y0 + yoff * M, ybuf.size() * 8);
+            yoff += L.N;
+        }
+        CU(cudaMemcpy(static_cast<double*>(h->d_mesh.p) + L.off, L.mesh.data(), size_t(L.N) * 8, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(static_cast<double*>(h->d_h.p) + L.off, L.h.data(), size_t(L.N - 1) * 8, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(static_cast<double*>(h->d_y.p) + L.off * M, ybuf.data(), ybuf.size() * 8, cudaMemcpyHostToDevice));
+        offs[q] = L.off;
+        Ns[q] = L.N;
+    }
+    CU(cudaMemcpyAsync(h->d_node_off.p, offs.data(), size_t(n) * 8, cudaMemcpyHostToDevice, h->stream));
+    BvpLargeArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n_inst = n;
+    a.n_params = P;
+    a.active = static_cast<const int*>(h->d_active.p);
+    a.params = static_cast<const double*>(h->d_params.p);
+    a.params_j = h->d_params_j.p;
+    a.node_off = static_cast<const bvp_i64*>(h->d_node_off.p);
+    a.N = static_cast<const int*>(h->d_N.p);
+    a.mesh = static_cast<double*>(h->d_mesh.p);
+    a.h = static_cast<double*>(h->d_h.p);
+    a.y = static_cast<double*>(h->d_y.p);
+    a.ybase = static_cast<double*>(h->d_ybase.p);
+    a.ybak = static_cast<double*>(h->d_ybak.p);
+    a.K = static_cast<double*>(h->d_K.p);
+    a.KI = static_cast<double*>(h->d_KI.p);
+    a.F = static_cast<double*>(h->d_F.p);
+    a.err = static_cast<double*>(h->d_err.p);
+    a.inc = static_cast<double*>(h->d_inc.p);
+    a.iold = static_cast<int*>(h->d_iold.p);
+    a.bcres = static_cast<double*>(h->d_bcres.p);
+    a.yj = h->d_yj.p;
+    a.Sb = h->d_Sb.p;
+    a.Rb = h->d_Rb.p;
+    a.G = h->d_G.p;
+    a.rec = h->d_rec.p;
+    a.delta = h->d_delta.p;
+    a.norm = static_cast<unsigned long long*>(h->d_lnorm.p);
+    a.sq = static_cast<double*>(h->d_lsq.p);
+    a.dnorm = static_cast<unsigned long long*>(h->d_ldnorm.p);
+    a.bad = static_cast<int*>(h->d_lbad.p);
+    a.tot = tot;
+    a.transfer_inplace = o.transfer_inplace;
+    a.newN = static_cast<const int*>(h->d_newN.p);
+    CU(cudaEventRecord(h->ev[0], h->stream));
+    CU(cudaEventRecord(h->ev[1], h->stream));
+    std::vector<unsigned long long> nb(n);
+    std::vector<double> sqv(n);
+    std::vector<int> badv(n);
+    auto upload_N = [&]() -> bvp_status {
+        for (int q = 0; q < n; ++q) Ns[q] = I[q].N;
+        CU(cudaMemcpyAsync(h->d_N.p, Ns.data(), size_t(n) * 4, cudaMemcpyHostToDevice, h->stream));
+        return BVP_OK;
+    };
+    auto maxN_of = [&](const std::vector<int>& ids) {
+        int mx = 2;
+        for (int q : ids) mx = std::max(mx, I[q].N);
+        return mx;
+    };
+    s = upload_N();
+    if (s != BVP_OK) return s;
+    for (int round = 0;; ++round) {
+        std::vector<int> act;
+        for (int q = 0; q < n; ++q)
+            if (!I[q].done) act.push_back(q);
+        if (act.empty()) break;
+        // ---- Newton (newton / newton_attempt) ----
+        for (int q : act) {
+            LargeInst& L = I[q];
+            ++L.rounds;
+            L.attempt = 0; L.iters = 0; L.why = LR_START; L.status = 0; L.stall = 0;
+        }
+        s = large_active(h, a, act);
+        if (s != BVP_OK) return s;
+        s = large_per_node(h, a, h->kl_copy, maxN_of(act), 3);   // ybak = y
+        if (s != BVP_OK) return s;
+        while (true) {
+            std::vector<int> run;
+            for (int q : act)
+                if (I[q].status == 0) run.push_back(q);
+            if (run.empty()) break;
+            // residual at every running instance's current iterate
+            s = large_active(h, a, run);
+            if (s != BVP_OK) return s;
+            CU(cudaMemsetAsync(h->d_lnorm.p, 0, size_t(n) * 8, h->stream));
+            CU(cudaMemsetAsync(h->d_lsq.p, 0, size_t(n) * 8, h->stream));
+            {
+                const int mx = maxN_of(run);
+                s = large_run(h, h->kl_res, dim3(unsigned((mx + 127) / 128), unsigned(run.size())), dim3(128), 0, a);
+                if (s != BVP_OK) return s;
+            }
+            CU(cudaMemcpyAsync(nb.data(), h->d_lnorm.p, size_t(n) * 8, cudaMemcpyDeviceToHost, h->stream));
+            CU(cudaMemcpyAsync(sqv.data(), h->d_lsq.p, size_t(n) * 8, cudaMemcpyDeviceToHost, h->stream));
+            CU(cudaStreamSynchronize(h->stream));
+            std::vector<int> step, restart;
+            std::map<double, std::vector<int>> trials;
+            auto attempt_failed = [&](LargeInst& L, int q) {
+                if (L.attempt == 0 && o.linesearch_fallback) {
+                    L.attempt = 1; L.iters = 0; L.why = LR_START; L.stall = 0;
+                    L.flags |= 1;
+                    restart.push_back(q);
+                } else {
+                    L.status = 2;
+                }
+            };
+            for (int q : run) {
+                LargeInst& L = I[q];
+                const double nrm = bits_to_double(nb[q]);
+                const double f1 = sqv[q];
+                if (L.why == LR_TRIAL) {
+                    if (!(std::isfinite(nrm) && f1 <= (1.0 - 2e-4 * L.alpha) * L.f0)) {
+                        L.alpha *= 0.5;
+                        if (++L.ls >= 20) { L.resid = nrm; attempt_failed(L, q); continue; }
+                        trials[L.alpha].push_back(q);
+                        continue;
+                    }
+                    L.why = LR_STEP;
+                }
+                L.resid = nrm;
+                L.sq = f1;
+                bool need_step = false;
+                if (L.why == LR_START) {
+                    if (!std::isfinite(nrm)) { attempt_failed(L, q); continue; }
+                    if (nrm <= o.abstol) { L.status = 1; continue; }
+                    L.nrm0 = nrm; L.best = nrm; L.stall = 0;
+                    need_step = true;
+                } else {
+                    if (!std::isfinite(nrm)) { attempt_failed(L, q); continue; }
+                    if (nrm <= o.abstol) { L.status = 1; continue; }
+                    if (nrm > o.divergence_factor * L.nrm0) { attempt_failed(L, q); continue; }
+                    if (nrm < L.best) { L.best = nrm; L.stall = 0; }
+                    else if (++L.stall >= o.stall_steps) { attempt_failed(L, q); continue; }
+                    need_step = true;
+                }
+                if (need_step) {
+                    if (L.iters >= o.max_newton) { attempt_failed(L, q); continue; }
+                    step.push_back(q);
+                }
+            }
+            // restarts of the line-search attempt from the saved start
+            if (!restart.empty()) {
+                s = large_active(h, a, restart);
+                if (s != BVP_OK) return s;
+                s = large_per_node(h, a, h->kl_copy, maxN_of(restart), 4);   // y = ybak
+                if (s != BVP_OK) return s;
+            }
+            // the line search's shorter trials (same direction, y = ybase + alpha delta)
+            for (auto& kv : trials) {
+                s = large_active(h, a, kv.second);
+                if (s != BVP_OK) return s;
+                a.alpha = kv.first;
+                s = large_per_node(h, a, h->kl_update, maxN_of(kv.second));
+                a.alpha = 0.0;
+                if (s != BVP_OK) return s;
+            }
+            if (step.empty()) continue;
+            // Newton steps: Jacobian blocks, factorisation and solve
+            s = large_active(h, a, step);
+            if (s != BVP_OK) return s;
+            {
+                const int mx = maxN_of(step);
+                const long long threads = (long long)mx * ((2 * M + 7) / 8);
+                s = large_run(h, h->kl_jac, dim3(unsigned((threads + 127) / 128), unsigned(step.size())), dim3(128), 0, a);
+                if (s != BVP_OK) return s;
+                s = large_run(h, h->kl_solve, dim3(unsigned(step.size())), dim3(unsigned(h->l_threads)), h->l_smem, a);
+                if (s != BVP_OK) return s;
+            }
+            CU(cudaMemcpyAsync(badv.data(), h->d_lbad.p, size_t(n) * 4, cudaMemcpyDeviceToHost, h->stream));
+            CU(cudaStreamSynchronize(h->stream));
+            std::vector<int> plain, ls;
+            restart.clear();
+            for (int q : step) {
+                LargeInst& L = I[q];
+                if (badv[q]) { attempt_failed(L, q); continue; }
+                ++L.iters;
+                ++L.newton_total;
+                if (L.attempt == 0) { plain.push_back(q); L.why = LR_STEP; }
+                else { ls.push_back(q); L.f0 = L.sq; L.alpha = 1.0; L.ls = 0; L.why = LR_TRIAL; }
+            }
+            if (!restart.empty()) {
+                s = large_active(h, a, restart);
+                if (s != BVP_OK) return s;
+                s = large_per_node(h, a, h->kl_copy, maxN_of(restart), 4);
+                if (s != BVP_OK) return s;
+            }
+            if (!plain.empty()) {
+                s = large_active(h, a, plain);
+                if (s != BVP_OK) return s;
+                a.alpha = 0.0;
+                s = large_per_node(h, a, h->kl_update, maxN_of(plain));
+                if (s != BVP_OK) return s;
+            }
+            if (!ls.empty()) {
+                s = large_active(h, a, ls);
+                if (s != BVP_OK) return s;
+                s = large_per_node(h, a, h->kl_copy, maxN_of(ls), 0);   // ybase = y
+                if (s != BVP_OK) return s;
+                a.alpha = 1.0;
+                s = large_per_node(h, a, h->kl_update, maxN_of(ls));
+                a.alpha = 0.0;
+                if (s != BVP_OK) return s;
+            }
+        }
+        // ---- defect of the converged instances ----
+        std::vector<int> conv;
+        for (int q : act)
+            if (I[q].status == 1) conv.push_back(q);
+        std::vector<double> dn(n, 0.0);
+        if (o.adaptive && !conv.empty()) {
+            s = large_active(h, a, conv);
+            if (s != BVP_OK) return s;
+            CU(cudaMemsetAsync(h->d_ldnorm.p, 0, size_t(n) * 8, h->stream));
+            const int mx = maxN_of(conv);
+            s = large_run(h, h->kl_defect, dim3(unsigned((mx + 127) / 128), unsigned(conv.size())), dim3(128), 0, a);
+            if (s != BVP_OK) return s;
+            CU(cudaMemcpyAsync(nb.data(), h->d_ldnorm.p, size_t(n) * 8, cudaMemcpyDeviceToHost, h->stream));
+            CU(cudaStreamSynchronize(h->stream));
+            for (int q : conv) dn[q] = bits_to_double(nb[q]);
+        }
+        // ---- outer-loop decisions (solve!, mirk.jl:286-388) ----
+        std::vector<int> refine, halve;
+        for (int q : act) {
+            LargeInst& L = I[q];
+            const bool nl_ok = L.status == 1;
+            if (!o.adaptive) { L.retcode = nl_ok ? BVP_RET_SUCCESS : BVP_RET_FAILURE; L.done = true; continue; }
+            double error_norm = 2 * o.abstol;
+            bool ok = nl_ok;
+            if (ok) {
+                error_norm = dn[q];
+                L.defect = error_norm;
+                ok = !(error_norm > o.defect_threshold) && !std::isnan(error_norm);
+            }
+            if (ok && error_norm > o.abstol) {
+                refine.push_back(q);   // continues unless the mesh selection fails (below)
+                continue;
+            }
+            int info_ok = 1;
+            if (!ok) {
+                if (2L * (L.N - 1) > o.max_subintervals || 2 * (L.N - 1) + 1 > L.cap) {
+                    info_ok = 0;
+                    if (2 * (L.N - 1) + 1 > L.cap) L.flags |= 2;
+                } else {
+                    halve.push_back(q);
+                }
+            }
+            if (!(info_ok && error_norm > o.abstol)) {
+                L.retcode = info_ok ? BVP_RET_SUCCESS : BVP_RET_FAILURE;
+                L.done = true;
+            }
+        }
+        // mesh selection (adaptivity.jl:23-75, 250-304) for the refined instances
+        std::vector<int> moved;
+        std::vector<int> newNs(n, 0);
+        for (int q : refine) {
+            LargeInst& L = I[q];
+            const int nI = L.N - 1;
+            std::vector<double> e(nI);
+            CU(cudaMemcpy(e.data(), static_cast<const double*>(h->d_err.p) + L.off, size_t(nI) * 8, cudaMemcpyDeviceToHost));
+            const double ex = 1.0 / (o.order + 1);
+            double r1 = -INFINITY, r2 = 0.0;
+            for (int i = 0; i < nI; ++i) { e[i] = std::pow(e[i] / o.abstol, ex); r1 = std::max(r1, e[i]); }
+            for (int i = 0; i < nI; ++i) r2 += e[i];
+            const double r3 = r2 / (L.N - 1);
+            long n_pred = (long)std::nearbyint(1.3 * r2 + 1);
+            const double n_ = 0.1 * nI;
+            if (std::fabs(double(n_pred - nI)) < n_) n_pred = (long)std::nearbyint(nI + n_);
+            std::vector<double> nm, nh;
+            bool ok = true;
+            if (r1 <= 1.0 * r3) {
+                if (2L * nI > o.max_subintervals || 2 * nI + 1 > L.cap) ok = false;
+                else {
+                    nm.assign(2 * nI + 1, 0.0); nh.assign(2 * nI, 0.0);
+                    for (int i = 0; i <= nI; ++i) nm[2 * i] = L.mesh[i];
+                    for (int i = 0; i < nI; ++i) {
+                        nm[2 * i + 1] = (L.mesh[i + 1] + L.mesh[i]) / 2.0;
+                        nh[2 * i] = L.h[i] / 2.0; nh[2 * i + 1] = L.h[i] / 2.0;
+                    }
+                }
+            } else {
+                const long lb = L.N / 2, ub = 4L * (L.N - 1);
+                long Nsub = std::min(std::max(n_pred, lb), ub);
+                if (Nsub > o.max_subintervals || Nsub + 1 > L.cap) ok = false;
+                else {
+                    for (int i = 0; i < nI; ++i) e[i] /= L.h[i];
+                    double tot_int = 0.0;
+                    for (int k = 0; k < nI; ++k) tot_int += e[k] * L.h[k];
+                    const double zeta = tot_int / double(Nsub);
+                    nm.assign(Nsub + 1, 0.0);
+                    nm[0] = L.mesh[0];
+                    double t = L.mesh[0], integral = 0.0;
+                    int k = 0, i = 0;
+                    long guard = 4L * (nI + Nsub) + 64;
+                    while (k < nI && --guard > 0) {
+                        const double next_piece = e[k] * (L.mesh[k + 1] - t);
+                        const double int_next = integral + next_piece;
+                        if (int_next > zeta) {
+                            const double pt = (zeta - integral) / e[k] + t;
+                            if (i + 1 < Nsub) nm[i + 1] = pt;
+                            t = pt; ++i; integral = 0.0;
+                        } else {
+                            integral = int_next; t = L.mesh[k + 1]; ++k;
+                        }
+                    }
+                    nm[Nsub] = L.mesh[nI];
+                    nh.resize(Nsub);
+                    for (int j = 0; j < Nsub; ++j) nh[j] = nm[j + 1] - nm[j];
+                }
+            }
+            if (!ok) { L.retcode = BVP_RET_FAILURE; L.done = true; continue; }
+            const int Nn = int(nm.size());
+            CU(cudaMemcpy(static_cast<double*>(h->d_mesh.p) + tot + L.off, nm.data(), size_t(Nn) * 8, cudaMemcpyHostToDevice));
+            CU(cudaMemcpy(static_cast<double*>(h->d_h.p) + tot + L.off, nh.data(), size_t(Nn - 1) * 8, cudaMemcpyHostToDevice));
+            newNs[q] = Nn;
+            moved.push_back(q);
+            L.mesh.swap(nm);
+            L.h.swap(nh);
+        }
+        if (!moved.empty()) {
+            CU(cudaMemcpyAsync(h->d_newN.p, newNs.data(), size_t(n) * 4, cudaMemcpyHostToDevice, h->stream));
+            s = large_active(h, a, moved);
+            if (s != BVP_OK) return s;
+            s = large_run(h, h->kl_transfer, dim3(unsigned((moved.size() * 32 + 127) / 128)), dim3(128), 0, a);
+            if (s != BVP_OK) return s;
+            CU(cudaStreamSynchronize(h->stream));
+            for (int q : moved) I[q].N = newNs[q];
+        }
+        // halving restart with a zero guess
+        for (int q : halve) {
+            LargeInst& L = I[q];
+            const int nI = L.N - 1;
+            std::vector<double> nm(2 * nI + 1), nh(2 * nI);
+            for (int i = 0; i <= nI; ++i) nm[2 * i] = L.mesh[i];
+            for (int i = 0; i < nI; ++i) {
+                nm[2 * i + 1] = (L.mesh[i + 1] + L.mesh[i]) / 2.0;
+                nh[2 * i] = L.h[i] / 2.0; nh[2 * i + 1] = L.h[i] / 2.0;
+            }
+            L.mesh.swap(nm); L.h.swap(nh);
+            L.N = 2 * nI + 1;
+            CU(cudaMemcpy(static_cast<double*>(h->d_mesh.p) + L.off, L.mesh.data(), size_t(L.N) * 8, cudaMemcpyHostToDevice));
+            CU(cudaMemcpy(static_cast<double*>(h->d_h.p) + L.off, L.h.data(), size_t(L.N - 1) * 8, cudaMemcpyHostToDevice));
+            CU(cudaMemset(static_cast<double*>(h->d_y.p) + L.off * M, 0, size_t(L.N) * M * 8));
+        }
+        s = upload_N();
+        if (s != BVP_OK) return s;
+        for (int q : act) {
+            LargeInst& L = I[q];
+            if (!L.done && L.rounds >= o.max_rounds) { L.retcode = BVP_RET_MAXITERS; L.done = true; }
+        }
+    }
+    CU(cudaEventRecord(h->ev[2], h->stream));
+    // results: per-instance state and the packed mesh and solution
+    long long total = 0;
+    for (int q = 0; q < n; ++q) total += I[q].N;
+    if (h->out_cap < total) {
+        s = grow_outputs(h, total);
+        if (s != BVP_OK) return s;
+    }
+    h->st.assign(n, BvpInstState{});
+    h->offsets.assign(n + 1, 0);
+    double* hm = static_cast<double*>(h->h_mesh.p);
+    double* hy = static_cast<double*>(h->h_y.p);
+    for (int q = 0; q < n; ++q) {
+        const LargeInst& L = I[q];
+        BvpInstState& st = h->st[q];
+        st.N = L.N; st.cur = 0; st.retcode = L.retcode; st.newton_iters = L.newton_total; st.rounds = L.rounds;
+        st.flags = L.flags; st.defect = L.defect; st.resid = L.resid;
+        const long long o0 = h->offsets[q];
+        std::memcpy(hm + o0, L.mesh.data(), size_t(L.N) * 8);
+        CU(cudaMemcpyAsync(hy + o0 * M, static_cast<const double*>(h->d_y.p) + L.off * M, size_t(L.N) * M * 8,
+                           cudaMemcpyDeviceToHost, h->stream));
+        h->offsets[q + 1] = o0 + L.N;
+    }
+    CU(cudaStreamSynchronize(h->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->ev[0], h->ev[2]);
+    h->timing_ms[0] = ms;
+    h->timing_ms[1] = ms;
+    h->last_n = n;
+    h->stages_ok = false;
+    h->have_results = true;
+    h->pending_device = false;
+    if (out) {
+        for (int q = 0; q < n; ++q) {
+            const BvpInstState& st = h->st[q];
+            if (out->retcode) out->retcode[q] = st.retcode;
+            if (out->n_nodes) out->n_nodes[q] = st.N;
+            if (out->newton_iters) out->newton_iters[q] = st.newton_iters;
+            if (out->rounds) out->rounds[q] = st.rounds;
+            if (out->defect) out->defect[q] = st.defect;
+            if (out->resid) out->resid[q] = st.resid;
+        }
+    }
+    return BVP_OK;
+}
+
 bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const int32_t* n_intervals,
                            const double* tspans, int32_t y0_mode, const double* y0, bvp_results* out) {
     if (!h) return BVP_ERR_INVALID;
     if (n < 1 || !n_intervals || !tspans || !y0 || (h->desc.n_params > 0 && !params) ||
         (y0_mode != 0 && y0_mode != 1))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
+    if (h->large) return solve_large(h, n, params, n_intervals, tspans, y0_mode, y0, out);
     const int M = h->L.M;
     long long tot = 0, y0_vals = 0, pts = 0;
     for (int q = 0; q < n; ++q) {

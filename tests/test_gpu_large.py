@@ -1,0 +1,77 @@
+"""The larger-state path (M > 8: csrc/bvp_large.cuh and the host-driven rounds) against the
+oracle, on the coupled nonlinear n = 32 family u' = A u + tanh(B u) + c with separated
+boundary conditions (16 components fixed at each end)."""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle, RET_SUCCESS
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle(p):
+    return Oracle(p.source, p.M, p.n_params, twopoint=p.twopoint, bc_t=p.bc_t, La=p.La, Lb=p.Lb)
+
+
+def _compare(res, ref, tol_rel, frac_tight=1.0):
+    n = len(res.n_nodes)
+    assert (res.retcode == ref["retcode"]).all(), (res.retcode, ref["retcode"])
+    assert (res.n_nodes == ref["n_nodes"]).all(), (res.n_nodes, ref["n_nodes"])
+    tight = []
+    for i in range(n):
+        N = int(ref["n_nodes"][i])
+        m, y = res.solution(i)
+        # FP64 sums in another order (FMA contraction) move redistributed points at 1e-11
+        assert np.abs(m - ref["mesh"][i, :N]).max() <= 1e-9
+        u = np.abs(ref["y"][i, :N]).max()
+        err = np.abs(y - ref["y"][i, :N]).max()
+        assert err <= tol_rel * max(1.0, u), (i, err)
+        tight.append(err <= max(1e-6, 1e-9 * u))
+    assert np.mean(tight) >= frac_tight
+
+
+@pytest.mark.parametrize("jac_precision", [64, 32])
+def test_nonlinear32_matches_oracle(pkg, problems, jac_precision):
+    # FP64 blocks: the Newton iterates follow the oracle's, solutions within max(abstol, 1e-9|u|);
+    # FP32 blocks (FP64 residual as right-hand side): the same root, within 1e-5 relative
+    p = problems.NONLINEAR32
+    params, nint, tsp, y0 = problems.nonlinear32_family(6, n_intervals=64)
+    sv = pkg.BatchSolver(p, order=4, jac_precision=jac_precision)
+    res = sv.solve(params, nint, tsp, y0)
+    ref = _oracle(p).solve_batch(params, nint, tsp, y0)
+    assert (res.retcode == RET_SUCCESS).all()
+    if jac_precision == 64:
+        assert (res.newton_iters == ref["newton_iters"]).all(), (res.newton_iters, ref["newton_iters"])
+        _compare(res, ref, 1e-6)
+    else:
+        _compare(res, ref, 1e-5)
+
+
+def test_nonlinear32_refines_like_the_oracle(pkg, problems):
+    # a coarse initial mesh forces mesh selection, redistribution and the in-place transfer
+    p = problems.NONLINEAR32
+    params, nint, tsp, y0 = problems.nonlinear32_family(4, seed=77, n_intervals=6)
+    sv = pkg.BatchSolver(p, order=4, jac_precision=64)
+    res = sv.solve(params, nint, tsp, y0)
+    ref = _oracle(p).solve_batch(params, nint, tsp, y0)
+    assert (ref["rounds"] > 1).any()
+    assert (res.rounds == ref["rounds"]).all(), (res.rounds, ref["rounds"])
+    _compare(res, ref, 1e-6)
+
+
+def test_nonlinear32_mirk6_and_reference_size(pkg, problems):
+    # the benchmark configuration's mesh (1024 intervals) on a few instances, and MIRK6: every
+    # result passes the reference's acceptance tests evaluated by the oracle
+    p = problems.NONLINEAR32
+    o = _oracle(p)
+    for order, nI, count in ((4, 1024, 8), (6, 64, 4)):
+        params, nint, tsp, y0 = problems.nonlinear32_family(count, seed=5, n_intervals=nI)
+        sv = pkg.BatchSolver(p, order=order)
+        res = sv.solve(params, nint, tsp, y0)
+        assert (res.retcode == RET_SUCCESS).all()
+        for i in range(count):
+            m, y = res.solution(i)
+            F, K, nrm = o.residual(params[i], m, y, order=order)
+            assert nrm <= 1e-6 * (1 + 1e-6), (order, i, nrm)
+            err, dn = o.defect(params[i], m, y, order=order)
+            assert dn <= 1e-6 * (1 + 1e-3), (order, i, dn)
