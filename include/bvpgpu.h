@@ -39,7 +39,8 @@ typedef enum {
  * (lib/BoundaryValueDiffEqMIRK/src/interpolation.jl:214-242); two-point problems give La
  * residuals at t0 and Lb at t1 (lib/BoundaryValueDiffEqCore/src/utils.jl:157-181). */
 typedef struct {
-    int32_t M;            /* state dimension (1..8 on the warp-per-instance kernels) */
+    int32_t M;            /* state dimension 1..32: up to 8 one warp solves an instance; above 8
+                             the larger-state kernels run (two-point BCs, bvp_solve_batch only) */
     int32_t n_params;     /* parameters per instance */
     int32_t twopoint;     /* 0 standard, 1 two-point */
     int32_t n_bc_pts;     /* standard: number of evaluation times (1..16) */
