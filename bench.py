@@ -129,9 +129,16 @@ def _max_over_ranks(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def rank_batch(P, n_inst, rank):
+    """Each rank solves its own seed-shifted batch: instances are independent, so the path
+    shards by instance with no exchange (weak scaling)."""
+    return P.pendulum_family(n_inst, seed=SEED + rank)
 
 
 def _algorithmic_bytes(res, M=2, s=3):
@@ -262,7 +269,7 @@ def main():
     net = sur.net
 
     # every rank solves its own 4096-instance batch (instances are independent: weak scaling)
-    params, nint, tsp, y0 = P.pendulum_family(n_inst, seed=SEED + rank)
+    params, nint, tsp, y0 = rank_batch(P, n_inst, rank)
     feats = params.astype(np.float32)
     sv = pkg.BatchSolver(P.PENDULUM, order=4, abstol=1e-6, jac_precision=args.jac_precision)
     lib = sv.lib
