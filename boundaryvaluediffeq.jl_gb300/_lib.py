@@ -77,6 +77,48 @@ def _run(cmd, log=None):
     return r
 
 
+def _nvrtc():
+    for name in ("libnvrtc.so", "libnvrtc.so.13", os.path.join(os.path.dirname(NVCC), "..", "lib64", "libnvrtc.so")):
+        try:
+            return C.CDLL(name)
+        except OSError:
+            continue
+    return None
+
+
+def nvrtc_check(problem, order: int, jac_bits: int = 32) -> None:
+    """Compile the problem's kernels with NVRTC exactly as bvp_create does (same source
+    assembly and options, no GPU needed); raises with the NVRTC log on failure."""
+    lib = _nvrtc()
+    if lib is None:
+        return
+    large = problem.M > 8
+    nbc = 2 if problem.twopoint else len(problem.bc_t)
+    src = ("#include \"bvp_prelude.cuh\"\n#line 1 \"problem_source\"\n" + problem.source +
+           ("\n#include \"bvp_large.cuh\"\n" if large else "\n#include \"bvp_kernels.cuh\"\n"))
+    opts = ["--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true", f"-DBVP_M={problem.M}",
+            f"-DBVP_ORDER={order}", f"-DBVP_TWOPOINT={int(problem.twopoint)}", f"-DBVP_NBC={nbc}",
+            f"-DBVP_LA={problem.La if problem.twopoint else 0}",
+            "-DBVP_JT=" + ("double" if jac_bits == 64 else "float")]
+    names = [fn.encode() for fn in EMBED]
+    bodies = [open(os.path.join(CSRC, fn), "rb").read() for fn in EMBED]
+    prog = C.c_void_p()
+    arr = lambda xs: (C.c_char_p * len(xs))(*xs)
+    if lib.nvrtcCreateProgram(C.byref(prog), src.encode(), b"bvp_problem.cu", len(EMBED), arr(bodies), arr(names)):
+        raise RuntimeError("nvrtcCreateProgram failed")
+    try:
+        rc = lib.nvrtcCompileProgram(prog, len(opts), arr([o.encode() for o in opts]))
+        n = C.c_size_t()
+        lib.nvrtcGetProgramLogSize(prog, C.byref(n))
+        log = C.create_string_buffer(n.value)
+        lib.nvrtcGetProgramLog(prog, log)
+        if rc != 0:
+            raise RuntimeError(f"NVRTC build check failed ({problem.name}, MIRK{order}, JT {jac_bits}):\n"
+                               + log.value.decode(errors="replace"))
+    finally:
+        lib.nvrtcDestroyProgram(C.byref(prog))
+
+
 def device_check_source(problem) -> str:
     """A translation unit with the problem inlined, for the nvcc sm_103a build check."""
     kernels = "bvp_large.cuh" if problem.M > 8 else "bvp_kernels.cuh"
@@ -113,6 +155,12 @@ def build_library(verbose: bool = False, force: bool = False, check_problems=Non
                    "-o", os.path.join(BUILD, f"check_{prob.name}_o{order}.cubin")]
             check_cmds.append((cmd, os.path.join(BUILD, f"ptxas_{prob.name}_o{order}.txt")))
             jobs.append(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
+        # the same kernels through NVRTC (what bvp_create runs), in both Jacobian precisions
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(max_workers=4) as ex:
+            futs = [ex.submit(nvrtc_check, prob, order, bits) for prob, order, _ in checks for bits in (32, 64)]
+            for f in futs:
+                f.result()
         outs = [j.communicate()[0] for j in jobs]
         if jobs[0].returncode != 0:
             raise RuntimeError("host library build failed:\n" + " ".join(host_cmd) + "\n" + outs[0])

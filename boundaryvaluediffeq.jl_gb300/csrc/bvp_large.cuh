@@ -9,11 +9,12 @@
 //   bl_jacobian  one thread per (instance, interval, 8 tangent directions): the blocks
 //                S_i = dr_i/dy_i, R_i = dr_i/dy_{i+1} by forward mode in BVP_JT, and the BC
 //                blocks
-//   bl_linsolve  one CTA per instance: each warp eliminates a chunk of intervals in shared
-//                memory (Gaussian elimination with row pivoting on the 2M x M column block,
-//                the warp owning two rows per lane), the chunk relations are combined
-//                pairwise, a 2M x 2M system with the BC rows gives the end values, and the
-//                warps back-substitute their chunks
+//   bl_linsolve  one CTA per instance: each warp eliminates a chunk of intervals node by
+//                node (the 2M x M pivot panel LU-factorised with row pivoting in registers,
+//                the trailing columns by a column-parallel triangular solve and Schur
+//                update from shared memory), the chunk relations are combined pairwise, a
+//                2M x 2M system with the BC rows gives the end values, and the warps
+//                back-substitute their chunks
 //   bl_update    y += delta (or y = ybase + alpha delta for the line search)
 //   bl_defect    one thread per interval: extra stages and the defect at tau*, 1 - tau*
 //   bl_transfer  one warp per refined instance: the new guess from the old interpolant
@@ -49,9 +50,6 @@ constexpr int NCH = 8;                        // tangent directions per Jacobian
 constexpr int NCHUNK = (D + NCH - 1) / NCH;   // thread slots per interval
 constexpr int NCHB = (M + NCH - 1) / NCH;     // thread slots of the BC Jacobian
 constexpr int RECW = 3 * M * M + M;
-constexpr int WR = 2 * M;                     // elimination workspace rows
-constexpr int WC = 3 * M + 1;                 // columns: δ_mid | δ_lo | δ_hi | rhs
-constexpr int WLD = WC + (WC % 2 == 0 ? 1 : 0);   // odd row stride: conflict-free columns
 static_assert(M <= 32 && M > 0, "M <= 32");
 
 BVP_DEV int lane_id() { return threadIdx.x & 31; }
@@ -227,24 +225,110 @@ extern "C" __global__ void __launch_bounds__(128) bl_jacobian(const BvpLargeArgs
 
 namespace bvp {
 
-// Gaussian elimination with row pivoting on the first M columns of the warp's 2M x WC
-// workspace W (lane l owns rows l and l + 32). Afterwards rows 0..M-1 hold the pivot rows
-// [U | X | Y | g] (U upper triangular) and rows M..2M-1 the reduced equations
-// [0 | A' | B' | g']. Returns false on a zero or non-finite pivot (uniform across the warp).
-BVP_DEV bool warp_gepp(JT* W, int ncols) {
+// ---- structured elimination of one node (K3 for the larger-state path) -------------------
+// The current relation of a warp, `Rel`, is B δ_mid + A δ_lo = g, stored as the M x (2M+1)
+// rows [B | A | g]. A new block row (the next interval, S_c δ_c + R_c δ_c+1 = -F_c, or a
+// partner warp's relation) brings Sb δ_mid + Rb δ_hi = gb. Eliminating δ_mid:
+//   1. the 2M x M panel [B; Sb] is LU-factorised with row pivoting in registers (lane l owns
+//      top row l and bottom row l; the pivot row travels by shuffles);
+//   2. the pivot rows' trailing columns (δ_lo | δ_hi | rhs) are solved with the unit lower
+//      factor L11 (U12 = L11^-1 T_top, column-parallel: lane c owns column c; the rhs column
+//      row-parallel), and the unpivoted rows get the Schur complement T_bot - L21 U12 (lane c
+//      again owns column c, L21 rows broadcast from shared memory);
+//   3. the pivot rows [U11 | U12] are the elimination record (δ_mid = U11^-1 (g - X δ_lo -
+//      Y δ_hi)), the Schur rows the new relation [B'' | A' | g'] on δ_hi (the new δ_mid)
+//      and δ_lo.
+// This is the block Gaussian elimination with row pivoting the reference's almost-banded LU
+// performs, ordered by node (LinearSolve/FastAlmostBandedMatrices, mirk.jl:774-778).
+
+// row strides: >= the row length and = 4 (mod 8), so eight lanes reading eight rows with
+// 16-byte loads touch distinct banks
+#define BVP_PAD48(n) ((n) % 8 <= 4 ? (n) + (4 - (n) % 8) : (n) + (12 - (n) % 8))
+constexpr int RLD = BVP_PAD48(2 * M + 1);  // relation rows [B | A | g]
+constexpr int LLD = BVP_PAD48(M);          // panel factor rows
+constexpr int DLD = 2 * M + 2;             // dense end system rows
+constexpr int WJT = M * RLD + 2 * M * LLD + ((M + 3) / 4) * 4;   // JT elements per warp
+constexpr int WARP_BYTES = ((WJT * int(sizeof(JT)) + 15) / 16) * 16 + ((2 * M * 4 + 15) / 16) * 16;
+constexpr int DENSE_BYTES = ((2 * M * DLD * int(sizeof(JT)) + 15) / 16) * 16;
+
+struct WarpMem {
+    JT* rel;    // M x RLD
+    JT* lf;     // 2M x LLD: rows 0..M-1 pivot rows (L11 | U11) in pivot order, M..2M-1 L21
+    JT* xs;     // M: the rhs column of U12
+    int* pidx;  // M: physical row of pivot k (top rows 0..M-1, bottom rows M..2M-1)
+    int* qidx;  // M: physical row of unpivoted row u
+};
+BVP_DEV WarpMem warp_mem(unsigned char* base, int w) {
+    unsigned char* p = base + (size_t)w * WARP_BYTES;
+    WarpMem m;
+    m.rel = reinterpret_cast<JT*>(p);
+    m.lf = m.rel + M * RLD;
+    m.xs = m.lf + 2 * M * LLD;
+    m.pidx = reinterpret_cast<int*>(p + ((WJT * int(sizeof(JT)) + 15) / 16) * 16);
+    m.qidx = m.pidx + M;
+    return m;
+}
+
+// bottom block row: the next interval's Jacobian blocks (global memory)
+struct BotInterval {
+    const JT* S;
+    const JT* R;
+    const double* F;
+    BVP_DEV JT panel(int u, int j) const { return S[u * M + j]; }
+    BVP_DEV JT hi(int u, int c) const { return R[u * M + c]; }
+    BVP_DEV JT rhs(int u) const { return JT(-F[u]); }
+};
+// bottom block row: a partner warp's relation [B2 | A2 | g2], whose δ_lo is the shared node
+struct BotRel {
+    const JT* rl;
+    BVP_DEV JT panel(int u, int j) const { return rl[u * RLD + M + j]; }
+    BVP_DEV JT hi(int u, int c) const { return rl[u * RLD + c]; }
+    BVP_DEV JT rhs(int u) const { return rl[u * RLD + 2 * M]; }
+};
+
+// pivot candidate: |x| for rows still unpivoted (NaN ranks first, so it is chosen and fails
+// the finiteness test), -1 for pivoted or absent rows
+BVP_DEV JT pivot_cand(JT x, bool live) {
+    if (!live) return JT(-1);
+    const JT v = fabs(x);
+    return v == v ? v : JT(__longlong_as_double(0x7ff0000000000000LL));
+}
+
+// 4 consecutive row entries from shared memory (16-byte aligned when JT is float)
+BVP_DEV void ld4(const JT* p, JT* v) {
+    if constexpr (sizeof(JT) == 4) {
+        const float4 t = *reinterpret_cast<const float4*>(p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else {
+        const double2 t0 = *reinterpret_cast<const double2*>(p);
+        const double2 t1 = *reinterpret_cast<const double2*>(p + 2);
+        v[0] = t0.x; v[1] = t0.y; v[2] = t1.x; v[3] = t1.y;
+    }
+}
+
+template <class Bot>
+BVP_DEV bool warp_eliminate(const WarpMem& wm, const Bot& bot, JT* rec) {
+    constexpr int M4 = ((M + 3) / 4) * 4;
     const int lane = lane_id();
-    bool ok = true;
-    for (int k = 0; k < M; ++k) {
-        JT v = JT(-1);
-        int pr = 0x7fffffff;
+    const bool act = lane < M;
+    JT* Rel = wm.rel;
+    JT* Lf = wm.lf;
+    // 1. panel rows in registers: top row `lane` = B, bottom row `lane` = the new block's
+    JT a0[M], a1[M];
 #pragma unroll
-        for (int h2 = 0; h2 < 2; ++h2) {
-            const int r = lane + 32 * h2;
-            if (r >= k && r < WR) {
-                const JT av = fabs(W[r * WLD + k]);
-                if (av > v) { v = av; pr = r; }
-            }
-        }
+    for (int j = 0; j < M; ++j) {
+        a0[j] = act ? Rel[lane * RLD + j] : JT(0);
+        a1[j] = act ? bot.panel(lane, j) : JT(0);
+    }
+    int st0 = act ? -1 : M, st1 = act ? -1 : M;   // pivot step of each row; -1 while unpivoted
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+        // pivot: largest |entry| in column k among unpivoted rows, ties to the lower row id
+        JT v = pivot_cand(a0[k], st0 < 0);
+        int pr = lane;
+        const JT v1 = pivot_cand(a1[k], st1 < 0);
+        if (v1 > v) { v = v1; pr = M + lane; }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const JT v2 = __shfl_xor_sync(FULL, v, o);
@@ -252,22 +336,137 @@ BVP_DEV bool warp_gepp(JT* W, int ncols) {
             if (v2 > v || (v2 == v && p2 < pr)) { v = v2; pr = p2; }
         }
         ok = ok && v > JT(0) && isfinite(v);
-        if (pr != k && pr < WR) {
-            for (int c = lane; c < ncols; c += 32) {
-                const JT tmp = W[k * WLD + c];
-                W[k * WLD + c] = W[pr * WLD + c];
-                W[pr * WLD + c] = tmp;
+        const bool pbot = pr >= M;
+        const int own = pbot ? pr - M : pr;
+        JT prow[M];
+#pragma unroll
+        for (int j = k; j < M; ++j) prow[j] = __shfl_sync(FULL, pbot ? a1[j] : a0[j], own);
+        if (lane == own) { if (pbot) st1 = k; else st0 = k; }
+        if (lane == 0) wm.pidx[k] = pr;
+        const JT inv = JT(1) / prow[k];
+        if (st0 < 0) {
+            const JT m = a0[k] * inv;
+            a0[k] = m;
+#pragma unroll
+            for (int j = k + 1; j < M; ++j) a0[j] -= m * prow[j];
+        }
+        if (st1 < 0) {
+            const JT m = a1[k] * inv;
+            a1[k] = m;
+#pragma unroll
+            for (int j = k + 1; j < M; ++j) a1[j] -= m * prow[j];
+        }
+    }
+    // 2. factor rows to shared memory: pivot rows by step, unpivoted rows compacted
+    //    (top rows first, by lane, then bottom rows)
+    const unsigned b0 = __ballot_sync(FULL, st0 < 0);
+    const unsigned b1 = __ballot_sync(FULL, st1 < 0);
+    const unsigned lt = (1u << lane) - 1u;
+    {
+        const int r0 = st0 >= 0 ? st0 : M + __popc(b0 & lt);
+        const int r1 = st1 >= 0 ? st1 : M + __popc(b0) + __popc(b1 & lt);
+        if (act) {
+#pragma unroll
+            for (int j = 0; j < M; ++j) { Lf[r0 * LLD + j] = a0[j]; Lf[r1 * LLD + j] = a1[j]; }
+            if (st0 < 0) wm.qidx[r0 - M] = lane;
+            if (st1 < 0) wm.qidx[r1 - M] = M + lane;
+        }
+    }
+    __syncwarp();
+    // 3. U11 into the record
+    if (act) {
+        for (int k = 0; k < M; ++k) rec[k * M + lane] = Lf[k * LLD + lane];
+    }
+    // 4. rhs column: forward substitution row-parallel (lane k owns pivot row k), then the
+    //    Schur rows (lane u owns unpivoted row u)
+    {
+        JT xr = JT(0);
+        JT Lk[M4];
+        if (act) {
+            const int p = wm.pidx[lane];
+            xr = p < M ? Rel[p * RLD + 2 * M] : bot.rhs(p - M);
+#pragma unroll
+            for (int j = 0; j < M4; j += 4) ld4(&Lf[lane * LLD + j], &Lk[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < M - 1; ++j) {
+            const JT xj = __shfl_sync(FULL, xr, j);
+            if (lane > j && act) xr -= Lk[j] * xj;
+        }
+        if (act) {
+            rec[3 * M * M + lane] = xr;
+            wm.xs[lane] = xr;
+        }
+        __syncwarp();
+        JT sr = JT(0);
+        if (act) {
+            const int qq = wm.qidx[lane];
+            sr = qq < M ? Rel[qq * RLD + 2 * M] : bot.rhs(qq - M);
+#pragma unroll
+            for (int j = 0; j < M4; j += 4) {
+                JT l4[4], x4[4];
+                ld4(&Lf[(M + lane) * LLD + j], l4);
+                ld4(&wm.xs[j], x4);
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (j + t < M) sr -= l4[t] * x4[t];
             }
         }
         __syncwarp();
-        const JT inv = JT(1) / W[k * WLD + k];
+        if (act) Rel[lane * RLD + 2 * M] = sr;
+    }
+    // 5. the δ_lo and δ_hi columns: lane c owns column c (two passes when M > 16)
+#pragma unroll 1
+    for (int s = 0; s < (2 * M + 31) / 32; ++s) {
+        const int c = lane + 32 * s;
+        const bool cv = c < 2 * M;
+        const bool lo = c < M;
+        JT x[M];
 #pragma unroll
-        for (int h2 = 0; h2 < 2; ++h2) {
-            const int r = lane + 32 * h2;
-            if (r > k && r < WR) {
-                const JT mlt = W[r * WLD + k] * inv;
-                for (int c = k; c < ncols; ++c) W[r * WLD + c] -= mlt * W[k * WLD + c];
+        for (int k = 0; k < M; ++k) {
+            const int p = wm.pidx[k];
+            JT t = JT(0);
+            if (cv) {
+                if (p < M) { if (lo) t = Rel[p * RLD + M + c]; }
+                else if (!lo) t = bot.hi(p - M, c - M);
             }
+#pragma unroll
+            for (int j = 0; j < k; j += 4) {
+                JT l4[4];
+                ld4(&Lf[k * LLD + j], l4);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (j + q < k) t -= l4[q] * x[j + q];
+            }
+            x[k] = t;
+        }
+        JT sc[M];
+#pragma unroll
+        for (int u = 0; u < M; ++u) {
+            const int qq = wm.qidx[u];
+            JT t = JT(0);
+            if (cv) {
+                if (qq < M) { if (lo) t = Rel[qq * RLD + M + c]; }
+                else if (!lo) t = bot.hi(qq - M, c - M);
+            }
+#pragma unroll
+            for (int j = 0; j < M4; j += 4) {
+                JT l4[4];
+                ld4(&Lf[(M + u) * LLD + j], l4);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (j + q < M) t -= l4[q] * x[j + q];
+            }
+            sc[u] = t;
+        }
+        __syncwarp();
+        if (cv) {
+            JT* rx = rec + (lo ? M * M + c : 2 * M * M + c - M);
+#pragma unroll
+            for (int k = 0; k < M; ++k) rx[k * M] = x[k];
+            const int dc = lo ? M + c : c - M;
+#pragma unroll
+            for (int u = 0; u < M; ++u) Rel[u * RLD + dc] = sc[u];
         }
         __syncwarp();
     }
@@ -292,41 +491,14 @@ BVP_DEV void warp_back_solve(const JT* rg, const JT* lo, const JT* hi, JT* x_out
     __syncwarp();
 }
 
-// store the pivot rows of W as an elimination record
-BVP_DEV void store_record(const JT* W, JT* rec) {
-    for (int e = lane_id(); e < M * M; e += 32) {
-        const int r = e / M, c = e % M;
-        rec[e] = W[r * WLD + c];
-        rec[M * M + e] = W[r * WLD + M + c];
-        rec[2 * M * M + e] = W[r * WLD + 2 * M + c];
-    }
-    for (int r = lane_id(); r < M; r += 32) rec[3 * M * M + r] = W[r * WLD + 3 * M];
-    __syncwarp();
-}
-
-// relation rows M..2M-1 of W ([0 | A | B | g]) moved to rows 0..M-1 as the current relation
-// in the layout [B | A | 0 | g] ready for the next elimination (δ_hi becomes δ_mid)
-BVP_DEV void relation_to_top(JT* W) {
-    for (int e = lane_id(); e < M * M; e += 32) {
-        const int r = e / M, c = e % M;
-        const JT A = W[(M + r) * WLD + M + c];
-        const JT B = W[(M + r) * WLD + 2 * M + c];
-        W[r * WLD + c] = B;
-        W[r * WLD + M + c] = A;
-        W[r * WLD + 2 * M + c] = JT(0);
-    }
-    for (int r = lane_id(); r < M; r += 32) W[r * WLD + 3 * M] = W[(M + r) * WLD + 3 * M];
-    __syncwarp();
-}
-
 }  // namespace bvp
 
 // ---- linear solve: one CTA per active instance ----------------------------------------------
-// Dynamic shared memory: one WR x WLD workspace per warp (BVP_JT).
+// Dynamic shared memory: WARP_BYTES per warp (relation, panel factors, indices) and the
+// dense end system (DENSE_BYTES).
 extern "C" __global__ void __launch_bounds__(256) bl_linsolve(const BvpLargeArgs a) {
     using namespace bvp;
     extern __shared__ __align__(16) unsigned char bl_smem[];
-    JT* Wall = reinterpret_cast<JT*>(bl_smem);
     __shared__ int s_lo[8], s_hi[8];
     __shared__ int s_bad;
     const int q = a.active[blockIdx.x];
@@ -336,7 +508,7 @@ extern "C" __global__ void __launch_bounds__(256) bl_linsolve(const BvpLargeArgs
     const int NWl = int(blockDim.x >> 5);
     const int NW = nI < NWl ? nI : NWl;             // warps with a chunk
     const long long nb = a.node_off[q];
-    JT* W = Wall + warp * (WR * WLD);
+    const WarpMem wm = warp_mem(bl_smem, warp);
     const JT* Sb = a.Sb + nb * (M * M);
     const JT* Rb = a.Rb + nb * (M * M);
     const double* F = a.F + nb * M;
@@ -349,28 +521,18 @@ extern "C" __global__ void __launch_bounds__(256) bl_linsolve(const BvpLargeArgs
     if (warp < NW) {
         c0 = (warp * nI) / NW;
         c1 = ((warp + 1) * nI) / NW;
-        // relation of interval c0: S δ_c0 + R δ_c0+1 = -F, in the top rows as [R | S | 0 | -F]
+        // relation of interval c0: S δ_c0 + R δ_c0+1 = -F as [R | S | -F] (δ_mid = δ_c0+1)
         for (int e = lane; e < M * M; e += 32) {
             const int r = e / M, c = e % M;
-            W[r * WLD + c] = Rb[(long long)c0 * M * M + e];
-            W[r * WLD + M + c] = Sb[(long long)c0 * M * M + e];
-            W[r * WLD + 2 * M + c] = JT(0);
+            wm.rel[r * RLD + c] = Rb[(long long)c0 * M * M + e];
+            wm.rel[r * RLD + M + c] = Sb[(long long)c0 * M * M + e];
         }
-        for (int r = lane; r < M; r += 32) W[r * WLD + 3 * M] = JT(-F[(long long)c0 * M + r]);
+        for (int r = lane; r < M; r += 32) wm.rel[r * RLD + 2 * M] = JT(-F[(long long)c0 * M + r]);
         __syncwarp();
+#pragma unroll 1
         for (int c = c0 + 1; c < c1; ++c) {
-            // bottom rows: interval c, [S_c | 0 | R_c | -F_c]
-            for (int e = lane; e < M * M; e += 32) {
-                const int r = e / M, cc = e % M;
-                W[(M + r) * WLD + cc] = Sb[(long long)c * M * M + e];
-                W[(M + r) * WLD + M + cc] = JT(0);
-                W[(M + r) * WLD + 2 * M + cc] = Rb[(long long)c * M * M + e];
-            }
-            for (int r = lane; r < M; r += 32) W[(M + r) * WLD + 3 * M] = JT(-F[(long long)c * M + r]);
-            __syncwarp();
-            ok &= warp_gepp(W, WC);
-            store_record(W, rec + (long long)c * RECW);
-            relation_to_top(W);
+            const BotInterval bot{Sb + (long long)c * M * M, Rb + (long long)c * M * M, F + (long long)c * M};
+            ok &= warp_eliminate(wm, bot, rec + (long long)c * RECW);
         }
         if (lane == 0) { s_lo[warp] = c0; s_hi[warp] = c1; }
     }
@@ -379,48 +541,31 @@ extern "C" __global__ void __launch_bounds__(256) bl_linsolve(const BvpLargeArgs
     //    with warp w + s; its relation then spans both chunks
     for (int s = 1; s < NW; s <<= 1) {
         if (warp < NW && (warp % (2 * s)) == 0 && warp + s < NW) {
-            const JT* W2 = Wall + (warp + s) * (WR * WLD);
-            // bottom rows: the partner's relation [B2 | A2 | 0 | g2] as [A2 | 0 | B2 | g2]
-            for (int e = lane; e < M * M; e += 32) {
-                const int r = e / M, cc = e % M;
-                W[(M + r) * WLD + cc] = W2[r * WLD + M + cc];
-                W[(M + r) * WLD + M + cc] = JT(0);
-                W[(M + r) * WLD + 2 * M + cc] = W2[r * WLD + cc];
-            }
-            for (int r = lane; r < M; r += 32) W[(M + r) * WLD + 3 * M] = W2[r * WLD + 3 * M];
-            __syncwarp();
-            ok &= warp_gepp(W, WC);
-            store_record(W, rec + (long long)s_hi[warp] * RECW);
-            relation_to_top(W);
+            const BotRel bot{warp_mem(bl_smem, warp + s).rel};
+            ok &= warp_eliminate(wm, bot, rec + (long long)s_hi[warp] * RECW);
             if (lane == 0) s_hi[warp] = s_hi[warp + s];
         }
         __syncthreads();
     }
-    // 3. warp 0: [dbca/dy0 rows | relation | dbcb/dyN rows] in δ_0, δ_N-1 (2M x 2M). The
-    //    relation sits in warp 0's top rows as [B | A | 0 | g] (A on δ_0, B on δ_N-1); it is
-    //    staged in warp 1's workspace in the column order δ_0 | δ_N-1 | rhs first.
+    // 3. warp 0: [dbca/dy0 rows | relation | dbcb/dyN rows] in δ_0, δ_N-1 (2M x 2M); the
+    //    relation is [B | A | g] with A on δ_0 and B on δ_N-1
     if (warp == 0) {
-        JT* Wd = W;
-        JT* Wt = Wall + 1 * (WR * WLD);
+        JT* Wd = reinterpret_cast<JT*>(bl_smem + (size_t)NWl * WARP_BYTES);
         const JT* G0 = a.G + (long long)q * 2 * M * M;
         const JT* G1 = G0 + M * M;
         const double* bc = a.bcres + (long long)q * M;
-        for (int e = lane; e < M * (2 * M + 1); e += 32) {
-            const int r = e / (2 * M + 1), c = e % (2 * M + 1);
-            Wt[r * WLD + c] = c < M ? W[r * WLD + M + c] : (c < 2 * M ? W[r * WLD + c - M] : W[r * WLD + 3 * M]);
-        }
-        __syncwarp();
+        const JT* Rl = wm.rel;
         for (int e = lane; e < LA * (2 * M + 1); e += 32) {
             const int r = e / (2 * M + 1), c = e % (2 * M + 1);
-            Wd[r * WLD + c] = c < M ? G0[r * M + c] : (c < 2 * M ? JT(0) : JT(-bc[r]));
+            Wd[r * DLD + c] = c < M ? G0[r * M + c] : (c < 2 * M ? JT(0) : JT(-bc[r]));
         }
         for (int e = lane; e < M * (2 * M + 1); e += 32) {
             const int r = e / (2 * M + 1), c = e % (2 * M + 1);
-            Wd[(LA + r) * WLD + c] = Wt[r * WLD + c];
+            Wd[(LA + r) * DLD + c] = c < M ? Rl[r * RLD + M + c] : (c < 2 * M ? Rl[r * RLD + c - M] : Rl[r * RLD + 2 * M]);
         }
         for (int e = lane; e < (M - LA) * (2 * M + 1); e += 32) {
             const int r = LA + e / (2 * M + 1), c = e % (2 * M + 1);
-            Wd[(M + r) * WLD + c] = c < M ? JT(0) : (c < 2 * M ? G1[r * M + c - M] : JT(-bc[r]));
+            Wd[(M + r) * DLD + c] = c < M ? JT(0) : (c < 2 * M ? G1[r * M + c - M] : JT(-bc[r]));
         }
         __syncwarp();
         // dense elimination with pivoting on all 2M columns, then back substitution
@@ -432,7 +577,7 @@ extern "C" __global__ void __launch_bounds__(256) bl_linsolve(const BvpLargeArgs
             for (int h2 = 0; h2 < 2; ++h2) {
                 const int r = lane + 32 * h2;
                 if (r >= k && r < 2 * M) {
-                    const JT av = fabs(Wd[r * WLD + k]);
+                    const JT av = pivot_cand(Wd[r * DLD + k], true);
                     if (av > v) { v = av; pr = r; }
                 }
             }
@@ -445,32 +590,32 @@ extern "C" __global__ void __launch_bounds__(256) bl_linsolve(const BvpLargeArgs
             dok = dok && v > JT(0) && isfinite(v);
             if (pr != k && pr < 2 * M) {
                 for (int c = lane; c <= 2 * M; c += 32) {
-                    const JT tmp = Wd[k * WLD + c];
-                    Wd[k * WLD + c] = Wd[pr * WLD + c];
-                    Wd[pr * WLD + c] = tmp;
+                    const JT tmp = Wd[k * DLD + c];
+                    Wd[k * DLD + c] = Wd[pr * DLD + c];
+                    Wd[pr * DLD + c] = tmp;
                 }
             }
             __syncwarp();
-            const JT inv = JT(1) / Wd[k * WLD + k];
+            const JT inv = JT(1) / Wd[k * DLD + k];
 #pragma unroll
             for (int h2 = 0; h2 < 2; ++h2) {
                 const int r = lane + 32 * h2;
                 if (r > k && r < 2 * M) {
-                    const JT mlt = Wd[r * WLD + k] * inv;
-                    for (int c = k; c <= 2 * M; ++c) Wd[r * WLD + c] -= mlt * Wd[k * WLD + c];
+                    const JT mlt = Wd[r * DLD + k] * inv;
+                    for (int c = k; c <= 2 * M; ++c) Wd[r * DLD + c] -= mlt * Wd[k * DLD + c];
                 }
             }
             __syncwarp();
         }
         for (int k = 2 * M - 1; k >= 0; --k) {
-            if (lane == 0) Wd[k * WLD + 2 * M] = Wd[k * WLD + 2 * M] / Wd[k * WLD + k];
+            if (lane == 0) Wd[k * DLD + 2 * M] = Wd[k * DLD + 2 * M] / Wd[k * DLD + k];
             __syncwarp();
-            for (int r = lane; r < k; r += 32) Wd[r * WLD + 2 * M] -= Wd[r * WLD + k] * Wd[k * WLD + 2 * M];
+            for (int r = lane; r < k; r += 32) Wd[r * DLD + 2 * M] -= Wd[r * DLD + k] * Wd[k * DLD + 2 * M];
             __syncwarp();
         }
         for (int m = lane; m < M; m += 32) {
-            dl[m] = Wd[m * WLD + 2 * M];
-            dl[(long long)(N - 1) * M + m] = Wd[(M + m) * WLD + 2 * M];
+            dl[m] = Wd[m * DLD + 2 * M];
+            dl[(long long)(N - 1) * M + m] = Wd[(M + m) * DLD + 2 * M];
         }
         ok &= dok;
     }
@@ -652,8 +797,9 @@ extern "C" __global__ void bl_convert_params(const double* p, bvp::JT* pj, long 
 extern "C" __global__ void bl_layout_probe(int* out) {
     out[0] = int(sizeof(BvpLargeArgs));
     out[1] = bvp::RECW;
-    out[2] = bvp::WLD;
+    out[2] = bvp::WARP_BYTES;
     out[3] = bvp::NCHUNK;
     out[4] = bvp::S;
     out[5] = bvp::NSXA;
+    out[6] = bvp::DENSE_BYTES;
 }

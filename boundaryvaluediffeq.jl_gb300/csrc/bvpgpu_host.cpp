@@ -310,7 +310,8 @@ bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bv
         if (got[0] != int(sizeof(BvpLargeArgs)) || got[1] != h->L.RECW || got[4] != h->L.S || got[5] != h->L.NSXA)
             return fail(h, BVP_ERR_STATE, "host/device layout mismatch (larger-state kernels)");
         h->l_threads = h->js == 8 ? 128 : 256;
-        h->l_smem = size_t(h->l_threads / 32) * size_t(2 * d.M) * size_t(got[2]) * size_t(h->js);
+        // per warp: relation, panel factors and pivot indices; plus the dense end system
+        h->l_smem = size_t(h->l_threads / 32) * size_t(got[2]) + size_t(got[6]);
         CU(cudaFuncSetAttribute((const void*)h->kl_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, int(h->l_smem)));
         return BVP_OK;
     }
