@@ -6,9 +6,10 @@
 // laid out differently:
 //   bl_residual  one thread per (instance, interval): FP64 stages and collocation residual,
 //                the BC rows on the instance's last thread; max |F| and sum F^2 per instance
-//   bl_jacobian  one thread per (instance, interval, 8 tangent directions): the blocks
-//                S_i = dr_i/dy_i, R_i = dr_i/dy_{i+1} by forward mode in BVP_JT, and the BC
-//                blocks
+//   bl_jacobian  one warp per run of 8 intervals: J_f at the stage points one column per
+//                lane (one-direction duals, node stages shared between neighbours), then
+//                the stage chain to the blocks S_i = dr_i/dy_i, R_i = dr_i/dy_{i+1} in
+//                BVP_JT; the warp after an instance's last run computes the BC blocks
 //   bl_linsolve  one CTA per instance: each warp eliminates a chunk of intervals node by
 //                node (the 2M x M pivot panel LU-factorised with row pivoting in registers,
 //                the trailing columns by a column-parallel triangular solve and Schur
@@ -46,10 +47,35 @@ constexpr int M = BVP_M;
 constexpr int D = 2 * M;
 constexpr int LA = BVP_LA;
 using JT = BVP_JT;
-constexpr int NCH = 8;                        // tangent directions per Jacobian thread
-constexpr int NCHUNK = (D + NCH - 1) / NCH;   // thread slots per interval
-constexpr int NCHB = (M + NCH - 1) / NCH;     // thread slots of the BC Jacobian
 constexpr int RECW = 3 * M * M + M;
+#define BVP_B16(n) ((((n) + 15) / 16) * 16)
+
+// Jacobian kernel layout: JG intervals per warp, JW tangent directions per chain pass, per
+// warp S stage-Jacobian slots (M x JLD), the primal stage points and one pass of dY rows
+constexpr bool LNODE = S >= 2 && ORD >= 4;   // stage 0 at the left node, stage 1 at the right
+constexpr int JG = 8;
+constexpr int JW = 16;
+constexpr int JLD = M + 1;                   // odd: lane m reading row m is conflict-free
+constexpr int DYLD = JW + 4;
+constexpr int JWARP_BYTES = BVP_B16((S * M * JLD + S * M + M * DYLD) * int(sizeof(JT)));
+constexpr int JPMAX = 6144;                  // parameters staged in shared memory up to this count
+// slot of stage r's J_f for the kk-th interval of a run: the two node stages alternate
+BVP_DEV int jslot(int r, int kk) {
+    if (LNODE && r == 0) return kk & 1;
+    if (LNODE && r == 1) return (kk + 1) & 1;
+    return r;
+}
+// 4 consecutive entries from shared memory (16-byte aligned)
+BVP_DEV void ld4(const JT* p, JT* v) {
+    if constexpr (sizeof(JT) == 4) {
+        const float4 t = *reinterpret_cast<const float4*>(p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else {
+        const double2 t0 = *reinterpret_cast<const double2*>(p);
+        const double2 t1 = *reinterpret_cast<const double2*>(p + 2);
+        v[0] = t0.x; v[1] = t0.y; v[2] = t1.x; v[3] = t1.y;
+    }
+}
 static_assert(M <= 32 && M > 0, "M <= 32");
 
 BVP_DEV int lane_id() { return threadIdx.x & 31; }
@@ -166,58 +192,188 @@ extern "C" __global__ void __launch_bounds__(128) bl_residual(const BvpLargeArgs
     reduce_norm(a, q, mx, sq, bad);
 }
 
-// ---- Jacobian blocks: threads over (interval, 8 tangent directions) ----------------------
+// ---- Jacobian blocks: one warp per run of JG intervals ---------------------------------------
+// Forward mode in two parts. (1) J_f at each stage point Y_r, column `lane` on lane `lane`
+// (a one-direction dual evaluation of the user's f; the primal stage points come from the
+// FP64 stages the residual wrote at the same iterate). With node stages (MIRK4-6: c = v = 0
+// and c = v = 1) the right node's J_f is the next interval's left node's, so each node is
+// evaluated once per run. (2) The stage chain over the 2M tangent directions, in passes of
+// JW directions with lane m owning row m: dY_r = (1 - v_r)[I 0] + v_r [0 I] + h Σ_j x_rj dK_j,
+// dK_r = J_r dY_r, and the blocks S_i = -I - h Σ_r b_r dK_r[:, :M], R_i = I - h Σ_r b_r dK_r[:, M:]
+// (the derivative of r_i = y_i+1 - y_i - h Σ b_r K_r, collocation.jl:44-72; the reference
+// differentiates the same function with ForwardDiff, mirk.jl:824-838).
+// The warp after the last run of an instance computes the BC blocks.
 extern "C" __global__ void __launch_bounds__(128) bl_jacobian(const BvpLargeArgs a) {
     using namespace bvp;
-    using DC = Dual<JT, NCH>;
+    extern __shared__ __align__(16) unsigned char bj_smem[];
     const int q = a.active[blockIdx.y];
     const int N = a.N[q];
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = t / NCHUNK, ch = t % NCHUNK;
-    if (i > N - 1) return;
+    const int nI = N - 1;
+    const int wpb = int(blockDim.x >> 5);
+    const int warp = threadIdx.x >> 5, lane = lane_id();
+    const int w = blockIdx.x * wpb + warp;
+    const int nruns = (nI + JG - 1) / JG;
+    if (blockIdx.x * wpb > nruns) return;   // whole block past the instance and its BC warp
     const long long nb = a.node_off[q];
-    const JT* pj = a.params_j + (long long)q * a.n_params;
-    const JT* yj = a.yj + nb * M;
-    if (i < N - 1) {
-        DC yi[M], yi1[M], K[S * M], r[M];
-        for (int m = 0; m < M; ++m) { yi[m] = DC(yj[i * M + m]); yi1[m] = DC(yj[(i + 1) * M + m]); }
+    // the instance's parameters in shared memory: every warp of the block evaluates f with them
+    const JT* pg = a.params_j + (long long)q * a.n_params;
+    const bool pstage = a.n_params <= JPMAX;
+    JT* ps = reinterpret_cast<JT*>(bj_smem);
+    if (pstage)
+        for (int k = threadIdx.x; k < a.n_params; k += blockDim.x) ps[k] = pg[k];
+    __syncthreads();
+    const JT* pj = pstage ? ps : pg;
+    if (w > nruns) return;
+    const double* y = a.y + nb * M;
+    if (w == nruns) {
+        // BC blocks: column `lane` of dbca/dy0 (rows 0..La-1) and dbcb/dyN (rows La..M-1)
+        if (lane < M) {
+            JT* G0 = a.G + (long long)q * 2 * M * M;
+            JT* G1 = G0 + M * M;
+            using D1 = Dual<JT, 1>;
+            {
+                D1 u[M], r[M];
 #pragma unroll
-        for (int d = 0; d < NCH; ++d) {
-            const int g = ch * NCH + d;
-            if (g < M) yi[g].d[d] = JT(1);
-            else if (g < D) yi1[g - M].d[d] = JT(1);
-        }
-        phi_large<DC, JT, JT>(yi, yi1, K, r, pj, JT(a.mesh[nb + i]), JT(a.h[nb + i]));
-        JT* Sg = a.Sb + (nb + i) * (M * M);
-        JT* Rg = a.Rb + (nb + i) * (M * M);
-        for (int rr = 0; rr < M; ++rr) {
+                for (int m = 0; m < M; ++m) {
+                    u[m] = D1(JT(y[m]));
+                    u[m].d[0] = m == lane ? JT(1) : JT(0);
+                    r[m] = D1(JT(0));
+                }
+                bvp_bca<D1, JT>(r, u, pj);
 #pragma unroll
-            for (int d = 0; d < NCH; ++d) {
-                const int g = ch * NCH + d;
-                if (g < M) Sg[rr * M + g] = r[rr].d[d];
-                else if (g < D) Rg[rr * M + g - M] = r[rr].d[d];
+                for (int k = 0; k < M; ++k) G0[k * M + lane] = k < LA ? r[k].d[0] : JT(0);
+            }
+            {
+                D1 u[M], r[M];
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    u[m] = D1(JT(y[(long long)(N - 1) * M + m]));
+                    u[m].d[0] = m == lane ? JT(1) : JT(0);
+                    r[m] = D1(JT(0));
+                }
+                bvp_bcb<D1, JT>(r, u, pj);
+#pragma unroll
+                for (int k = 0; k < M; ++k) G1[k * M + lane] = k >= LA ? r[k - LA].d[0] : JT(0);
             }
         }
-    } else if (ch < NCHB) {
-        // BC blocks: columns ch*8.. of dbca/dy0 and dbcb/dyN
-        DC ya[M], yb[M], ra[M], rb[M];
-        for (int m = 0; m < M; ++m) { ya[m] = DC(yj[m]); yb[m] = DC(yj[(N - 1) * M + m]); ra[m] = DC(JT(0)); rb[m] = DC(JT(0)); }
+        return;
+    }
+    const int pb = pstage ? BVP_B16(a.n_params * int(sizeof(JT))) : 0;
+    JT* Jm = reinterpret_cast<JT*>(bj_smem + pb + (size_t)warp * JWARP_BYTES);   // S slots x M x JLD
+    JT* Yp = Jm + S * M * JLD;                                                   // S x M
+    JT* dY = Yp + S * M;                                                         // M x DYLD
+    const double* mesh = a.mesh + nb;
+    const double* hh = a.h + nb;
+    const double* Kg = a.K + nb * (S * M);
+    const int i0 = w * JG;
+    const int i1 = min(i0 + JG, nI);
+#pragma unroll 1
+    for (int i = i0; i < i1; ++i) {
+        const int kk = i - i0;
+        const double ti = mesh[i], hi = hh[i];
+        // primal stage points Y_r = (1 - v_r) y_i + v_r y_i+1 + h Σ_j x_rj K_j
+        for (int m = lane; m < M; m += 32) {
+            const double yi = y[(long long)i * M + m], yi1 = y[(long long)(i + 1) * M + m];
 #pragma unroll
-        for (int d = 0; d < NCH; ++d) {
-            const int g = ch * NCH + d;
-            if (g < M) { ya[g].d[d] = JT(1); yb[g].d[d] = JT(1); }
+            for (int r = 0; r < S; ++r) {
+                double Y = (1.0 - tab_v(r)) * yi + tab_v(r) * yi1;
+#pragma unroll
+                for (int j = 0; j < r; ++j)
+                    if (tab_x(r, j) != 0.0) Y = Y + hi * (Kg[((long long)i * S + j) * M + m] * tab_x(r, j));
+                Yp[r * M + m] = JT(Y);
+            }
         }
-        bvp_bca<DC, JT>(ra, ya, pj);
-        bvp_bcb<DC, JT>(rb, yb, pj);
-        JT* G0 = a.G + (long long)q * 2 * M * M;
-        JT* G1 = G0 + M * M;
-        for (int k = 0; k < M; ++k) {
+        __syncwarp();
+        // J_f at the stage points (the left node's comes with the previous interval of the run)
 #pragma unroll
-            for (int d = 0; d < NCH; ++d) {
-                const int g = ch * NCH + d;
-                if (g >= M) continue;
-                if (k < LA) { G0[k * M + g] = ra[k].d[d]; G1[k * M + g] = JT(0); }
-                else { G1[k * M + g] = rb[k - LA].d[d]; G0[k * M + g] = JT(0); }
+        for (int r = 0; r < S; ++r) {
+            if (LNODE && r == 0 && kk > 0) continue;
+            if (lane < M) {
+                using D1 = Dual<JT, 1>;
+                D1 u[M], du[M];
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    u[m] = D1(Yp[r * M + m]);
+                    u[m].d[0] = m == lane ? JT(1) : JT(0);
+                }
+                bvp_f<D1, JT>(du, u, pj, JT(ti + tab_c(r) * hi));
+                JT* Js = Jm + jslot(r, kk) * M * JLD;
+#pragma unroll
+                for (int m = 0; m < M; ++m) Js[m * JLD + lane] = du[m].d[0];
+            }
+        }
+        __syncwarp();
+        // the stage chain, JW directions per pass; lane m owns row m
+        const JT hj = JT(hi);
+        JT* Sg = a.Sb + (nb + i) * (M * M);
+        JT* Rg = a.Rb + (nb + i) * (M * M);
+#pragma unroll 1
+        for (int p = 0; p < (2 * M + JW - 1) / JW; ++p) {
+            JT dK[S][JW];
+            JT dR[JW];
+#pragma unroll
+            for (int c = 0; c < JW; ++c) dR[c] = JT(0);
+#pragma unroll
+            for (int r = 0; r < S; ++r) {
+                const JT* Jr = Jm + jslot(r, kk) * M * JLD;
+                bool xfree = true;
+#pragma unroll
+                for (int j = 0; j < r; ++j) xfree = xfree && tab_x(r, j) == 0.0;
+                if (xfree) {
+                    // dY_r = (1 - v_r)[I 0] + v_r [0 I]: dK_r is a scaled column of J_r
+#pragma unroll
+                    for (int c = 0; c < JW; ++c) {
+                        const int d = p * JW + c;
+                        JT v = JT(0);
+                        if (lane < M && d < 2 * M)
+                            v = d < M ? JT(1.0 - tab_v(r)) * Jr[lane * JLD + d] : JT(tab_v(r)) * Jr[lane * JLD + d - M];
+                        dK[r][c] = v;
+                    }
+                } else {
+                    if (lane < M) {
+#pragma unroll
+                        for (int c = 0; c < JW; ++c) {
+                            const int d = p * JW + c;
+                            JT v = JT(0);
+                            if (d < M) v = lane == d ? JT(1.0 - tab_v(r)) : JT(0);
+                            else if (d < 2 * M) v = lane == d - M ? JT(tab_v(r)) : JT(0);
+#pragma unroll
+                            for (int j = 0; j < r; ++j)
+                                if (tab_x(r, j) != 0.0) v = v + hj * (dK[j][c] * JT(tab_x(r, j)));
+                            dY[lane * DYLD + c] = v;
+                        }
+                    }
+                    __syncwarp();
+                    JT acc[JW];
+#pragma unroll
+                    for (int c = 0; c < JW; ++c) acc[c] = JT(0);
+                    if (lane < M) {
+#pragma unroll 4
+                        for (int k = 0; k < M; ++k) {
+                            const JT jv = Jr[lane * JLD + k];
+#pragma unroll
+                            for (int c = 0; c < JW; c += 4) {
+                                JT v4[4];
+                                ld4(&dY[k * DYLD + c], v4);
+#pragma unroll
+                                for (int t = 0; t < 4; ++t) acc[c + t] += jv * v4[t];
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < JW; ++c) dK[r][c] = acc[c];
+                    __syncwarp();
+                }
+#pragma unroll
+                for (int c = 0; c < JW; ++c) dR[c] += dK[r][c] * JT(tab_b(r));
+            }
+            if (lane < M) {
+#pragma unroll
+                for (int c = 0; c < JW; ++c) {
+                    const int d = p * JW + c;
+                    if (d < M) Sg[lane * M + d] = (lane == d ? JT(-1) : JT(0)) - hj * dR[c];
+                    else if (d < 2 * M) Rg[lane * M + d - M] = (lane == d - M ? JT(1) : JT(0)) - hj * dR[c];
+                }
             }
         }
     }
@@ -248,15 +404,20 @@ constexpr int RLD = BVP_PAD48(2 * M + 1);  // relation rows [B | A | g]
 constexpr int LLD = BVP_PAD48(M);          // panel factor rows
 constexpr int DLD = 2 * M + 2;             // dense end system rows
 constexpr int WJT = M * RLD + 2 * M * LLD + ((M + 3) / 4) * 4;   // JT elements per warp
-constexpr int WARP_BYTES = ((WJT * int(sizeof(JT)) + 15) / 16) * 16 + ((2 * M * 4 + 15) / 16) * 16;
-constexpr int DENSE_BYTES = ((2 * M * DLD * int(sizeof(JT)) + 15) / 16) * 16;
+constexpr int OFF_IDX = BVP_B16(WJT * int(sizeof(JT)));
+constexpr int OFF_RS = OFF_IDX + BVP_B16(2 * M * 4);
+constexpr int OFF_FS = OFF_RS + BVP_B16(M * M * int(sizeof(JT)));
+constexpr int WARP_BYTES = OFF_FS + BVP_B16(M * 8);
+constexpr int DENSE_BYTES = BVP_B16(2 * M * DLD * int(sizeof(JT)));
 
 struct WarpMem {
-    JT* rel;    // M x RLD
-    JT* lf;     // 2M x LLD: rows 0..M-1 pivot rows (L11 | U11) in pivot order, M..2M-1 L21
-    JT* xs;     // M: the rhs column of U12
-    int* pidx;  // M: physical row of pivot k (top rows 0..M-1, bottom rows M..2M-1)
-    int* qidx;  // M: physical row of unpivoted row u
+    JT* rel;     // M x RLD
+    JT* lf;      // 2M x LLD: rows 0..M-1 pivot rows (L11 | U11) in pivot order, M..2M-1 L21
+    JT* xs;      // M: the rhs column of U12
+    int* pidx;   // M: physical row of pivot k (top rows 0..M-1, bottom rows M..2M-1)
+    int* qidx;   // M: physical row of unpivoted row u
+    JT* rs;      // M x M: the next interval's R block, staged by cp.async
+    double* fs;  // M: its residual F
 };
 BVP_DEV WarpMem warp_mem(unsigned char* base, int w) {
     unsigned char* p = base + (size_t)w * WARP_BYTES;
@@ -264,19 +425,50 @@ BVP_DEV WarpMem warp_mem(unsigned char* base, int w) {
     m.rel = reinterpret_cast<JT*>(p);
     m.lf = m.rel + M * RLD;
     m.xs = m.lf + 2 * M * LLD;
-    m.pidx = reinterpret_cast<int*>(p + ((WJT * int(sizeof(JT)) + 15) / 16) * 16);
+    m.pidx = reinterpret_cast<int*>(p + OFF_IDX);
     m.qidx = m.pidx + M;
+    m.rs = reinterpret_cast<JT*>(p + OFF_RS);
+    m.fs = reinterpret_cast<double*>(p + OFF_FS);
     return m;
 }
 
-// bottom block row: the next interval's Jacobian blocks (global memory)
+// asynchronous global -> shared copies (cp.async, completed by cp_async_wait_all)
+BVP_DEV void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src));
+}
+BVP_DEV void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src));
+}
+BVP_DEV void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src));
+}
+BVP_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+BVP_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// warp-cooperative copy of n bytes (a multiple of 4) in the widest pieces both ends allow
+BVP_DEV void warp_stage(void* dst, const void* src, int n) {
+    char* d = static_cast<char*>(dst);
+    const char* s = static_cast<const char*>(src);
+    const unsigned long long al = reinterpret_cast<unsigned long long>(d) | reinterpret_cast<unsigned long long>(s);
+    if ((al & 15) == 0 && n % 16 == 0) {
+        for (int o = lane_id() * 16; o < n; o += 32 * 16) cp_async16(d + o, s + o);
+    } else if ((al & 7) == 0 && n % 8 == 0) {
+        for (int o = lane_id() * 8; o < n; o += 32 * 8) cp_async8(d + o, s + o);
+    } else {
+        for (int o = lane_id() * 4; o < n; o += 32 * 4) cp_async4(d + o, s + o);
+    }
+}
+
+// bottom block row: the next interval (R block and F staged in shared memory; the S block's
+// rows come in registers from the caller)
 struct BotInterval {
-    const JT* S;
-    const JT* R;
-    const double* F;
-    BVP_DEV JT panel(int u, int j) const { return S[u * M + j]; }
-    BVP_DEV JT hi(int u, int c) const { return R[u * M + c]; }
-    BVP_DEV JT rhs(int u) const { return JT(-F[u]); }
+    const JT* rs;
+    const double* fs;
+    BVP_DEV JT hi(int u, int c) const { return rs[u * M + c]; }
+    BVP_DEV JT rhs(int u) const { return JT(-fs[u]); }
+    BVP_DEV void wait() const {
+        cp_async_wait_all();
+        __syncwarp();
+    }
 };
 // bottom block row: a partner warp's relation [B2 | A2 | g2], whose δ_lo is the shared node
 struct BotRel {
@@ -284,6 +476,10 @@ struct BotRel {
     BVP_DEV JT panel(int u, int j) const { return rl[u * RLD + M + j]; }
     BVP_DEV JT hi(int u, int c) const { return rl[u * RLD + c]; }
     BVP_DEV JT rhs(int u) const { return rl[u * RLD + 2 * M]; }
+    BVP_DEV void wait() const {}
+};
+struct NoPrefetch {
+    BVP_DEV void operator()() const {}
 };
 
 // pivot candidate: |x| for rows still unpivoted (NaN ranks first, so it is chosen and fails
@@ -294,32 +490,21 @@ BVP_DEV JT pivot_cand(JT x, bool live) {
     return v == v ? v : JT(__longlong_as_double(0x7ff0000000000000LL));
 }
 
-// 4 consecutive row entries from shared memory (16-byte aligned when JT is float)
-BVP_DEV void ld4(const JT* p, JT* v) {
-    if constexpr (sizeof(JT) == 4) {
-        const float4 t = *reinterpret_cast<const float4*>(p);
-        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
-    } else {
-        const double2 t0 = *reinterpret_cast<const double2*>(p);
-        const double2 t1 = *reinterpret_cast<const double2*>(p + 2);
-        v[0] = t0.x; v[1] = t0.y; v[2] = t1.x; v[3] = t1.y;
-    }
-}
 
-template <class Bot>
-BVP_DEV bool warp_eliminate(const WarpMem& wm, const Bot& bot, JT* rec) {
+// a1: the bottom block's panel row `lane` (in registers, from the caller). `pre` runs once
+// the panel is factorised (the caller's prefetch of the next panel rows); bot.wait() makes
+// the staged bottom block visible before its first use.
+template <class Bot, class Pre>
+BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* rec, const Pre& pre) {
     constexpr int M4 = ((M + 3) / 4) * 4;
     const int lane = lane_id();
     const bool act = lane < M;
     JT* Rel = wm.rel;
     JT* Lf = wm.lf;
     // 1. panel rows in registers: top row `lane` = B, bottom row `lane` = the new block's
-    JT a0[M], a1[M];
+    JT a0[M];
 #pragma unroll
-    for (int j = 0; j < M; ++j) {
-        a0[j] = act ? Rel[lane * RLD + j] : JT(0);
-        a1[j] = act ? bot.panel(lane, j) : JT(0);
-    }
+    for (int j = 0; j < M; ++j) a0[j] = act ? Rel[lane * RLD + j] : JT(0);
     int st0 = act ? -1 : M, st1 = act ? -1 : M;   // pivot step of each row; -1 while unpivoted
     bool ok = true;
 #pragma unroll
@@ -372,6 +557,8 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, const Bot& bot, JT* rec) {
             if (st1 < 0) wm.qidx[r1 - M] = M + lane;
         }
     }
+    pre();
+    bot.wait();
     __syncwarp();
     // 3. U11 into the record
     if (act) {
@@ -529,10 +716,27 @@ extern "C" __global__ void __launch_bounds__(256) bl_linsolve(const BvpLargeArgs
         }
         for (int r = lane; r < M; r += 32) wm.rel[r * RLD + 2 * M] = JT(-F[(long long)c0 * M + r]);
         __syncwarp();
+        // the next interval's S block rows, one interval ahead of the elimination
+        const bool act = lane < M;
+        JT sp[M];
+        auto load_s = [&](int c) {
+            const JT* S = Sb + (long long)c * M * M + lane * M;
+#pragma unroll
+            for (int j = 0; j < M; ++j) sp[j] = act ? S[j] : JT(0);
+        };
+        if (c0 + 1 < c1) load_s(c0 + 1);
 #pragma unroll 1
         for (int c = c0 + 1; c < c1; ++c) {
-            const BotInterval bot{Sb + (long long)c * M * M, Rb + (long long)c * M * M, F + (long long)c * M};
-            ok &= warp_eliminate(wm, bot, rec + (long long)c * RECW);
+            warp_stage(wm.rs, Rb + (long long)c * M * M, M * M * int(sizeof(JT)));
+            warp_stage(wm.fs, F + (long long)c * M, M * 8);
+            cp_async_commit();
+            JT a1[M];
+#pragma unroll
+            for (int j = 0; j < M; ++j) a1[j] = sp[j];
+            const BotInterval bot{wm.rs, wm.fs};
+            ok &= warp_eliminate(wm, a1, bot, rec + (long long)c * RECW, [&]() {
+                if (c + 1 < c1) load_s(c + 1);
+            });
         }
         if (lane == 0) { s_lo[warp] = c0; s_hi[warp] = c1; }
     }
@@ -542,7 +746,10 @@ extern "C" __global__ void __launch_bounds__(256) bl_linsolve(const BvpLargeArgs
     for (int s = 1; s < NW; s <<= 1) {
         if (warp < NW && (warp % (2 * s)) == 0 && warp + s < NW) {
             const BotRel bot{warp_mem(bl_smem, warp + s).rel};
-            ok &= warp_eliminate(wm, bot, rec + (long long)s_hi[warp] * RECW);
+            JT a1[M];
+#pragma unroll
+            for (int j = 0; j < M; ++j) a1[j] = lane < M ? bot.panel(lane, j) : JT(0);
+            ok &= warp_eliminate(wm, a1, bot, rec + (long long)s_hi[warp] * RECW, NoPrefetch{});
             if (lane == 0) s_hi[warp] = s_hi[warp + s];
         }
         __syncthreads();
@@ -798,7 +1005,8 @@ extern "C" __global__ void bl_layout_probe(int* out) {
     out[0] = int(sizeof(BvpLargeArgs));
     out[1] = bvp::RECW;
     out[2] = bvp::WARP_BYTES;
-    out[3] = bvp::NCHUNK;
+    out[3] = bvp::JWARP_BYTES;
+    out[7] = bvp::JPMAX;
     out[4] = bvp::S;
     out[5] = bvp::NSXA;
     out[6] = bvp::DENSE_BYTES;

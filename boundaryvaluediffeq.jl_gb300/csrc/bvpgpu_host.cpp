@@ -62,6 +62,8 @@ struct bvp_handle_s {
                  kl_defect = nullptr, kl_transfer = nullptr, kl_convert = nullptr, kl_probe = nullptr;
     int l_threads = 256;     // bl_linsolve block size (8 warps; 4 with FP64 blocks)
     size_t l_smem = 0;
+    size_t j_warp_bytes = 0; // bl_jacobian: shared memory per warp, and the parameter staging limit
+    int j_pmax = 0;
     DevBuf d_bcres, d_G, d_lnorm, d_lsq, d_ldnorm, d_lbad, d_active, d_N, d_newN;
     // device arrays
     DevBuf d_mesh, d_h, d_y, d_ybak, d_ybase, d_K, d_KI, d_F, d_err, d_inc, d_iold, d_Sb, d_Rb,
@@ -259,6 +261,8 @@ static bvp_status compile_and_load(bvp_handle* h) {
     return BVP_OK;
 }
 
+static size_t large_jac_smem(const bvp_handle* h);
+
 bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bvp_options* opt,
                       bvp_handle** out) {
     bvp_handle* h = nullptr;
@@ -313,6 +317,10 @@ bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bv
         // per warp: relation, panel factors and pivot indices; plus the dense end system
         h->l_smem = size_t(h->l_threads / 32) * size_t(got[2]) + size_t(got[6]);
         CU(cudaFuncSetAttribute((const void*)h->kl_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, int(h->l_smem)));
+        h->j_warp_bytes = size_t(got[3]);
+        h->j_pmax = got[7];
+        CU(cudaFuncSetAttribute((const void*)h->kl_jac, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(large_jac_smem(h))));
         return BVP_OK;
     }
     // check that host and device agree on the launch ABI
@@ -654,6 +662,13 @@ double bits_to_double(unsigned long long b) {
 }
 }  // namespace
 
+// bl_jacobian's dynamic shared memory: the staged parameters and 4 warps' workspaces
+static size_t large_jac_smem(const bvp_handle* h) {
+    const int P = h->desc.n_params;
+    const size_t pb = P <= h->j_pmax ? (size_t(P) * size_t(h->js) + 15) / 16 * 16 : 0;
+    return pb + 4 * h->j_warp_bytes;
+}
+
 static bvp_status large_run(bvp_handle* h, cudaKernel_t k, dim3 grid, dim3 block, size_t smem, BvpLargeArgs& a,
                             int* mode = nullptr) {
     void* args1[] = {&a};
@@ -889,8 +904,9 @@ static bvp_status solve_large(bvp_handle* h, int n, const double* params, const 
             if (s != BVP_OK) return s;
             {
                 const int mx = maxN_of(step);
-                const long long threads = (long long)mx * ((2 * M + 7) / 8);
-                s = large_run(h, h->kl_jac, dim3(unsigned((threads + 127) / 128), unsigned(step.size())), dim3(128), 0, a);
+                const int runs = (mx - 1 + 7) / 8 + 1;   // runs of 8 intervals, plus the BC warp
+                s = large_run(h, h->kl_jac, dim3(unsigned((runs + 3) / 4), unsigned(step.size())), dim3(128),
+                              large_jac_smem(h), a);
                 if (s != BVP_OK) return s;
                 s = large_run(h, h->kl_solve, dim3(unsigned(step.size())), dim3(unsigned(h->l_threads)), h->l_smem, a);
                 if (s != BVP_OK) return s;
