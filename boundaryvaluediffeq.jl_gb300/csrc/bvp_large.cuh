@@ -65,6 +65,9 @@ BVP_DEV int jslot(int r, int kk) {
     if (LNODE && r == 1) return (kk + 1) & 1;
     return r;
 }
+// correctly rounded reciprocal
+BVP_DEV float rcp_rn(float x) { return __frcp_rn(x); }
+BVP_DEV double rcp_rn(double x) { return __drcp_rn(x); }
 // 4 consecutive entries from shared memory (16-byte aligned)
 BVP_DEV void ld4(const JT* p, JT* v) {
     if constexpr (sizeof(JT) == 4) {
@@ -514,13 +517,25 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* 
         int pr = lane;
         const JT v1 = pivot_cand(a1[k], st1 < 0);
         if (v1 > v) { v = v1; pr = M + lane; }
+        if constexpr (sizeof(JT) == 4) {
+            // one warp reduction on (|v| with its 6 lowest mantissa bits replaced by 63 - row,
+            // offset by 64 so that every live row outranks the pivoted ones, whose key is 0):
+            // the float bits of a non-negative value order like the value, so this selects the
+            // largest magnitude to 17 bits, ties (within 2^-17) to the lower row
+            const unsigned key = v < JT(0) ? 0u : (((__float_as_uint(v) & ~63u) + 64u) | unsigned(63 - pr));
+            const unsigned best = __reduce_max_sync(FULL, key);
+            pr = 63 - int(best & 63u);
+            v = __uint_as_float((best & ~63u) - 64u);
+        } else {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const JT v2 = __shfl_xor_sync(FULL, v, o);
-            const int p2 = __shfl_xor_sync(FULL, pr, o);
-            if (v2 > v || (v2 == v && p2 < pr)) { v = v2; pr = p2; }
+            for (int o = 16; o > 0; o >>= 1) {
+                const JT v2 = __shfl_xor_sync(FULL, v, o);
+                const int p2 = __shfl_xor_sync(FULL, pr, o);
+                if (v2 > v || (v2 == v && p2 < pr)) { v = v2; pr = p2; }
+            }
         }
         ok = ok && v > JT(0) && isfinite(v);
+        pr = pr < 2 * M ? pr : 2 * M - 1;   // always holds (a live row exists at every step)
         const bool pbot = pr >= M;
         const int own = pbot ? pr - M : pr;
         JT prow[M];
@@ -528,18 +543,16 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* 
         for (int j = k; j < M; ++j) prow[j] = __shfl_sync(FULL, pbot ? a1[j] : a0[j], own);
         if (lane == own) { if (pbot) st1 = k; else st0 = k; }
         if (lane == 0) wm.pidx[k] = pr;
-        const JT inv = JT(1) / prow[k];
-        if (st0 < 0) {
-            const JT m = a0[k] * inv;
-            a0[k] = m;
+        const JT inv = rcp_rn(prow[k]);
+        // branch-free update: pivoted rows take a zero multiplier
+        const JT m0 = st0 < 0 ? a0[k] * inv : JT(0);
+        const JT m1 = st1 < 0 ? a1[k] * inv : JT(0);
+        a0[k] = st0 < 0 ? m0 : a0[k];
+        a1[k] = st1 < 0 ? m1 : a1[k];
 #pragma unroll
-            for (int j = k + 1; j < M; ++j) a0[j] -= m * prow[j];
-        }
-        if (st1 < 0) {
-            const JT m = a1[k] * inv;
-            a1[k] = m;
-#pragma unroll
-            for (int j = k + 1; j < M; ++j) a1[j] -= m * prow[j];
+        for (int j = k + 1; j < M; ++j) {
+            a0[j] -= m0 * prow[j];
+            a1[j] -= m1 * prow[j];
         }
     }
     // 2. factor rows to shared memory: pivot rows by step, unpivoted rows compacted
@@ -608,15 +621,19 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* 
         const int c = lane + 32 * s;
         const bool cv = c < 2 * M;
         const bool lo = c < M;
+        // T entries of this column, read branch-free from clamped (always valid) addresses:
+        // top rows carry the δ_lo coefficients, bottom rows the δ_hi ones
+        const int clo = lo ? c : 0;
+        const int chi = (cv && !lo) ? c - M : 0;
+        auto tval = [&](int p) {
+            const JT tv = Rel[(p < M ? p : 0) * RLD + M + clo];
+            const JT bv = bot.hi(p < M ? 0 : p - M, chi);
+            return cv ? (p < M ? (lo ? tv : JT(0)) : (lo ? JT(0) : bv)) : JT(0);
+        };
         JT x[M];
 #pragma unroll
         for (int k = 0; k < M; ++k) {
-            const int p = wm.pidx[k];
-            JT t = JT(0);
-            if (cv) {
-                if (p < M) { if (lo) t = Rel[p * RLD + M + c]; }
-                else if (!lo) t = bot.hi(p - M, c - M);
-            }
+            JT t = tval(wm.pidx[k]);
 #pragma unroll
             for (int j = 0; j < k; j += 4) {
                 JT l4[4];
@@ -630,12 +647,7 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* 
         JT sc[M];
 #pragma unroll
         for (int u = 0; u < M; ++u) {
-            const int qq = wm.qidx[u];
-            JT t = JT(0);
-            if (cv) {
-                if (qq < M) { if (lo) t = Rel[qq * RLD + M + c]; }
-                else if (!lo) t = bot.hi(qq - M, c - M);
-            }
+            JT t = tval(wm.qidx[u]);
 #pragma unroll
             for (int j = 0; j < M4; j += 4) {
                 JT l4[4];
@@ -663,14 +675,15 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* 
 // x = U^{-1} (g - X lo - Y hi) from a record (U, X, Y, g), the warp cooperating (lane r: row r)
 BVP_DEV void warp_back_solve(const JT* rg, const JT* lo, const JT* hi, JT* x_out) {
     const int lane = lane_id();
-    JT t = JT(0);
+    JT t = JT(0), inv = JT(1);
     if (lane < M) {
         t = rg[3 * M * M + lane];
         for (int c = 0; c < M; ++c)
             t -= rg[M * M + lane * M + c] * lo[c] + rg[2 * M * M + lane * M + c] * hi[c];
+        inv = rcp_rn(rg[lane * M + lane]);
     }
     for (int r = M - 1; r >= 0; --r) {
-        const JT xr = __shfl_sync(FULL, t / (lane < M ? rg[lane * M + lane] : JT(1)), r);
+        const JT xr = __shfl_sync(FULL, t * inv, r);
         if (lane == r) t = xr;
         if (lane < r) t -= rg[lane * M + r] * xr;
     }

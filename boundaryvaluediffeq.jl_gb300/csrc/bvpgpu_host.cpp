@@ -60,8 +60,10 @@ struct bvp_handle_s {
     bool large = false;
     cudaKernel_t kl_res = nullptr, kl_jac = nullptr, kl_solve = nullptr, kl_update = nullptr, kl_copy = nullptr,
                  kl_defect = nullptr, kl_transfer = nullptr, kl_convert = nullptr, kl_probe = nullptr;
-    int l_threads = 256;     // bl_linsolve block size (8 warps; 4 with FP64 blocks)
+    int l_threads = 256;     // bl_linsolve block size, picked by large_tune_linsolve
     size_t l_smem = 0;
+    size_t l_warp_bytes = 0, l_dense_bytes = 0;
+    bool l_tuned = false;
     size_t j_warp_bytes = 0; // bl_jacobian: shared memory per warp, and the parameter staging limit
     int j_pmax = 0;
     DevBuf d_bcres, d_G, d_lnorm, d_lsq, d_ldnorm, d_lbad, d_active, d_N, d_newN;
@@ -313,9 +315,19 @@ bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bv
         cudaFree(probe.p);
         if (got[0] != int(sizeof(BvpLargeArgs)) || got[1] != h->L.RECW || got[4] != h->L.S || got[5] != h->L.NSXA)
             return fail(h, BVP_ERR_STATE, "host/device layout mismatch (larger-state kernels)");
-        h->l_threads = h->js == 8 ? 128 : 256;
-        // per warp: relation, panel factors and pivot indices; plus the dense end system
-        h->l_smem = size_t(h->l_threads / 32) * size_t(got[2]) + size_t(got[6]);
+        // per warp: relation, panel factors, pivot indices and the staged block; plus the
+        // dense end system. Up to 8 warps as fit in the SM's shared memory; the block size is
+        // tuned on the first solve (large_tune_linsolve).
+        h->l_warp_bytes = size_t(got[2]);
+        h->l_dense_bytes = size_t(got[6]);
+        int max_smem = 0, dev = 0;
+        CU(cudaGetDevice(&dev));
+        CU(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        int wmax = int((size_t(max_smem) - h->l_dense_bytes) / h->l_warp_bytes);
+        wmax = std::min(wmax, 8);
+        if (wmax < 3) return fail(h, BVP_ERR_STATE, "larger-state linear solve: shared memory too small");
+        h->l_threads = 32 * wmax;
+        h->l_smem = size_t(wmax) * h->l_warp_bytes + h->l_dense_bytes;
         CU(cudaFuncSetAttribute((const void*)h->kl_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, int(h->l_smem)));
         h->j_warp_bytes = size_t(got[3]);
         h->j_pmax = got[7];
@@ -670,6 +682,43 @@ static size_t large_jac_smem(const bvp_handle* h) {
 }
 
 static bvp_status large_run(bvp_handle* h, cudaKernel_t k, dim3 grid, dim3 block, size_t smem, BvpLargeArgs& a,
+                            int* mode);
+
+// Autotuner of the linear solve's block size (warps per instance = chunks of the mesh): on
+// the first Newton step of the handle, every candidate from 3 warps up to the largest that
+// fits is timed on the step's own systems (the solve reads the Jacobian blocks and the
+// residual and writes only the step and its elimination records, so rerunning it is
+// harmless), and the fastest is kept for the handle's life. Fewer warps per instance let
+// more instances share an SM; more warps shorten each instance's chain of eliminations.
+static bvp_status large_tune_linsolve(bvp_handle* h, BvpLargeArgs& a, int n_active) {
+    const int wmax = h->l_threads / 32;
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    float best = 0.0f;
+    int best_w = wmax;
+    for (int rep = 0; rep < 2; ++rep) {   // the first pass warms up
+        for (int w = 3; w <= wmax; ++w) {
+            const size_t smem = size_t(w) * h->l_warp_bytes + h->l_dense_bytes;
+            CU(cudaEventRecord(e0, h->stream));
+            bvp_status s = large_run(h, h->kl_solve, dim3(unsigned(n_active)), dim3(unsigned(32 * w)), smem, a, nullptr);
+            if (s != BVP_OK) return s;
+            CU(cudaEventRecord(e1, h->stream));
+            CU(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            CU(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep == 1 && (w == 3 || ms < best)) { best = ms; best_w = w; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->l_threads = 32 * best_w;
+    h->l_smem = size_t(best_w) * h->l_warp_bytes + h->l_dense_bytes;
+    h->l_tuned = true;
+    return BVP_OK;
+}
+
+static bvp_status large_run(bvp_handle* h, cudaKernel_t k, dim3 grid, dim3 block, size_t smem, BvpLargeArgs& a,
                             int* mode = nullptr) {
     void* args1[] = {&a};
     void* args2[] = {&a, mode};
@@ -908,6 +957,10 @@ static bvp_status solve_large(bvp_handle* h, int n, const double* params, const 
                 s = large_run(h, h->kl_jac, dim3(unsigned((runs + 3) / 4), unsigned(step.size())), dim3(128),
                               large_jac_smem(h), a);
                 if (s != BVP_OK) return s;
+                if (!h->l_tuned) {
+                    s = large_tune_linsolve(h, a, int(step.size()));
+                    if (s != BVP_OK) return s;
+                }
                 s = large_run(h, h->kl_solve, dim3(unsigned(step.size())), dim3(unsigned(h->l_threads)), h->l_smem, a);
                 if (s != BVP_OK) return s;
             }
@@ -1381,6 +1434,12 @@ bvp_status bvp_dense_output(bvp_handle* h, int32_t nq, const double* tq, int32_t
     cudaFree(dt.p);
     cudaFree(dout.p);
     return s;
+}
+
+bvp_status bvp_get_tuning(bvp_handle* h, int32_t* threads) {
+    if (!h || !threads) return BVP_ERR_INVALID;
+    threads[0] = (h->large && h->l_tuned) ? h->l_threads : 0;
+    return BVP_OK;
 }
 
 bvp_status bvp_last_timing(bvp_handle* h, double* ms2) {

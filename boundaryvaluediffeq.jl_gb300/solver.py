@@ -221,6 +221,12 @@ class BatchSolver:
         self._check(self.lib.bvp_last_timing(self.h, f64(t)), "bvp_last_timing")
         return float(t[0]), float(t[1])
 
+    def tuning(self) -> dict:
+        """Launch shapes the library's autotuner picked for this handle."""
+        t = np.zeros(1, np.int32)
+        self._check(self.lib.bvp_get_tuning(self.h, i32(t)), "bvp_get_tuning")
+        return {"linsolve_threads": int(t[0])}
+
     def stream_ptr(self) -> int:
         return int(self.lib.bvp_stream(self.h) or 0)
 

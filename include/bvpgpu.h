@@ -228,6 +228,11 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n_inst, int
  * stream): [0] whole solve, [1] fused solve kernel. */
 bvp_status bvp_last_timing(bvp_handle* h, double* ms2);
 
+/* Launch shapes the handle's autotuner picked (no reference counterpart: the reference runs
+ * on the CPU). threads[0]: block size of the larger-state linear solve (0 until the first
+ * Newton step of a state dimension above 8 has run). */
+bvp_status bvp_get_tuning(bvp_handle* h, int32_t* threads);
+
 /* The handle's CUDA stream (cudaStream_t as void*). */
 void* bvp_stream(bvp_handle* h);
 
