@@ -494,6 +494,20 @@ BVP_DEV JT pivot_cand(JT x, bool live) {
 }
 
 
+// a register row of M values to global memory (16-byte stores when aligned)
+BVP_DEV void store_row(JT* dst, const JT (&x)[M]) {
+    if constexpr (sizeof(JT) == 4 && M % 4 == 0) {
+        if ((reinterpret_cast<unsigned long long>(dst) & 15) == 0) {
+#pragma unroll
+            for (int k = 0; k < M; k += 4)
+                *reinterpret_cast<float4*>(dst + k) = make_float4(x[k], x[k + 1], x[k + 2], x[k + 3]);
+            return;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < M; ++k) dst[k] = x[k];
+}
+
 // a1: the bottom block's panel row `lane` (in registers, from the caller). `pre` runs once
 // the panel is factorised (the caller's prefetch of the next panel rows); bot.wait() makes
 // the staged bottom block visible before its first use.
@@ -573,9 +587,12 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* 
     pre();
     bot.wait();
     __syncwarp();
-    // 3. U11 into the record
-    if (act) {
-        for (int k = 0; k < M; ++k) rec[k * M + lane] = Lf[k * LLD + lane];
+    // 3. U11 into the record, transposed (UT[j][k] = U[k][j]): each pivot row's owner writes
+    //    its row as a column (the entries below the diagonal are multipliers, never read)
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+        if (act && st0 >= 0) rec[j * M + st0] = a0[j];
+        if (act && st1 >= 0) rec[j * M + st1] = a1[j];
     }
     // 4. rhs column: forward substitution row-parallel (lane k owns pivot row k), then the
     //    Schur rows (lane u owns unpivoted row u)
@@ -660,9 +677,8 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* 
         }
         __syncwarp();
         if (cv) {
-            JT* rx = rec + (lo ? M * M + c : 2 * M * M + c - M);
-#pragma unroll
-            for (int k = 0; k < M; ++k) rx[k * M] = x[k];
+            // column c of U12 is row c of XT (δ_lo) or row c - M of YT (δ_hi)
+            store_row(rec + (lo ? M * M + c * M : 2 * M * M + (c - M) * M), x);
             const int dc = lo ? M + c : c - M;
 #pragma unroll
             for (int u = 0; u < M; ++u) Rel[u * RLD + dc] = sc[u];
@@ -672,24 +688,30 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* 
     return ok;
 }
 
-// x = U^{-1} (g - X lo - Y hi) from a record (U, X, Y, g), the warp cooperating (lane r: row r)
-BVP_DEV void warp_back_solve(const JT* rg, const JT* lo, const JT* hi, JT* x_out) {
+// x = U^{-1} (g - X lo - Y hi) from an elimination record [UT | XT | YT | g] (blocks stored
+// transposed, so lane r's reads of row r are coalesced across the warp); lane c holds lo[c]
+// and hi[c] on entry, lane r returns x[r]
+BVP_DEV JT warp_back_solve(const JT* rg, JT lo_l, JT hi_l) {
     const int lane = lane_id();
-    JT t = JT(0), inv = JT(1);
-    if (lane < M) {
-        t = rg[3 * M * M + lane];
-        for (int c = 0; c < M; ++c)
-            t -= rg[M * M + lane * M + c] * lo[c] + rg[2 * M * M + lane * M + c] * hi[c];
-        inv = rcp_rn(rg[lane * M + lane]);
+    const bool act = lane < M;
+    const int l = act ? lane : 0;
+    JT t = rg[3 * M * M + l];
+#pragma unroll
+    for (int c = 0; c < M; ++c) {
+        const JT loc = __shfl_sync(FULL, lo_l, c);
+        const JT hic = __shfl_sync(FULL, hi_l, c);
+        t -= rg[M * M + c * M + l] * loc + rg[2 * M * M + c * M + l] * hic;
     }
+    const JT inv = rcp_rn(rg[l * M + l]);
+#pragma unroll
     for (int r = M - 1; r >= 0; --r) {
         const JT xr = __shfl_sync(FULL, t * inv, r);
-        if (lane == r) t = xr;
-        if (lane < r) t -= rg[lane * M + r] * xr;
+        const JT ur = rg[r * M + l];   // U[lane][r]
+        t = lane == r ? xr : (lane < r ? t - ur * xr : t);
     }
-    if (lane < M) x_out[lane] = t;
-    __syncwarp();
+    return act ? t : JT(0);
 }
+
 
 }  // namespace bvp
 
@@ -848,17 +870,23 @@ extern "C" __global__ void __launch_bounds__(256) bl_linsolve(const BvpLargeArgs
             const int lo = s_lo[warp];
             const int mid = s_lo[warp + s];
             const int hi = s_hi[warp + s];
-            JT* xm = dl + (long long)mid * M;
-            warp_back_solve(rec + (long long)mid * RECW, dl + (long long)lo * M, dl + (long long)hi * M, xm);
+            const JT lo_l = lane < M ? dl[(long long)lo * M + lane] : JT(0);
+            const JT hi_l = lane < M ? dl[(long long)hi * M + lane] : JT(0);
+            const JT x = warp_back_solve(rec + (long long)mid * RECW, lo_l, hi_l);
+            if (lane < M) dl[(long long)mid * M + lane] = x;
+            __syncwarp();
         }
         __syncthreads();
     }
     // 5. back substitution inside each chunk (the chunk ends are known)
     if (warp < NW) {
-        const int lo = c0;
-        for (int c = c1 - 1; c > c0; --c)
-            warp_back_solve(rec + (long long)c * RECW, dl + (long long)lo * M, dl + (long long)(c + 1) * M,
-                            dl + (long long)c * M);
+        const JT lo_l = lane < M ? dl[(long long)c0 * M + lane] : JT(0);
+        JT hi_l = lane < M ? dl[(long long)c1 * M + lane] : JT(0);
+#pragma unroll 1
+        for (int c = c1 - 1; c > c0; --c) {
+            hi_l = warp_back_solve(rec + (long long)c * RECW, lo_l, hi_l);
+            if (lane < M) dl[(long long)c * M + lane] = hi_l;
+        }
     }
     if (!ok && lane == 0) atomicExch(&s_bad, 1);
     __syncthreads();
