@@ -99,7 +99,8 @@ def nvrtc_check(problem, order: int, jac_bits: int = 32) -> None:
     opts = ["--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true", f"-DBVP_M={problem.M}",
             f"-DBVP_ORDER={order}", f"-DBVP_TWOPOINT={int(problem.twopoint)}", f"-DBVP_NBC={nbc}",
             f"-DBVP_LA={problem.La if problem.twopoint else 0}",
-            "-DBVP_JT=" + ("double" if jac_bits == 64 else "float")]
+            "-DBVP_JT=" + ("double" if jac_bits == 64 else "float"),
+            f"-DBVP_SINGULAR={int('BVP_SING' in problem.source)}"]
     names = [fn.encode() for fn in EMBED]
     bodies = [open(os.path.join(CSRC, fn), "rb").read() for fn in EMBED]
     prog = C.c_void_p()
@@ -142,7 +143,7 @@ def build_library(verbose: bool = False, force: bool = False, check_problems=Non
                     os.path.join(CSRC, "bvp_mlp.cu"), "-o", tmp, "-lnvrtc", "-ldl"]
         jobs.append(subprocess.Popen(host_cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
         checks = check_problems if check_problems is not None else [
-            (P.PENDULUM, 4, 0), (P.SINGULAR_PERTURBATION, 6, 0), (P.NONLINEAR32, 4, 0)]
+            (P.PENDULUM, 4, 0), (P.SINGULAR_PERTURBATION, 6, 0), (P.NONLINEAR32, 4, 0), (P.LANE_EMDEN, 4, 0)]
         check_cmds = []
         for prob, order, nbc_dummy in checks:
             src = os.path.join(BUILD, f"check_{prob.name}_o{order}.cu")
@@ -151,7 +152,8 @@ def build_library(verbose: bool = False, force: bool = False, check_problems=Non
             nbc = 2 if prob.twopoint else len(prob.bc_t)
             cmd = [NVCC, "-cubin", ARCH, "-std=c++17", "-lineinfo", "-O3", "-Xptxas", "-v",
                    f"-DBVP_M={prob.M}", f"-DBVP_ORDER={order}", f"-DBVP_TWOPOINT={int(prob.twopoint)}",
-                   f"-DBVP_NBC={nbc}", f"-DBVP_LA={prob.La}", "-DBVP_JT=float", "-I", CSRC, src,
+                   f"-DBVP_NBC={nbc}", f"-DBVP_LA={prob.La}", "-DBVP_JT=float",
+                   f"-DBVP_SINGULAR={int('BVP_SING' in prob.source)}", "-I", CSRC, src,
                    "-o", os.path.join(BUILD, f"check_{prob.name}_o{order}.cubin")]
             check_cmds.append((cmd, os.path.join(BUILD, f"ptxas_{prob.name}_o{order}.txt")))
             jobs.append(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))

@@ -190,6 +190,25 @@ template <class T, class PT> BVP_DEV void call_f(T* du, const T* u, const PT* p,
 #endif
     bvp_f<T, PT>(du, u, p, t);
 }
+#ifndef BVP_SINGULAR
+#define BVP_SINGULAR 0
+#endif
+// A collocation stage: f plus the singular term S u / t for t > 0 (collocation.jl:60-66 with
+// __add_singular_term!, Core/src/utils.jl:936-941). The interpolant's extra stages and the
+// defect evaluate f alone, as the reference does (interpolation.jl:337-372,
+// adaptivity.jl:416-461).
+template <class T, class PT> BVP_DEV void call_stage_f(T* du, const T* u, const PT* p, PT t) {
+    call_f<T, PT>(du, u, p, t);
+#if BVP_SINGULAR
+    if (t > PT(0)) {
+        T su[M];
+        bvp_sing<T, PT>(su, u, p);
+        const PT it = PT(1) / t;
+#pragma unroll
+        for (int m = 0; m < M; ++m) du[m] = du[m] + su[m] * it;
+    }
+#endif
+}
 
 // MIRK4/5/6 put their first two stages on the mesh nodes (c = v = 0 and c = v = 1, no x
 // terms): K_1 of interval i is f(y_i, t_i) and K_2 is f(y_{i+1}, t_{i+1}), which is K_1 of
@@ -215,7 +234,7 @@ BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, 
             continue;
         }
         if (NODE_SHARE && r == 1 && node) {
-            call_f<T, PT>(&Ki[M], yi1, p, PT(ti1));
+            call_stage_f<T, PT>(&Ki[M], yi1, p, PT(ti1));
 #pragma unroll
             for (int m = 0; m < M; ++m) node[m] = Ki[M + m];
             continue;
@@ -229,7 +248,7 @@ BVP_DEV void phi_interval(const T* yi, const T* yi1, T* Ki, T* ri, const PT* p, 
                 for (int m = 0; m < M; ++m) Y[m] = Y[m] + hi * (Ki[j * M + m] * PT(tab_x(r, j)));
             }
         }
-        call_f<T, PT>(&Ki[r * M], Y, p, PT(ti + TT(tab_c(r)) * hi_d));
+        call_stage_f<T, PT>(&Ki[r * M], Y, p, PT(ti + TT(tab_c(r)) * hi_d));
     }
 #pragma unroll
     for (int m = 0; m < M; ++m) {
@@ -388,7 +407,7 @@ BVP_DEV double residual(const Args& a, const Inst& I) {
         R y0v[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) y0v[m] = y_at<R>(a, I, i0 * M + m);
-        call_f<R, R>(node, y0v, pr, sizeof(R) == 8 ? R(mesh[i0]) : R(a.tj[I.nb + i0]));
+        call_stage_f<R, R>(node, y0v, pr, sizeof(R) == 8 ? R(mesh[i0]) : R(a.tj[I.nb + i0]));
     }
     const double* y64 = y_of(a, I, I.cur);
     // interior BC points: the lane whose block holds the interval evaluates the
@@ -945,7 +964,7 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
             DI y0v[M];
 #pragma unroll
             for (int m = 0; m < M; ++m) { y0v[m] = DI(yj[blo * M + m]); y0v[m].d[m] = JT(1); }
-            if (NODE_SHARE) call_f<DI, JT>(node, y0v, I.pj, tj[blo]);
+            if (NODE_SHARE) call_stage_f<DI, JT>(node, y0v, I.pj, tj[blo]);
         }
 #pragma unroll 1
         for (int c = blo; c < bhi; ++c) {

@@ -84,6 +84,25 @@ static_assert(M <= 32 && M > 0, "M <= 32");
 BVP_DEV int lane_id() { return threadIdx.x & 31; }
 BVP_DEV unsigned long long norm_bits(double v) { return (unsigned long long)__double_as_longlong(v); }
 
+#ifndef BVP_SINGULAR
+#define BVP_SINGULAR 0
+#endif
+// A collocation stage: f plus the singular term S u / t for t > 0 (collocation.jl:60-66 with
+// __add_singular_term!, Core/src/utils.jl:936-941); the interpolant's extra stages and the
+// defect evaluate f alone, as the reference does.
+template <class T, class PT> BVP_DEV void stage_f(T* du, const T* u, const PT* p, PT t) {
+    bvp_f<T, PT>(du, u, p, t);
+#if BVP_SINGULAR
+    if (t > PT(0)) {
+        T su[M];
+        bvp_sing<T, PT>(su, u, p);
+        const PT it = PT(1) / t;
+#pragma unroll
+        for (int m = 0; m < M; ++m) du[m] = du[m] + su[m] * it;
+    }
+#endif
+}
+
 // stages and residual of one interval (collocation.jl:44-72), the expression order of the
 // warp-per-instance kernels
 template <class T, class PT, class TT>
@@ -101,7 +120,7 @@ BVP_DEV void phi_large(const T* yi, const T* yi1, T* K, T* r, const PT* p, TT ti
                 for (int m = 0; m < M; ++m) Y[m] = Y[m] + hi * (K[j * M + m] * PT(tab_x(rr, j)));
             }
         }
-        bvp_f<T, PT>(&K[rr * M], Y, p, PT(ti + TT(tab_c(rr)) * hi_t));
+        stage_f<T, PT>(&K[rr * M], Y, p, PT(ti + TT(tab_c(rr)) * hi_t));
     }
 #pragma unroll 4
     for (int m = 0; m < M; ++m) {
@@ -299,7 +318,7 @@ extern "C" __global__ void __launch_bounds__(128) bl_jacobian(const BvpLargeArgs
                     u[m] = D1(Yp[r * M + m]);
                     u[m].d[0] = m == lane ? JT(1) : JT(0);
                 }
-                bvp_f<D1, JT>(du, u, pj, JT(ti + tab_c(r) * hi));
+                stage_f<D1, JT>(du, u, pj, JT(ti + tab_c(r) * hi));
                 JT* Js = Jm + jslot(r, kk) * M * JLD;
 #pragma unroll
                 for (int m = 0; m < M; ++m) Js[m * JLD + lane] = du[m].d[0];

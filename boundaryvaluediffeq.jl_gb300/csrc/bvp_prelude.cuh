@@ -17,6 +17,10 @@
     template <class T, class P> BVP_DEV void bvp_bca(T* res, const T* ua, const P* p)
 #define BVP_BCB \
     template <class T, class P> BVP_DEV void bvp_bcb(T* res, const T* ub, const P* p)
+// optional: S u for the singular term S y / t of y' = S y / t + f(t, y) (a source that
+// defines BVP_SING is compiled with BVP_SINGULAR=1)
+#define BVP_SING \
+    template <class T, class P> BVP_DEV void bvp_sing(T* su, const T* u, const P* p)
 
 namespace bvp {
 

@@ -204,6 +204,8 @@ static bvp_status compile_and_load(bvp_handle* h) {
         "-DBVP_NBC=" + std::to_string(d.twopoint ? 2 : d.n_bc_pts),
         "-DBVP_LA=" + std::to_string(d.twopoint ? d.La : 0),
         std::string("-DBVP_JT=") + (o.jac_precision == 64 ? "double" : "float"),
+        // a source with BVP_SING has a singular term S y / t (the problem's singular_term)
+        std::string("-DBVP_SINGULAR=") + (h->source.find("BVP_SING") != std::string::npos ? "1" : "0"),
     };
     const bool large = d.M > 8;
     const std::string src = std::string("#include \"bvp_prelude.cuh\"\n#line 1 \"problem_source\"\n") +

@@ -142,6 +142,29 @@ BVP_BCB { res[0] = ub[0]; }
     twopoint=True, La=1, Lb=1, tspan=(0.0, 5.0), u0=(5.0, -3.5))
 
 
+# Lane-Emden equation of index 1, y'' + (2/t) y' + y = 0, y(0) = 1, y(1) = sin(1), written as
+# u' = S u / t + f(t, u) with u = (y, y'), f = (u2, -u1), S = [[0, 0], [0, -2]] (the problem the
+# reference's singular-BVP test describes, lib/BoundaryValueDiffEqMIRK/test/Core/
+# singular_bvp_tests.jl:14-50); exact solution y = sin(t)/t
+LANE_EMDEN = Problem(
+    name="lane_emden", M=2, n_params=0,
+    source="""
+BVP_F { du[0] = u[1]; du[1] = -u[0]; }
+BVP_SING { su[0] = T(P(0.0)); su[1] = u[1] * P(-2.0); }
+BVP_BCA { res[0] = ua[0] - P(1.0); }
+BVP_BCB { res[0] = ub[0] - P(0.8414709848078965); }
+""",
+    twopoint=True, La=1, Lb=1, tspan=(0.0, 1.0), u0=(1.0, 0.0))
+
+
+def lane_emden_analytic(t):
+    t = np.asarray(t, dtype=np.float64)
+    ts = np.where(t == 0, 1.0, t)
+    y = np.where(t == 0, 1.0, np.sin(ts) / ts)
+    yp = np.where(t == 0, 0.0, (ts * np.cos(ts) - np.sin(ts)) / ts ** 2)
+    return np.stack([y, yp], -1)
+
+
 def linear_analytic(t):
     t = np.asarray(t, dtype=np.float64)
     cot5 = math.cos(5.0) / math.sin(5.0)
@@ -252,5 +275,5 @@ def nonlinear32_family(n: int, seed: int = 2026, n_intervals: int = 1024, dim: i
     return params, nint, tspans, y0
 
 
-ALL = {p.name: p for p in (PENDULUM, SINGULAR_PERTURBATION, NONLINEAR32, AFFINE, AFFINE_TWOPOINT,
+ALL = {p.name: p for p in (PENDULUM, SINGULAR_PERTURBATION, NONLINEAR32, LANE_EMDEN, AFFINE, AFFINE_TWOPOINT,
                            LINEAR, LINEAR_TWOPOINT, TWOPOINT_INTERP, MULTIPOINT, TORUS, ENSEMBLE)}

@@ -152,7 +152,18 @@ struct InstanceSolver {
                 if (tb.x[r][j] == 0) continue;
                 for (int m = 0; m < M; ++m) Y[m] = Y[m] + hi * (Ki[j * M + m] * tb.x[r][j]);
             }
-            bvp_f<T, double>(&Ki[r * M], Y, p, mesh[i] + tb.c[r] * hi);
+            const double tr = mesh[i] + tb.c[r] * hi;
+            bvp_f<T, double>(&Ki[r * M], Y, p, tr);
+#if BVP_SINGULAR
+            // K_r += S Y_r / t_r for t_r > 0 (collocation.jl:60-66 via __add_singular_term!,
+            // Core/src/utils.jl:936-941); only the collocation stages carry the term
+            if (tr > 0.0) {
+                T su[M];
+                bvp_sing<T, double>(su, Y, p);
+                const double it = 1.0 / tr;
+                for (int m = 0; m < M; ++m) Ki[r * M + m] = Ki[r * M + m] + su[m] * it;
+            }
+#endif
         }
         for (int m = 0; m < M; ++m) {
             T acc = T(0.0);

@@ -56,7 +56,8 @@ def _compile(source: str, M: int, twopoint: bool) -> str:
             h.update(f.read())
     h.update(source.encode())
     trace = bool(os.environ.get("BVP_ORACLE_TRACE"))
-    h.update(f"M={M};tp={int(twopoint)};trace={int(trace)}".encode())
+    sing = "BVP_SING" in source
+    h.update(f"M={M};tp={int(twopoint)};trace={int(trace)};sing={int(sing)}".encode())
     key = h.hexdigest()[:20]
     os.makedirs(_BUILD, exist_ok=True)
     so = os.path.join(_BUILD, f"oracle_{key}.so")
@@ -68,7 +69,7 @@ def _compile(source: str, M: int, twopoint: bool) -> str:
     tmp = so + f".tmp{os.getpid()}"
     cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
            f"-DBVP_M={M}", f"-DBVP_TWOPOINT={int(twopoint)}",
-           f'-DBVP_PROBLEM_HEADER="{hdr}"', "-I", _HERE,
+           f"-DBVP_SINGULAR={int(sing)}", f'-DBVP_PROBLEM_HEADER="{hdr}"', "-I", _HERE,
            os.path.join(_HERE, "oracle_entry.cpp"), "-o", tmp] + (["-DBVP_TRACE"] if trace else [])
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     os.replace(tmp, so)

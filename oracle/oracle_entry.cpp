@@ -22,6 +22,8 @@ using oracle::Dual;
 #define BVP_BC template <class T, class P> inline void bvp_bc(T* res, const T* const* ua, const P* p)
 #define BVP_BCA template <class T, class P> inline void bvp_bca(T* res, const T* ua, const P* p)
 #define BVP_BCB template <class T, class P> inline void bvp_bcb(T* res, const T* ub, const P* p)
+// optional singular term S u of y' = S y / t + f(t, y) (the problem's singular_term)
+#define BVP_SING template <class T, class P> inline void bvp_sing(T* su, const T* u, const P* p)
 
 #ifndef BVP_M
 #error "BVP_M must be defined"

@@ -218,3 +218,30 @@ def test_invalid_arguments_rejected(pkg, problems):
         sv.solve(np.zeros((1, 3)), [0], [[0, 1.0]], [[0, 0]])     # no intervals
     with pytest.raises(pkg.BVPError):
         sv.solve(np.zeros((1, 3)), [8], [[1.0, 1.0]], [[0, 0]])   # empty tspan
+
+
+@pytest.mark.parametrize("jac_precision", [64, 32])
+def test_singular_term_matches_oracle(pkg, problems, jac_precision):
+    # Lane-Emden with its singular term (MIRK4, MIRK6, fixed and adaptive meshes): the GPU
+    # reproduces the oracle's retcode, rounds and final mesh; FP64 mode agrees point by point
+    # within max(abstol, 1e-9 |u|), FP32 mode passes the reference's acceptance test (the FP64
+    # residual of the returned solution, evaluated by the oracle, within abstol)
+    p = problems.LANE_EMDEN
+    o = _oracle(p)
+    params = np.zeros((1, 0))
+    y0 = np.array([p.u0])
+    for order in (4, 6):
+        for adaptive in (0, 1):
+            sv = pkg.BatchSolver(p, order=order, jac_precision=jac_precision, adaptive=adaptive)
+            res = sv.solve(params, [100], [[0.0, 1.0]], y0)
+            ref = o.solve_batch(params, [100], [[0.0, 1.0]], y0, order=order, adaptive=adaptive)
+            assert res.retcode[0] == ref["retcode"][0]
+            assert res.n_nodes[0] == ref["n_nodes"][0]
+            assert res.rounds[0] == ref["rounds"][0]
+            same, errs = _parity_report(res, ref)
+            assert same[0]
+            if jac_precision == 64:
+                assert errs[0] <= 1e-6, (order, adaptive, errs[0])
+            elif res.retcode[0] == RET_SUCCESS:
+                m, y = res.solution(0)
+                assert o.residual(params[0], m, y, order=order)[2] <= 1e-6 * (1 + 1e-6)

@@ -154,3 +154,26 @@ def test_pendulum_reference_config(problems):
     assert sol.success
     assert abs(sol.sol(0.0)[0] - y[0, 0]) < 1e-4
     assert abs(sol.sol(0.0)[1] - y[0, 1]) < 1e-4
+
+
+@pytest.mark.parametrize("order", (3, 4, 5, 6))
+def test_singular_term_lane_emden(problems, order):
+    # the singular term S y / t (Core/src/utils.jl:925-941) enters the collocation stages for
+    # t > 0 (collocation.jl:60-66). Lane-Emden y'' + (2/t) y' + y = 0 (singular_bvp_tests.jl:14-50)
+    # on fixed meshes converges to y = sin(t)/t; the stage at t = 0 lacks the term's limit, so the
+    # order is one. (The reference test builds its problem without passing singular_term, so it
+    # pins no value for this path.)
+    p = problems.LANE_EMDEN
+    errs = []
+    for n in (100, 200, 400):
+        o, r, N = _solve1(p, n=n, order=order, adaptive=0)
+        assert r["retcode"][0] == RET_SUCCESS
+        m, y = r["mesh"][0, :N], r["y"][0, :N]
+        errs.append(np.abs(y - problems.lane_emden_analytic(m)).max())
+    assert errs[0] < 1e-3
+    for e0, e1 in zip(errs, errs[1:]):
+        assert 1.6 < e0 / e1 < 2.5, errs
+    # adaptive: the defect (adaptivity.jl:416-461) evaluates f without the singular term, so the
+    # estimate stays above the 10% threshold and the mesh halves until it exceeds the cap
+    o, r, N = _solve1(p, n=100, order=order)
+    assert r["retcode"][0] != RET_SUCCESS and N > 1000
