@@ -224,6 +224,90 @@ GRID = 64
 EPOCHS = 40
 
 
+# The other configurations of the metric (parity cases; each prints its own line, the default
+# run is the pendulum batch above): name -> (description, problem, order, family builder)
+WORKLOADS = {
+    "pendulum1": "single simple pendulum (g 9.81, BCs theta(pi/4) = -pi/2, theta(pi/2) = pi/2), MIRK4, "
+                 "dt 0.05 -> 32 intervals, guess (pi/2, pi/2)",
+    "singular": "singularly perturbed eps y'' + y' + y = 0 x1024, y(0) = 1, y(1) = 0, eps log-uniform "
+                "[1e-3, 1e-1], MIRK6, log-uniform 512..4096 intervals, max_subintervals 3000",
+    "nonlinear32": "coupled nonlinear n = 32 u' = A u + tanh(B u) + c x256, separated BCs, MIRK4, "
+                   "1024 intervals, guess 0",
+}
+
+
+def _workload_inputs(P, name, n):
+    import math as _m
+    if name == "pendulum1":
+        params = np.tile([[9.81, 0.0, 0.0]], (n, 1))
+        return P.PENDULUM, 4, (params, np.full(n, 32, np.int32), np.tile([0.0, _m.pi / 2], (n, 1)),
+                               np.tile([_m.pi / 2, _m.pi / 2], (n, 1)))
+    if name == "singular":
+        return P.SINGULAR_PERTURBATION, 6, P.singular_perturbation_family(n)
+    return P.NONLINEAR32, 4, P.nonlinear32_family(n)
+
+
+def run_workload(args):
+    """One of the other configurations, solved through the Python face of the C ABI with host
+    buffers (copies in and results out inside the timed region, like e2e); the CPU oracle
+    (all host threads) times a bounded sample of the same instances."""
+    ws, rank = _dist()
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    P = pkg.problems
+    name = args.workload
+    n = args.instances if args.instances != N_INST else {"pendulum1": 1, "singular": 1024, "nonlinear32": 256}[name]
+    prob, order, (params, nint, tsp, y0) = _workload_inputs(P, name, n)
+    sv = pkg.BatchSolver(prob, order=order, abstol=1e-6, jac_precision=args.jac_precision)
+    for _ in range(args.warmup):
+        res = sv.solve(params, nint, tsp, y0)
+    _barrier(ws)
+    times = []
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = sv.solve(params, nint, tsp, y0)
+            times.append(time.perf_counter() - t0)
+    tot = _max_over_ranks(sum(times), ws)
+    value = n * ws * args.steps / tot
+    if rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 residual/defect, " + ("f32" if args.jac_precision == 32 else "f64") + " Jacobian/factorisation",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOADS[name], "instances": n, "method": f"MIRK{order}",
+                       "timing": "wall clock of the whole solve call with host buffers (copies included)",
+                       "newton_iters_mean": float(res.newton_iters.mean()), "rounds_mean": float(res.rounds.mean()),
+                       "final_points_mean": float(res.n_nodes.mean()),
+                       "retcodes": np.bincount(res.retcode, minlength=3).tolist(), "tuning": sv.tuning()},
+            "clocks": clk.summary()}
+    if not args.no_cpu:
+        from oracle.oracle import Oracle
+        o = Oracle(prob.source, prob.M, prob.n_params, twopoint=prob.twopoint, bc_t=prob.bc_t, La=prob.La, Lb=prob.Lb)
+        threads = os.cpu_count() or 1
+        k = {"pendulum1": 1, "singular": 256, "nonlinear32": 16}[name]
+        t0 = time.perf_counter()
+        reps = 0
+        while True:
+            o.solve_batch(params[:k], nint[:k], tsp[:k], y0[:k], order=order, nthreads=threads)
+            reps += 1
+            if time.perf_counter() - t0 > (2.0 if name != "nonlinear32" else 0.5):
+                break
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": reps * k / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+                                "sample": f"{reps} passes over the first {k} instances ({dt:.1f} s wall)"}
+    print(json.dumps(line))
+    return 0
+
+
 def _ptr(x):
     import ctypes as C
     return C.c_void_p(x.data_ptr() if hasattr(x, "data_ptr") else int(x))
@@ -239,9 +323,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--instances", type=int, default=N_INST,
                     help="batch size (4096 is the benchmark; smaller batches only for profiling)")
+    ap.add_argument("--workload", default="pendulum", choices=["pendulum"] + sorted(WORKLOADS),
+                    help="pendulum: the benchmark (default); the others time the remaining configurations")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "pendulum":
+        args.warmup = max(args.warmup, 1)
+        return run_workload(args)
     args.warmup = max(args.warmup, 3)
 
     ws, rank = _dist()
