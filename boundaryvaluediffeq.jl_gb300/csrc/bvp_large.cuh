@@ -65,6 +65,34 @@ BVP_DEV int jslot(int r, int kk) {
     if (LNODE && r == 1) return (kk + 1) & 1;
     return r;
 }
+// 4 entries of a register row (zero past its end) to 16-byte aligned shared memory
+template <int N>
+BVP_DEV void st4(JT* p, const JT (&a)[N], int j) {
+    const JT v0 = a[j], v1 = j + 1 < N ? a[j + 1] : JT(0), v2 = j + 2 < N ? a[j + 2] : JT(0),
+             v3 = j + 3 < N ? a[j + 3] : JT(0);
+    if constexpr (sizeof(JT) == 4) {
+        *reinterpret_cast<float4*>(p) = make_float4(v0, v1, v2, v3);
+    } else {
+        *reinterpret_cast<double2*>(p) = make_double2(v0, v1);
+        *reinterpret_cast<double2*>(p + 2) = make_double2(v2, v3);
+    }
+}
+// TF32 head and tail of an FP32 value (x = head + tail to about 2^-22 relative)
+BVP_DEV void tf32_split(float x, unsigned& hi, unsigned& lo) {
+    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(hi) : "f"(x));
+    const float r = x - __uint_as_float(hi);
+    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(lo) : "f"(r));
+}
+// d += a b on the tensor cores: a 16 x 8 (row), b 8 x 8 (column), d 16 x 8, FP32 accumulation
+BVP_DEV void mma_tf32(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+// the Schur update of the larger-state elimination runs on the tensor cores for FP32 blocks
+// of state dimension 32
+constexpr bool MMA_SCHUR = sizeof(JT) == 4 && M == 32;
 // correctly rounded reciprocal
 BVP_DEV float rcp_rn(float x) { return __frcp_rn(x); }
 BVP_DEV double rcp_rn(double x) { return __drcp_rn(x); }
@@ -652,24 +680,19 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* 
         if (act) Rel[lane * RLD + 2 * M] = sr;
     }
     // 5. the δ_lo and δ_hi columns: lane c owns column c (two passes when M > 16)
-#pragma unroll 1
-    for (int s = 0; s < (2 * M + 31) / 32; ++s) {
-        const int c = lane + 32 * s;
-        const bool cv = c < 2 * M;
-        const bool lo = c < M;
-        // T entries of this column, read branch-free from clamped (always valid) addresses:
-        // top rows carry the δ_lo coefficients, bottom rows the δ_hi ones
-        const int clo = lo ? c : 0;
-        const int chi = (cv && !lo) ? c - M : 0;
-        auto tval = [&](int p) {
-            const JT tv = Rel[(p < M ? p : 0) * RLD + M + clo];
-            const JT bv = bot.hi(p < M ? 0 : p - M, chi);
-            return cv ? (p < M ? (lo ? tv : JT(0)) : (lo ? JT(0) : bv)) : JT(0);
-        };
-        JT x[M];
+    // T entry of column c in physical row p, read branch-free from clamped (always valid)
+    // addresses: top rows carry the δ_lo coefficients, bottom rows the δ_hi ones
+    auto tval = [&](int c, int p) {
+        const bool cv = c < 2 * M, lo = c < M;
+        const JT tv = Rel[(p < M ? p : 0) * RLD + M + (lo ? c : 0)];
+        const JT bv = bot.hi(p < M ? 0 : p - M, (cv && !lo) ? c - M : 0);
+        return cv ? (p < M ? (lo ? tv : JT(0)) : (lo ? JT(0) : bv)) : JT(0);
+    };
+    // column c of U12 = L11^-1 T_top (forward substitution in pivot order)
+    auto fwd_col = [&](int c, JT (&x)[M]) {
 #pragma unroll
         for (int k = 0; k < M; ++k) {
-            JT t = tval(wm.pidx[k]);
+            JT t = tval(c, wm.pidx[k]);
 #pragma unroll
             for (int j = 0; j < k; j += 4) {
                 JT l4[4];
@@ -680,29 +703,108 @@ BVP_DEV bool warp_eliminate(const WarpMem& wm, JT (&a1)[M], const Bot& bot, JT* 
             }
             x[k] = t;
         }
-        JT sc[M];
+    };
+    if constexpr (!MMA_SCHUR) {
+#pragma unroll 1
+        for (int s = 0; s < (2 * M + 31) / 32; ++s) {
+            const int c = lane + 32 * s;
+            JT x[M];
+            fwd_col(c, x);
+            JT sc[M];
 #pragma unroll
-        for (int u = 0; u < M; ++u) {
-            JT t = tval(wm.qidx[u]);
+            for (int u = 0; u < M; ++u) {
+                JT t = tval(c, wm.qidx[u]);
 #pragma unroll
-            for (int j = 0; j < M4; j += 4) {
-                JT l4[4];
-                ld4(&Lf[(M + u) * LLD + j], l4);
+                for (int j = 0; j < M4; j += 4) {
+                    JT l4[4];
+                    ld4(&Lf[(M + u) * LLD + j], l4);
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (j + q < M) t -= l4[q] * x[j + q];
+                    for (int q = 0; q < 4; ++q)
+                        if (j + q < M) t -= l4[q] * x[j + q];
+                }
+                sc[u] = t;
             }
-            sc[u] = t;
-        }
-        __syncwarp();
-        if (cv) {
-            // column c of U12 is row c of XT (δ_lo) or row c - M of YT (δ_hi)
-            store_row(rec + (lo ? M * M + c * M : 2 * M * M + (c - M) * M), x);
-            const int dc = lo ? M + c : c - M;
+            __syncwarp();
+            if (c < 2 * M) {
+                // column c of U12 is row c of XT (δ_lo) or row c - M of YT (δ_hi)
+                store_row(rec + (c < M ? M * M + c * M : 2 * M * M + (c - M) * M), x);
+                const int dc = c < M ? M + c : c - M;
 #pragma unroll
-            for (int u = 0; u < M; ++u) Rel[u * RLD + dc] = sc[u];
+                for (int u = 0; u < M; ++u) Rel[u * RLD + dc] = sc[u];
+            }
+            __syncwarp();
         }
-        __syncwarp();
+    } else {
+        // M = 32, FP32: the forward substitutions as above, then the Schur update
+        // T_bot - L21 U12 (32 x 64 x 32) on the tensor cores, mma.sync m16n8k8 TF32 with each
+        // operand split into a TF32 head and tail (three products: near-FP32 accuracy),
+        // 32 columns at a time with U12 staged (transposed) in the dead L11 rows of Lf
+        JT xh[2][M];
+        fwd_col(lane, xh[0]);
+        fwd_col(lane + 32, xh[1]);
+        store_row(rec + M * M + lane * M, xh[0]);        // XT row `lane`
+        store_row(rec + 2 * M * M + lane * M, xh[1]);    // YT row `lane`
+        __syncwarp();                                    // L11 is read no more
+        const int g = lane >> 2, tg = lane & 3;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            {
+                JT* row = Lf + lane * LLD;               // U12 column 32h + lane as a row
+#pragma unroll
+                for (int k = 0; k < M; k += 4) st4(row + k, xh[h], k);
+            }
+            __syncwarp();
+            float d[2][4][4];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int r8 = 0; r8 < 2; ++r8) {
+                    const int qq = wm.qidx[16 * mt + g + 8 * r8];
+#pragma unroll
+                    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+                        for (int e = 0; e < 2; ++e) d[mt][nt][2 * r8 + e] = tval(32 * h + 8 * nt + 2 * tg + e, qq);
+                }
+#pragma unroll
+            for (int kt = 0; kt < M / 8; ++kt) {
+                unsigned ah[2][4], al[2][4];
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt) {
+                    const JT* L0 = Lf + (M + 16 * mt + g) * LLD + 8 * kt + tg;
+                    tf32_split(-L0[0], ah[mt][0], al[mt][0]);
+                    tf32_split(-L0[8 * LLD], ah[mt][1], al[mt][1]);
+                    tf32_split(-L0[4], ah[mt][2], al[mt][2]);
+                    tf32_split(-L0[8 * LLD + 4], ah[mt][3], al[mt][3]);
+                }
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) {
+                    const JT* B = Lf + (8 * nt + g) * LLD + 8 * kt + tg;
+                    unsigned bh[2], bl[2];
+                    tf32_split(B[0], bh[0], bl[0]);
+                    tf32_split(B[4], bh[1], bl[1]);
+#pragma unroll
+                    for (int mt = 0; mt < 2; ++mt) {
+                        mma_tf32(d[mt][nt], al[mt], bh);
+                        mma_tf32(d[mt][nt], ah[mt], bl);
+                        mma_tf32(d[mt][nt], ah[mt], bh);
+                    }
+                }
+            }
+            __syncwarp();                                // T reads and tile reads done
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int r8 = 0; r8 < 2; ++r8)
+#pragma unroll
+                    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+                        for (int e = 0; e < 2; ++e) {
+                            const int u = 16 * mt + g + 8 * r8;
+                            const int c = 32 * h + 8 * nt + 2 * tg + e;
+                            Rel[u * RLD + (c < M ? M + c : c - M)] = d[mt][nt][2 * r8 + e];
+                        }
+            __syncwarp();
+        }
     }
     return ok;
 }
