@@ -1158,6 +1158,39 @@ extern "C" __global__ void bl_transfer(const BvpLargeArgs a) {
     for (int k = lane; k < Nn * M; k += 32) y0[k] = ny[k];
 }
 
+// ---- dense output u(t) / u'(t) from the final mesh, solution and stages (interpolation.jl:17-206):
+//      one warp per instance, lanes over the query times -------------------------------------
+extern "C" __global__ void bl_dense(const BvpLargeArgs a, int nq, const double* tq, int deriv, double* out) {
+    using namespace bvp;
+    const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (q >= a.n_inst) return;
+    const int N = a.N[q];
+    const long long nb = a.node_off[q];
+    const double* mesh = a.mesh + nb;
+    const double* y = a.y + nb * M;
+    for (int j = lane_id(); j < nq; j += 32) {
+        const double t = tq[(long long)q * nq + j];
+        // EvalSol's interval rule (interpolation.jl:214-242, Core/src/utils.jl:119-121)
+        int lo = 0, hi = N;
+        while (lo < hi) { const int mid = (lo + hi) >> 1; if (mesh[mid] < t) lo = mid + 1; else hi = mid; }
+        int i = lo - 1;
+        i = i < 0 ? 0 : (i > N - 2 ? N - 2 : i);
+        const double dt = a.h[nb + i];
+        double w[SS], wp[SS];
+        interp_weights<double>((t - mesh[i]) / dt, w, wp);
+        const double* wv = deriv ? wp : w;
+        const double* Kg = a.K + (nb + i) * (S * M);
+        const double* KIg = a.KI + (nb + i) * (NSXA * M);
+        double* o = out + ((long long)q * nq + j) * M;
+        for (int m = 0; m < M; ++m) {
+            double acc = Kg[m] * wv[0];
+            for (int r = 1; r < S; ++r) acc += Kg[r * M + m] * wv[r];
+            for (int qq = 0; qq < NSX; ++qq) acc += KIg[qq * M + m] * wv[S + qq];
+            o[m] = deriv ? acc : acc * dt + y[(long long)i * M + m];
+        }
+    }
+}
+
 extern "C" __global__ void bl_convert_params(const double* p, bvp::JT* pj, long long n) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
         pj[k] = bvp::JT(p[k]);

@@ -59,7 +59,9 @@ struct bvp_handle_s {
     // larger-state path (M > 8, bvp_large.cuh)
     bool large = false;
     cudaKernel_t kl_res = nullptr, kl_jac = nullptr, kl_solve = nullptr, kl_update = nullptr, kl_copy = nullptr,
-                 kl_defect = nullptr, kl_transfer = nullptr, kl_convert = nullptr, kl_probe = nullptr;
+                 kl_defect = nullptr, kl_transfer = nullptr, kl_convert = nullptr, kl_probe = nullptr,
+                 kl_dense = nullptr;
+    BvpLargeArgs la{};       // the last larger-state solve's arguments (dense output reads them)
     int l_threads = 256;     // bl_linsolve block size, picked by large_tune_linsolve
     size_t l_smem = 0;
     size_t l_warp_bytes = 0, l_dense_bytes = 0;
@@ -252,6 +254,7 @@ static bvp_status compile_and_load(bvp_handle* h) {
         CU(cudaLibraryGetKernel(&h->kl_transfer, h->lib, "bl_transfer"));
         CU(cudaLibraryGetKernel(&h->kl_convert, h->lib, "bl_convert_params"));
         CU(cudaLibraryGetKernel(&h->kl_probe, h->lib, "bl_layout_probe"));
+        CU(cudaLibraryGetKernel(&h->kl_dense, h->lib, "bl_dense"));
         return BVP_OK;
     }
     CU(cudaLibraryGetKernel(&h->k_fused, h->lib, "bvp_solve_fused"));
@@ -1148,8 +1151,24 @@ static bvp_status solve_large(bvp_handle* h, int n, const double* params, const 
             if (!L.done && L.rounds >= o.max_rounds) { L.retcode = BVP_RET_MAXITERS; L.done = true; }
         }
     }
+    const bool stages = o.want_stages != 0;
+    if (stages) {
+        // the interpolant's extra stages at every instance's final mesh and solution (the
+        // stages K are the last residual's, at the accepted iterate): the defect pass over all
+        // instances writes them
+        std::vector<int> all(n);
+        int mx = 2;
+        for (int q = 0; q < n; ++q) { all[q] = q; mx = std::max(mx, I[q].N); }
+        s = upload_N();
+        if (s != BVP_OK) return s;
+        s = large_active(h, a, all);
+        if (s != BVP_OK) return s;
+        CU(cudaMemsetAsync(h->d_ldnorm.p, 0, size_t(n) * 8, h->stream));
+        s = large_run(h, h->kl_defect, dim3(unsigned((mx + 127) / 128), unsigned(n)), dim3(128), 0, a);
+        if (s != BVP_OK) return s;
+    }
     CU(cudaEventRecord(h->ev[2], h->stream));
-    // results: per-instance state and the packed mesh and solution
+    // results: per-instance state and the packed mesh and solution (and stages)
     long long total = 0;
     for (int q = 0; q < n; ++q) total += I[q].N;
     if (h->out_cap < total) {
@@ -1169,6 +1188,13 @@ static bvp_status solve_large(bvp_handle* h, int n, const double* params, const 
         std::memcpy(hm + o0, L.mesh.data(), size_t(L.N) * 8);
         CU(cudaMemcpyAsync(hy + o0 * M, static_cast<const double*>(h->d_y.p) + L.off * M, size_t(L.N) * M * 8,
                            cudaMemcpyDeviceToHost, h->stream));
+        if (stages) {
+            const int SM = h->L.S * M, XM = h->L.NSXA * M;
+            CU(cudaMemcpyAsync(static_cast<double*>(h->h_K.p) + o0 * SM, static_cast<const double*>(h->d_K.p) + L.off * SM,
+                               size_t(L.N - 1) * SM * 8, cudaMemcpyDeviceToHost, h->stream));
+            CU(cudaMemcpyAsync(static_cast<double*>(h->h_KI.p) + o0 * XM, static_cast<const double*>(h->d_KI.p) + L.off * XM,
+                               size_t(L.N - 1) * XM * 8, cudaMemcpyDeviceToHost, h->stream));
+        }
         h->offsets[q + 1] = o0 + L.N;
     }
     CU(cudaStreamSynchronize(h->stream));
@@ -1177,7 +1203,9 @@ static bvp_status solve_large(bvp_handle* h, int n, const double* params, const 
     h->timing_ms[0] = ms;
     h->timing_ms[1] = ms;
     h->last_n = n;
-    h->stages_ok = false;
+    h->stages_ok = stages;
+    h->la = a;
+    h->la.n_inst = n;
     h->have_results = true;
     h->pending_device = false;
     if (out) {
@@ -1423,13 +1451,21 @@ bvp_status bvp_dense_output(bvp_handle* h, int32_t nq, const double* tq, int32_t
     bvp_status s = BVP_OK;
     do {
         if (cudaMemcpyAsync(dt.p, tq, size_t(n) * nq * 8, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "H2D"); break; }
-        BvpArgs a;
-        fill_args(h, a, n, h->last_tot, 0, static_cast<const double*>(h->d_params.p), nullptr, nullptr, nullptr, nullptr);
         int nqq = nq, dv = deriv;
         const double* tp = static_cast<const double*>(dt.p);
         double* op = static_cast<double*>(dout.p);
-        void* args[] = {&a, &nqq, &tp, &dv, &op};
-        if (cudaLaunchKernel((const void*)h->k_dense, dim3((n * 32 + 127) / 128), dim3(128), args, 0, h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "dense launch"); break; }
+        cudaError_t e;
+        if (h->large) {
+            // the larger-state kernels keep the final point counts in d_N (uploaded by the solve)
+            void* args[] = {&h->la, &nqq, &tp, &dv, &op};
+            e = cudaLaunchKernel((const void*)h->kl_dense, dim3((n * 32 + 127) / 128), dim3(128), args, 0, h->stream);
+        } else {
+            BvpArgs a;
+            fill_args(h, a, n, h->last_tot, 0, static_cast<const double*>(h->d_params.p), nullptr, nullptr, nullptr, nullptr);
+            void* args[] = {&a, &nqq, &tp, &dv, &op};
+            e = cudaLaunchKernel((const void*)h->k_dense, dim3((n * 32 + 127) / 128), dim3(128), args, 0, h->stream);
+        }
+        if (e != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "dense launch"); break; }
         if (cudaMemcpyAsync(out, dout.p, size_t(n) * nq * M * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "D2H"); break; }
         if (cudaStreamSynchronize(h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "sync"); break; }
     } while (0);

@@ -75,3 +75,42 @@ def test_nonlinear32_mirk6_and_reference_size(pkg, problems):
             assert nrm <= 1e-6 * (1 + 1e-6), (order, i, nrm)
             err, dn = o.defect(params[i], m, y, order=order)
             assert dn <= 1e-6 * (1 + 1e-3), (order, i, dn)
+
+
+def test_nonlinear32_dense_output(pkg, problems):
+    # sol(t) and sol(t, Val{1}) of the larger-state path (interpolation.jl:17-206): the stages the
+    # library returns are the oracle's at the GPU's solution, and the dense output is the MIRK
+    # interpolant of those stages
+    p = problems.NONLINEAR32
+    o = _oracle(p)
+    params, nint, tsp, y0 = problems.nonlinear32_family(3, seed=11, n_intervals=64)
+    sv = pkg.BatchSolver(p, order=4, jac_precision=64, want_stages=1)
+    res = sv.solve(params, nint, tsp, y0)
+    assert (res.retcode == RET_SUCCESS).all()
+    rng = np.random.default_rng(3)
+    tq = np.sort(rng.uniform(0.0, 1.0, (3, 21)), axis=1)
+    tq[:, 0], tq[:, -1] = 0.0, 1.0
+    u = sv.dense(tq)
+    du = sv.dense(tq, deriv=1)
+    checked_ki = 0
+    for i in range(3):
+        m, y = res.solution(i)
+        K, KI = res.stages(i)
+        n = len(m)
+        F, Kref, nrm = o.residual(params[i], m, y)
+        scale = max(1.0, np.abs(Kref).max())
+        assert np.abs(K - Kref.reshape(K.shape)).max() <= 1e-10 * scale
+        if res.rounds[i] == 1:
+            # uniform mesh: the oracle started from the GPU's (converged) solution returns its
+            # own interpolant stages there
+            ref = o.solve_batch(params[i:i + 1], [n - 1], tsp[i:i + 1], y, y0_mode=1, adaptive=0,
+                                want_stages=True)
+            assert np.abs(KI - ref["KI"][0, :n - 1]).max() <= 1e-10 * scale
+            checked_ki += 1
+        assert np.abs(u[i] - o.interpolate(4, m, y, K, KI, tq[i])).max() < 1e-12
+        assert np.abs(du[i] - o.interpolate(4, m, y, K, KI, tq[i], deriv=1)).max() < 1e-11
+        # at t0 the interpolant is the first node; at t1 it meets the last node up to the last
+        # interval's collocation residual, which the accepted solution keeps within abstol
+        assert np.abs(u[i][0] - y[0]).max() == 0.0
+        assert np.abs(u[i][-1] - y[-1]).max() <= 1e-6 * (1 + 1e-6)
+    assert checked_ki >= 1
