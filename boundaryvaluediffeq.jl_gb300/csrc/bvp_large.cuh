@@ -1191,6 +1191,21 @@ extern "C" __global__ void bl_dense(const BvpLargeArgs a, int nq, const double* 
     }
 }
 
+// ---- initial meshes, spacings and guesses from one packed upload into the arena ----------------
+extern "C" __global__ void bl_scatter(const BvpLargeArgs a, const double* pm, const double* ph, const double* py,
+                                      const long long* poff) {
+    using namespace bvp;
+    const int q = blockIdx.y;
+    const long long p0 = poff[q];
+    const int N = int(poff[q + 1] - p0);
+    const long long nb = a.node_off[q];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N * M; k += gridDim.x * blockDim.x) {
+        a.y[nb * M + k] = py[p0 * M + k];
+        if (k < N) a.mesh[nb + k] = pm[p0 + k];
+        if (k < N - 1) a.h[nb + k] = ph[p0 + k];
+    }
+}
+
 extern "C" __global__ void bl_convert_params(const double* p, bvp::JT* pj, long long n) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
         pj[k] = bvp::JT(p[k]);

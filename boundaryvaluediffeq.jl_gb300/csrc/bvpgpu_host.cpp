@@ -60,7 +60,7 @@ struct bvp_handle_s {
     bool large = false;
     cudaKernel_t kl_res = nullptr, kl_jac = nullptr, kl_solve = nullptr, kl_update = nullptr, kl_copy = nullptr,
                  kl_defect = nullptr, kl_transfer = nullptr, kl_convert = nullptr, kl_probe = nullptr,
-                 kl_dense = nullptr;
+                 kl_dense = nullptr, kl_scatter = nullptr;
     BvpLargeArgs la{};       // the last larger-state solve's arguments (dense output reads them)
     int l_threads = 256;     // bl_linsolve block size, picked by large_tune_linsolve
     size_t l_smem = 0;
@@ -255,6 +255,7 @@ static bvp_status compile_and_load(bvp_handle* h) {
         CU(cudaLibraryGetKernel(&h->kl_convert, h->lib, "bl_convert_params"));
         CU(cudaLibraryGetKernel(&h->kl_probe, h->lib, "bl_layout_probe"));
         CU(cudaLibraryGetKernel(&h->kl_dense, h->lib, "bl_dense"));
+        CU(cudaLibraryGetKernel(&h->kl_scatter, h->lib, "bl_scatter"));
         return BVP_OK;
     }
     CU(cudaLibraryGetKernel(&h->k_fused, h->lib, "bvp_solve_fused"));
@@ -780,7 +781,11 @@ static bvp_status solve_large(bvp_handle* h, int n, const double* params, const 
         void* args[] = {&src, &dst, &np};
         if (np) CU(cudaLaunchKernel((const void*)h->kl_convert, dim3(256), dim3(256), args, 0, h->stream));
     }
-    std::vector<double> ybuf;
+    // initial meshes, spacings and guesses packed instance after instance, uploaded at once and
+    // scattered into the arena by bl_scatter
+    std::vector<long long> poff(n + 1, 0);
+    for (int q = 0; q < n; ++q) poff[q + 1] = poff[q] + n_intervals[q] + 1;
+    std::vector<double> pm(size_t(poff[n])), ph(size_t(poff[n])), py(size_t(poff[n]) * M);
     long long yoff = 0;
     for (int q = 0; q < n; ++q) {
         LargeInst& L = I[q];
@@ -792,17 +797,16 @@ static bvp_status solve_large(bvp_handle* h, int n, const double* params, const 
         L.h.resize(ni);
         for (int i = 0; i <= ni; ++i) L.mesh[i] = (i == ni) ? t1 : std::fma(double(i), hh, t0);
         for (int i = 0; i < ni; ++i) L.h[i] = L.mesh[i + 1] - L.mesh[i];
-        ybuf.assign(size_t(L.N) * M, 0.0);
+        double* yq = py.data() + size_t(poff[q]) * M;
         if (y0_mode == 0) {
             for (int i = 0; i < L.N; ++i)
-                for (int m = 0; m < M; ++m) ybuf[size_t(i) * M + m] = y0[size_t(q) * M + m];
+                for (int m = 0; m < M; ++m) yq[size_t(i) * M + m] = y0[size_t(q) * M + m];
         } else {
-            std::memcpy(ybuf.data(), y0 + yoff * M, ybuf.size() * 8);
+            std::memcpy(yq, y0 + yoff * M, size_t(L.N) * M * 8);
             yoff += L.N;
         }
-        CU(cudaMemcpy(static_cast<double*>(h->d_mesh.p) + L.off, L.mesh.data(), size_t(L.N) * 8, cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(static_cast<double*>(h->d_h.p) + L.off, L.h.data(), size_t(L.N - 1) * 8, cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(static_cast<double*>(h->d_y.p) + L.off * M, ybuf.data(), ybuf.size() * 8, cudaMemcpyHostToDevice));
+        std::memcpy(pm.data() + poff[q], L.mesh.data(), size_t(L.N) * 8);
+        std::memcpy(ph.data() + poff[q], L.h.data(), size_t(L.N - 1) * 8);
         offs[q] = L.off;
         Ns[q] = L.N;
     }
@@ -841,6 +845,27 @@ static bvp_status solve_large(bvp_handle* h, int n, const double* params, const 
     a.tot = tot;
     a.transfer_inplace = o.transfer_inplace;
     a.newN = static_cast<const int*>(h->d_newN.p);
+    {
+        // the packed inputs go through scratch arrays of the arena that the solve rewrites
+        // before reading (ybase, inc, err), then into place
+        double* dpy = static_cast<double*>(h->d_ybase.p);
+        double* dpm = static_cast<double*>(h->d_inc.p);
+        double* dph = dpm + poff[n];
+        long long* dpo = static_cast<long long*>(h->d_err.p);
+        CU(cudaMemcpyAsync(dpy, py.data(), py.size() * 8, cudaMemcpyHostToDevice, h->stream));
+        CU(cudaMemcpyAsync(dpm, pm.data(), pm.size() * 8, cudaMemcpyHostToDevice, h->stream));
+        CU(cudaMemcpyAsync(dph, ph.data(), ph.size() * 8, cudaMemcpyHostToDevice, h->stream));
+        CU(cudaMemcpyAsync(dpo, poff.data(), poff.size() * 8, cudaMemcpyHostToDevice, h->stream));
+        int mxN = 2;
+        for (int q = 0; q < n; ++q) mxN = std::max(mxN, I[q].N);
+        const double* cpy = dpy;
+        const double* cpm = dpm;
+        const double* cph = dph;
+        const long long* cpo = dpo;
+        void* args[] = {&a, &cpm, &cph, &cpy, &cpo};
+        CU(cudaLaunchKernel((const void*)h->kl_scatter, dim3(unsigned(std::min(64, (mxN * M + 255) / 256)), unsigned(n)),
+                            dim3(256), args, 0, h->stream));
+    }
     CU(cudaEventRecord(h->ev[0], h->stream));
     CU(cudaEventRecord(h->ev[1], h->stream));
     std::vector<unsigned long long> nb(n);
