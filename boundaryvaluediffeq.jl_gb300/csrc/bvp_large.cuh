@@ -44,7 +44,6 @@ namespace bvp {
 static_assert(BVP_TWOPOINT == 1, "the larger-state kernels take two-point boundary conditions");
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int M = BVP_M;
-constexpr int D = 2 * M;
 constexpr int LA = BVP_LA;
 using JT = BVP_JT;
 constexpr int RECW = 3 * M * M + M;
