@@ -40,6 +40,9 @@ def test_nonlinear32_matches_oracle(pkg, problems, jac_precision):
     res = sv.solve(params, nint, tsp, y0)
     ref = _oracle(p).solve_batch(params, nint, tsp, y0)
     assert (res.retcode == RET_SUCCESS).all()
+    # the autotuner picked a linear-solve block of 3..8 warps on the first Newton step
+    t = sv.tuning()["linsolve_threads"]
+    assert t % 32 == 0 and 96 <= t <= 256, t
     if jac_precision == 64:
         assert (res.newton_iters == ref["newton_iters"]).all(), (res.newton_iters, ref["newton_iters"])
         _compare(res, ref, 1e-6)
