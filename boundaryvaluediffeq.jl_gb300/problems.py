@@ -165,6 +165,26 @@ def lane_emden_analytic(t):
     return np.stack([y, yp], -1)
 
 
+# Mathieu eigenvalue: y'' + (lambda - 10 cos 2t) y = 0 on (0, pi), y'(0) = 0, y(0) = 1, y'(pi) = 0,
+# with the unknown lambda carried as a third state (lambda' = 0), which is how the reference's
+# tune_parameters solves it (lib/BoundaryValueDiffEqMIRK/test/Core/mirk_basic_tests.jl:485-507:
+# guess (cos 4t, -4 sin 4t), lambda = 15, MIRK4, dt = 0.05; lambda = 17.09658 within 1e-4)
+MATHIEU = Problem(
+    name="mathieu", M=3, n_params=0,
+    source="""
+BVP_F { du[0] = u[1]; du[1] = -(u[2] - P(10.0) * cos(P(2.0) * t)) * u[0]; du[2] = T(P(0.0)); }
+BVP_BCA { res[0] = ua[1]; res[1] = ua[0] - P(1.0); }
+BVP_BCB { res[0] = ub[1]; }
+""",
+    twopoint=True, La=2, Lb=1, tspan=(0.0, math.pi), u0=(1.0, 0.0, 15.0))
+
+
+def mathieu_guess(n_intervals: int):
+    """The reference test's guess (cos 4t, -4 sin 4t) and lambda = 15 on the uniform initial mesh."""
+    t = np.array([math.pi if i == n_intervals else i * (math.pi / n_intervals) for i in range(n_intervals + 1)])
+    return np.stack([np.cos(4 * t), -4 * np.sin(4 * t), np.full_like(t, 15.0)], -1)
+
+
 def linear_analytic(t):
     t = np.asarray(t, dtype=np.float64)
     cot5 = math.cos(5.0) / math.sin(5.0)
@@ -275,5 +295,5 @@ def nonlinear32_family(n: int, seed: int = 2026, n_intervals: int = 1024, dim: i
     return params, nint, tspans, y0
 
 
-ALL = {p.name: p for p in (PENDULUM, SINGULAR_PERTURBATION, NONLINEAR32, LANE_EMDEN, AFFINE, AFFINE_TWOPOINT,
+ALL = {p.name: p for p in (PENDULUM, SINGULAR_PERTURBATION, NONLINEAR32, LANE_EMDEN, MATHIEU, AFFINE, AFFINE_TWOPOINT,
                            LINEAR, LINEAR_TWOPOINT, TWOPOINT_INTERP, MULTIPOINT, TORUS, ENSEMBLE)}

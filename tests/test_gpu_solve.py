@@ -245,3 +245,26 @@ def test_singular_term_matches_oracle(pkg, problems, jac_precision):
             elif res.retcode[0] == RET_SUCCESS:
                 m, y = res.solution(0)
                 assert o.residual(params[0], m, y, order=order)[2] <= 1e-6 * (1 + 1e-6)
+
+
+@pytest.mark.parametrize("jac_precision", [64, 32])
+def test_mathieu_eigenvalue_gpu(pkg, problems, jac_precision):
+    # the reference's parameter-estimation golden value (mirk_basic_tests.jl:485-507):
+    # lambda = 17.09658 within 1e-4, from the test's guess, MIRK4, dt = 0.05
+    p = problems.MATHIEU
+    n = int(math.ceil(math.pi / 0.05 - 1e-12))
+    guess = problems.mathieu_guess(n)
+    sv = pkg.BatchSolver(p, order=4, jac_precision=jac_precision)
+    res = sv.solve(np.zeros((1, 0)), [n], [[0.0, math.pi]], guess, y0_mode=1)
+    assert res.retcode[0] == RET_SUCCESS
+    m, y = res.solution(0)
+    assert np.abs(y[:, 2] - 17.09658).max() < 1e-4
+    o = _oracle(p)
+    if jac_precision == 64:
+        # FP64 blocks follow the oracle's iterates: same rounds and final mesh
+        ref = o.solve_batch(np.zeros((1, 0)), [n], [[0.0, math.pi]], guess, y0_mode=1, order=4)
+        assert res.n_nodes[0] == ref["n_nodes"][0] and res.rounds[0] == ref["rounds"][0]
+    else:
+        # FP32 blocks: the reference's acceptance tests, evaluated in FP64 by the oracle
+        assert o.residual(np.zeros(0), m, y)[2] <= 1e-6 * (1 + 1e-6)
+        assert o.defect(np.zeros(0), m, y)[1] <= 1e-6 * (1 + 1e-3)

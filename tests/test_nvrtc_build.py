@@ -12,7 +12,7 @@ def _nvrtc_available(pkg):
 CASES = [
     ("pendulum", 2, 32), ("pendulum", 3, 32), ("pendulum", 5, 64), ("pendulum", 6, 32),
     ("multipoint", 4, 32), ("affine_twopoint", 3, 64), ("torus", 4, 32),
-    ("lane_emden", 6, 64), ("nonlinear32", 6, 32), ("nonlinear32", 4, 64), ("nonlinear32", 3, 32),
+    ("lane_emden", 6, 64), ("nonlinear32", 6, 32), ("nonlinear32", 4, 64), ("nonlinear32", 3, 32), ("mathieu", 4, 32),
 ]
 
 

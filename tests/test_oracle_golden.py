@@ -177,3 +177,16 @@ def test_singular_term_lane_emden(problems, order):
     # estimate stays above the 10% threshold and the mesh halves until it exceeds the cap
     o, r, N = _solve1(p, n=100, order=order)
     assert r["retcode"][0] != RET_SUCCESS and N > 1000
+
+
+def test_mathieu_eigenvalue(problems):
+    # mirk_basic_tests.jl:485-507: unknown-parameter estimation, lambda = 17.09658 (atol 1e-4);
+    # the parameter is carried as a state with zero derivative, MIRK4, dt = 0.05 on (0, pi)
+    p = problems.MATHIEU
+    n = int(math.ceil(math.pi / 0.05 - 1e-12))
+    o = _oracle(p)
+    r = o.solve_batch(np.zeros((1, 0)), [n], [[0.0, math.pi]], problems.mathieu_guess(n), y0_mode=1, order=4)
+    assert r["retcode"][0] == RET_SUCCESS
+    N = int(r["n_nodes"][0])
+    lam = r["y"][0, :N, 2]
+    assert np.abs(lam - 17.09658).max() < 1e-4
