@@ -268,3 +268,29 @@ def test_mathieu_eigenvalue_gpu(pkg, problems, jac_precision):
         # FP32 blocks: the reference's acceptance tests, evaluated in FP64 by the oracle
         assert o.residual(np.zeros(0), m, y)[2] <= 1e-6 * (1 + 1e-6)
         assert o.defect(np.zeros(0), m, y)[1] <= 1e-6 * (1 + 1e-3)
+
+
+def test_reference_style_solve(pkg, problems):
+    # the reference's own call, solve(prob, MIRK4(), dt = 0.05) on the pendulum
+    # (benchmark/simple_pendulum.jl), through the reference-style front end, and an ensemble
+    sciml = pkg.sciml
+    p = problems.PENDULUM
+    sol = sciml.solve(p, sciml.MIRK4(jac_precision=64), dt=0.05, p=[9.81, 0.0, 0.0],
+                      u0=[math.pi / 2, math.pi / 2])
+    o = _oracle(p)
+    ref = o.solve_batch(np.array([[9.81, 0.0, 0.0]]), [32], [[0.0, math.pi / 2]],
+                        np.array([[math.pi / 2, math.pi / 2]]))
+    assert sol.successful and ref["retcode"][0] == RET_SUCCESS
+    N = int(ref["n_nodes"][0])
+    assert len(sol.t) == N
+    assert np.abs(sol.u - ref["y"][0, :N]).max() <= 1e-6
+    # sol(t): the interpolant meets the nodes within the collocation residual
+    assert np.abs(sol(sol.t[:6]) - sol.u[:6]).max() <= 1e-6
+    assert sol(0.0).shape == (2,)
+    params, nint, tsp, y0 = problems.pendulum_family(8, seed=12)
+    sols = sciml.solve(sciml.EnsembleProblem(p, params=params, tspans=tsp), sciml.MIRK4(jac_precision=64), dt=0.05)
+    refs = o.solve_batch(params, [32] * 8, tsp, np.tile([math.pi / 2, math.pi / 2], (8, 1)))
+    for i, s in enumerate(sols):
+        n = int(refs["n_nodes"][i])
+        assert s.successful and len(s.t) == n
+        assert np.abs(s.u - refs["y"][i, :n]).max() <= 1e-6
