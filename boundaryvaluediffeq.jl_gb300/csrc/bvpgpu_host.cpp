@@ -1628,7 +1628,10 @@ void bvp_destroy(bvp_handle* h) {
                       &h->d_delta, &h->d_yj, &h->d_Fj, &h->d_scr, &h->d_iscr, &h->d_st, &h->d_order, &h->d_cap,
                       &h->d_node_off, &h->d_counter, &h->d_params, &h->d_params_j, &h->d_n_init,
                       &h->d_tspans, &h->d_y0, &h->d_y0_off, &h->d_out_off, &h->d_out_mesh,
-                      &h->d_out_y, &h->d_out_K, &h->d_out_KI, &h->d_norm, &h->d_feat, &h->d_grid};
+                      &h->d_out_y, &h->d_out_K, &h->d_out_KI, &h->d_norm, &h->d_feat, &h->d_grid,
+                      // the larger-state path's per-instance arrays
+                      &h->d_bcres, &h->d_G, &h->d_lnorm, &h->d_lsq, &h->d_ldnorm, &h->d_lbad,
+                      &h->d_active, &h->d_N, &h->d_newN};
     for (DevBuf* b : devs)
         if (b->p) cudaFree(b->p);
     HostBuf* hosts[] = {&h->h_in, &h->h_st, &h->h_off, &h->h_mesh, &h->h_y, &h->h_K, &h->h_KI};

@@ -63,3 +63,18 @@ def test_device_code_compiles_for_sm103a(pkg):
     rep = os.path.join(os.path.dirname(path), "ptxas_pendulum_o4.txt")
     txt = open(rep).read()
     assert "bvp_solve_fused" in txt and "sm_103a" in txt
+
+
+def test_destroy_releases_every_buffer_of_the_handle():
+    # every device and pinned host buffer the handle owns is released by bvp_destroy
+    import re
+    src = open(os.path.join(ROOT, "boundaryvaluediffeq.jl_gb300", "csrc", "bvpgpu_host.cpp")).read()
+    start = src.index("struct bvp_handle_s {")
+    decl = src[start:src.index("};", start)]
+    body = src[src.index("void bvp_destroy(bvp_handle* h) {"):]
+    body = body[:body.index("delete h;")]
+    freed = set(re.findall(r"&h->(\w+)", body))
+    for kind in ("DevBuf", "HostBuf"):
+        for m in re.finditer(kind + r" ([^;]+);", decl):
+            for name in (x.strip() for x in m.group(1).replace("\n", " ").split(",")):
+                assert name in freed, name
