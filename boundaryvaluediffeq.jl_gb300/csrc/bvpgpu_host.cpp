@@ -698,26 +698,32 @@ static bvp_status large_run(bvp_handle* h, cudaKernel_t k, dim3 grid, dim3 block
 // more instances share an SM; more warps shorten each instance's chain of eliminations.
 static bvp_status large_tune_linsolve(bvp_handle* h, BvpLargeArgs& a, int n_active) {
     const int wmax = h->l_threads / 32;
-    cudaEvent_t e0, e1;
-    CU(cudaEventCreate(&e0));
-    CU(cudaEventCreate(&e1));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return fail(h, BVP_ERR_CUDA, "autotuner: event creation failed");
+    }
     float best = 0.0f;
     int best_w = wmax;
-    for (int rep = 0; rep < 2; ++rep) {   // the first pass warms up
-        for (int w = 3; w <= wmax; ++w) {
+    bvp_status s = BVP_OK;
+    for (int rep = 0; rep < 2 && s == BVP_OK; ++rep) {   // the first pass warms up
+        for (int w = 3; w <= wmax && s == BVP_OK; ++w) {
             const size_t smem = size_t(w) * h->l_warp_bytes + h->l_dense_bytes;
-            CU(cudaEventRecord(e0, h->stream));
-            bvp_status s = large_run(h, h->kl_solve, dim3(unsigned(n_active)), dim3(unsigned(32 * w)), smem, a, nullptr);
-            if (s != BVP_OK) return s;
-            CU(cudaEventRecord(e1, h->stream));
-            CU(cudaEventSynchronize(e1));
             float ms = 0.0f;
-            CU(cudaEventElapsedTime(&ms, e0, e1));
+            if (cudaEventRecord(e0, h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "autotuner: event"); break; }
+            s = large_run(h, h->kl_solve, dim3(unsigned(n_active)), dim3(unsigned(32 * w)), smem, a, nullptr);
+            if (s != BVP_OK) break;
+            if (cudaEventRecord(e1, h->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+                s = fail(h, BVP_ERR_CUDA, "autotuner: timing");
+                break;
+            }
             if (rep == 1 && (w == 3 || ms < best)) { best = ms; best_w = w; }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (s != BVP_OK) return s;
     h->l_threads = 32 * best_w;
     h->l_smem = size_t(best_w) * h->l_warp_bytes + h->l_dense_bytes;
     h->l_tuned = true;
