@@ -9,4 +9,4 @@ from ._lib import build_library, load_library, LIB_PATH, EXPORTS  # noqa: F401
 from .solver import BatchSolver, BatchResult, BVPError, RET_SUCCESS, RET_FAILURE, RET_MAXITERS  # noqa: F401
 from .surrogate import MLP, Surrogate, resample_host  # noqa: F401
 from . import sciml  # noqa: F401
-from .sciml import solve, EnsembleProblem, MIRK2, MIRK3, MIRK4, MIRK5, MIRK6  # noqa: F401
+from .sciml import solve, EnsembleProblem, MIRK2, MIRK3, MIRK4, MIRK5, MIRK6, MIRK6I  # noqa: F401

@@ -86,7 +86,7 @@ def _nvrtc():
     return None
 
 
-def nvrtc_check(problem, order: int, jac_bits: int = 32) -> None:
+def nvrtc_check(problem, order: int, jac_bits: int = 32, mirk6i: int = 0) -> None:
     """Compile the problem's kernels with NVRTC exactly as bvp_create does (same source
     assembly and options, no GPU needed); raises with the NVRTC log on failure."""
     lib = _nvrtc()
@@ -99,7 +99,7 @@ def nvrtc_check(problem, order: int, jac_bits: int = 32) -> None:
     opts = ["--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true", f"-DBVP_M={problem.M}",
             f"-DBVP_ORDER={order}", f"-DBVP_TWOPOINT={int(problem.twopoint)}", f"-DBVP_NBC={nbc}",
             f"-DBVP_LA={problem.La if problem.twopoint else 0}",
-            "-DBVP_JT=" + ("double" if jac_bits == 64 else "float"),
+            "-DBVP_JT=" + ("double" if jac_bits == 64 else "float"), f"-DBVP_MIRK6I={int(bool(mirk6i))}",
             f"-DBVP_SINGULAR={int('BVP_SING' in problem.source)}"]
     names = [fn.encode() for fn in EMBED]
     bodies = [open(os.path.join(CSRC, fn), "rb").read() for fn in EMBED]
@@ -195,7 +195,7 @@ class Options(C.Structure):
                 ("bc_jac_exact", C.c_int32), ("linesearch_fallback", C.c_int32),
                 ("stall_steps", C.c_int32), ("jac_precision", C.c_int32), ("want_stages", C.c_int32),
                 ("fp32_phase", C.c_int32), ("abstol", C.c_double), ("defect_threshold", C.c_double),
-                ("divergence_factor", C.c_double)]
+                ("divergence_factor", C.c_double), ("mirk6i", C.c_int32)]
 
 
 class Results(C.Structure):

@@ -116,7 +116,7 @@ struct BvpLargeArgs {
     const int* newN;               // bl_transfer: point count of the new mesh (buffer 1)
 };
 
-// Scratch layout as a function of (M, order, BC evaluation points, two-point).
+// Scratch layout as a function of (M, order, BC evaluation points, two-point, MIRK6I).
 struct BvpLayout {
     int M, S, SS, NSX, NSXA, EQW, RECW, NBCB, KMAX, NDENSE;
     int SCR_BCRES, SCR_BCBLK, SCR_SEG, SCR_UA, SCR_BCW, SCRW;
@@ -129,11 +129,11 @@ struct BvpLayout {
 #define BVP_LAYOUT_FN inline
 #endif
 
-BVP_LAYOUT_FN BvpLayout bvp_make_layout(int M, int order, int nbc, int twopoint) {
+BVP_LAYOUT_FN BvpLayout bvp_make_layout(int M, int order, int nbc, int twopoint, int mirk6i = 0) {
     BvpLayout L;
     L.M = M;
     L.S = order - 1;
-    L.SS = (order == 2 || order == 3) ? 3 : (order == 4 ? 4 : (order == 5 ? 6 : 9));
+    L.SS = (order == 2 || order == 3) ? 3 : (order == 4 ? 4 : (order == 5 ? 6 : (mirk6i ? 8 : 9)));
     L.NSX = L.SS - L.S;
     L.NSXA = L.NSX > 0 ? L.NSX : 1;
     L.EQW = 2 * M * M + M;

@@ -190,6 +190,7 @@ void bvp_default_options(bvp_options* o) {
     o->abstol = 1e-6;
     o->defect_threshold = 0.1;
     o->divergence_factor = 1e3;
+    o->mirk6i = 0;
 }
 
 const char* bvp_last_error(bvp_handle* h) { return h ? h->err.c_str() : "null handle"; }
@@ -206,6 +207,7 @@ static bvp_status compile_and_load(bvp_handle* h) {
         "-DBVP_NBC=" + std::to_string(d.twopoint ? 2 : d.n_bc_pts),
         "-DBVP_LA=" + std::to_string(d.twopoint ? d.La : 0),
         std::string("-DBVP_JT=") + (o.jac_precision == 64 ? "double" : "float"),
+        std::string("-DBVP_MIRK6I=") + (o.mirk6i ? "1" : "0"),
         // a source with BVP_SING has a singular term S y / t (the problem's singular_term)
         std::string("-DBVP_SINGULAR=") + (h->source.find("BVP_SING") != std::string::npos ? "1" : "0"),
     };
@@ -289,11 +291,12 @@ bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bv
     else if (!d.twopoint && (d.n_bc_pts < 1 || d.n_bc_pts > 16)) why = "n_bc_pts must be in 1..16";
     else if (d.twopoint && (d.La < 0 || d.Lb < 0 || d.La + d.Lb != d.M)) why = "La + Lb must equal M";
     else if (o.order < 2 || o.order > 6) why = "order must be 2..6";
+    else if (o.mirk6i != 0 && (o.mirk6i != 1 || o.order != 6)) why = "mirk6i takes order 6";
     else if (!(o.abstol > 0)) why = "abstol must be > 0";
     else if (o.max_subintervals < 1) why = "max_subintervals must be >= 1";
     else if (o.jac_precision != 32 && o.jac_precision != 64) why = "jac_precision must be 32 or 64";
     if (!why.empty()) { delete h; return BVP_ERR_INVALID; }
-    h->L = bvp_make_layout(d.M, o.order, d.twopoint ? 2 : d.n_bc_pts, d.twopoint);
+    h->L = bvp_make_layout(d.M, o.order, d.twopoint ? 2 : d.n_bc_pts, d.twopoint, o.mirk6i);
     h->js = o.jac_precision == 64 ? 8 : 4;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

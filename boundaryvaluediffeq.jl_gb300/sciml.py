@@ -34,10 +34,13 @@ class MIRK:
     jac_precision: int = 32
     max_num_subintervals: int = 3000
     defect_threshold: float = 0.1
+    mirk6i: bool = False          # MIRK6I() (mirk_tableaus.jl:154-194): order 6, own interpolant
 
     def __post_init__(self):
         if self.order not in (2, 3, 4, 5, 6):
             raise ValueError(f"MIRK order must be 2..6, got {self.order}")
+        if self.mirk6i and self.order != 6:
+            raise ValueError("MIRK6I is an order-6 scheme")
         if self.jac_precision not in (32, 64):
             raise ValueError("jac_precision must be 32 or 64")
 
@@ -47,6 +50,7 @@ def MIRK3(**kw): return MIRK(3, **kw)  # noqa: E704
 def MIRK4(**kw): return MIRK(4, **kw)  # noqa: E704
 def MIRK5(**kw): return MIRK(5, **kw)  # noqa: E704
 def MIRK6(**kw): return MIRK(6, **kw)  # noqa: E704
+def MIRK6I(**kw): return MIRK(6, mirk6i=True, **kw)  # noqa: E704
 
 
 @dataclass
@@ -125,7 +129,8 @@ def _solver(problem, alg: MIRK, abstol, adaptive, dense, solver_cls):
     if sv is None:
         sv = solver_cls(problem, order=alg.order, abstol=abstol, jac_precision=alg.jac_precision,
                         adaptive=int(adaptive), want_stages=int(dense),
-                        max_subintervals=alg.max_num_subintervals, defect_threshold=alg.defect_threshold)
+                        max_subintervals=alg.max_num_subintervals, defect_threshold=alg.defect_threshold,
+                        mirk6i=int(alg.mirk6i))
         _CACHE[key] = sv
     return sv
 
@@ -176,5 +181,5 @@ def solve(prob, alg: MIRK, *, dt: float, abstol: float = 1e-6, adaptive: bool = 
     return _to_solutions(res, sv, dense)[0]
 
 
-__all__ = ["solve", "MIRK", "MIRK2", "MIRK3", "MIRK4", "MIRK5", "MIRK6", "EnsembleProblem", "BVPSolution",
+__all__ = ["solve", "MIRK", "MIRK2", "MIRK3", "MIRK4", "MIRK5", "MIRK6", "MIRK6I", "EnsembleProblem", "BVPSolution",
            "RET_SUCCESS", "RET_MAXITERS"]

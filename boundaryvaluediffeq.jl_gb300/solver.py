@@ -19,6 +19,12 @@ STATUS = {0: "OK", 1: "INVALID", 2: "COMPILE", 3: "CUDA", 4: "NOMEM", 5: "STATE"
 RET_SUCCESS, RET_FAILURE, RET_MAXITERS = 0, 1, 2
 S_OF = {2: 1, 3: 2, 4: 3, 5: 4, 6: 5}
 NSX_OF = {2: 2, 3: 1, 4: 1, 5: 2, 6: 4}
+NSX_MIRK6I = 3      # MIRK6I: 8 interpolant stages over its 5 discrete ones
+
+
+def n_extra_stages(order: int, mirk6i: int = 0) -> int:
+    """Extra interpolant stages of MIRKn (or MIRK6I), at least one slot."""
+    return NSX_MIRK6I if mirk6i else max(1, NSX_OF[order])
 
 
 class BVPError(RuntimeError):
@@ -139,7 +145,7 @@ class BatchSolver:
                           y_packed=np.ctypeslib.as_array(y, shape=(tot * M,)).copy().reshape(tot, M),
                           order=self.order, **r)
         if self.options.want_stages and bool(K) and bool(KI):
-            s, nsx = S_OF[self.order], max(1, NSX_OF[self.order])
+            s, nsx = S_OF[self.order], n_extra_stages(self.order, self.options.mirk6i)
             res.K_packed = np.ctypeslib.as_array(K, shape=(tot * s * M,)).copy().reshape(tot, s, M)
             res.KI_packed = np.ctypeslib.as_array(KI, shape=(tot * nsx * M,)).copy().reshape(tot, nsx, M)
         return res

@@ -53,7 +53,7 @@ typedef struct {
  * (lib/BoundaryValueDiffEqMIRK/src/mirk.jl:49-53, algorithms.jl:55-61,
  *  lib/BoundaryValueDiffEqCore/src/calc_errors.jl:54-60). */
 typedef struct {
-    int32_t order;                /* MIRK order: 2, 3, 4, 5 or 6 */
+    int32_t order;                /* MIRK order: 2, 3, 4, 5 or 6 (see mirk6i) */
     int32_t adaptive;             /* 1: defect-controlled mesh refinement */
     int32_t max_subintervals;     /* mesh cap (reference default 3000) */
     int32_t max_newton;           /* Newton iterations per attempt */
@@ -70,6 +70,9 @@ typedef struct {
     double abstol;
     double defect_threshold;
     double divergence_factor;     /* Newton stops when ||F|| exceeds this times its start */
+    int32_t mirk6i;               /* 1 with order 6: MIRK6I, the order-6 scheme with Lobatto-point
+                                     stages and its own interpolant (mirk_tableaus.jl:154-194,
+                                     interpolation.jl:583-693; BoundaryValueDiffEqMIRK.jl:179) */
 } bvp_options;
 
 /* Per-instance outputs of a batch (caller-owned arrays of n_inst entries; any may be NULL). */

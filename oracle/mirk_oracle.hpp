@@ -60,13 +60,14 @@ struct Options {
     double abstol;             // reference default 1e-6 (mirk.jl:50)
     double defect_threshold;   // reference default 0.1 (calc_errors.jl:54-60)
     double divergence_factor;
+    int32_t mirk6i;            // 1 with order 6: MIRK6I (mirk_tableaus.jl:154-194)
 };
 
 inline void fill_default_options(Options* o) {
     o->order = 4; o->adaptive = 1; o->max_subintervals = 3000; o->max_newton = 100;
     o->max_rounds = 64; o->transfer_inplace = 1; o->bc_jac_exact = 0;
     o->linesearch_fallback = 1; o->stall_steps = 32; o->nthreads = 0;
-    o->abstol = 1e-6; o->defect_threshold = 0.1; o->divergence_factor = 1e3;
+    o->abstol = 1e-6; o->defect_threshold = 0.1; o->divergence_factor = 1e3; o->mirk6i = 0;
 }
 
 // Julia's round(Int, x): round half to even (the default rounding mode of rint).
@@ -212,7 +213,7 @@ struct InstanceSolver {
         const int ii = interval_of(mesh.data(), N, t);
         const double tau = (t - mesh[ii]) / h[ii];
         double w[9], wp[9];
-        interp_weights(tb.order, tau, w, wp);
+        interp_weights(tb.scheme, tau, w, wp);
         std::vector<double> kiv(std::max(1, ns() * M));
         interp_stages_interval<double>(ii, &y[ii * M], &y[(ii + 1) * M], &K[ii * tb.s * M], kiv.data());
         sum_stages<double>(ii, w, &y[ii * M], &K[ii * tb.s * M], kiv.data(), z);
@@ -333,7 +334,7 @@ struct InstanceSolver {
                 const int ii = node[k];
                 const double tau = (pi.bc_t[k] - mesh[ii]) / h[ii];
                 double w[9], wp[9];
-                interp_weights(tb.order, tau, w, wp);
+                interp_weights(tb.scheme, tau, w, wp);
                 DualI yi[M], yi1[M], ri[M], z[M];
                 std::vector<DualI> Kd2(size_t(S) * M), KId(std::max(1, ns()) * M);
                 for (int m = 0; m < M; ++m) {
@@ -551,8 +552,8 @@ struct InstanceSolver {
         KI.assign(size_t(N - 1) * std::max(1, ns()) * M, 0.0);
         err_max.assign(N - 1, 0.0);
         double w1[9], w1p[9], w2[9], w2p[9];
-        interp_weights(tb.order, tb.tau_star, w1, w1p);
-        interp_weights(tb.order, 1.0 - tb.tau_star, w2, w2p);
+        interp_weights(tb.scheme, tb.tau_star, w1, w1p);
+        interp_weights(tb.scheme, 1.0 - tb.tau_star, w2, w2p);
         double dn = 0;
         for (int i = 0; i < N - 1; ++i) {
             const double* Ki = &K[size_t(i) * S * M];
@@ -680,7 +681,7 @@ struct InstanceSolver {
             const double dt = old_h[i];
             const double tau = (m_t - old_mesh[i]) / dt;
             double w[9], wp[9];
-            interp_weights(tb.order, tau, w, wp);
+            interp_weights(tb.scheme, tau, w, wp);
             double z[M];
             for (int m = 0; m < M; ++m) {
                 double acc = 0;

@@ -41,8 +41,15 @@ class Options(C.Structure):
         ("bc_jac_exact", C.c_int32), ("linesearch_fallback", C.c_int32),
         ("stall_steps", C.c_int32), ("nthreads", C.c_int32),
         ("abstol", C.c_double), ("defect_threshold", C.c_double),
-        ("divergence_factor", C.c_double),
+        ("divergence_factor", C.c_double), ("mirk6i", C.c_int32),
     ]
+
+
+def stage_counts(order: int, mirk6i: int = 0):
+    """(discrete stages, extra interpolant stages >= 1) of MIRKn, or of MIRK6I."""
+    if mirk6i:
+        return 5, 3
+    return {2: 1, 3: 2, 4: 3, 5: 4, 6: 5}[order], max(1, {2: 2, 3: 1, 4: 1, 5: 2, 6: 4}[order])
 
 
 def _p(a, ct):
@@ -121,8 +128,7 @@ class Oracle:
             cap_nodes = int(max(int(n_int.max()) + 1, 4 * int(n_int.max()) + 1,
                                 o.max_subintervals + 1))
         M = self.M
-        s = {2: 1, 3: 2, 4: 3, 5: 4, 6: 5}[o.order]
-        ns = max(1, {2: 2, 3: 1, 4: 1, 5: 2, 6: 4}[o.order])
+        s, ns = stage_counts(o.order, o.mirk6i)
         out = dict(
             retcode=np.zeros(n, np.int32), n_nodes=np.zeros(n, np.int32),
             mesh=np.zeros((n, cap_nodes)), y=np.zeros((n, cap_nodes, M)),
@@ -153,35 +159,35 @@ class Oracle:
         y = np.ascontiguousarray(y, dtype=np.float64).reshape(len(mesh), self.M)
         return params, mesh, y
 
-    def residual(self, params, mesh, y, order=4):
+    def residual(self, params, mesh, y, order=4, mirk6i=0):
         params, mesh, y = self._prep(params, mesh, y)
         N, M = len(mesh), self.M
-        s = {2: 1, 3: 2, 4: 3, 5: 4, 6: 5}[order]
+        s = stage_counts(order, mirk6i)[0]
         F = np.zeros(N * M)
         K = np.zeros((N - 1, s, M))
-        o = self.options(order=order)
+        o = self.options(order=order, mirk6i=mirk6i)
         nrm = self.lib.oracle_residual(C.byref(self.info), C.byref(o), _p(params, C.c_double),
                                        C.c_int(N), _p(mesh, C.c_double), _p(y, C.c_double),
                                        _p(F, C.c_double), _p(K, C.c_double))
         return F, K, nrm
 
-    def jacobian(self, params, mesh, y, order=4, bc_jac_exact=0):
+    def jacobian(self, params, mesh, y, order=4, bc_jac_exact=0, mirk6i=0):
         params, mesh, y = self._prep(params, mesh, y)
         N, M = len(mesh), self.M
         S = np.zeros((N - 1, M, M)); R = np.zeros((N - 1, M, M))
         nodes = np.zeros(64, np.int32); blocks = np.zeros((64, M, M))
-        o = self.options(order=order, bc_jac_exact=bc_jac_exact)
+        o = self.options(order=order, bc_jac_exact=bc_jac_exact, mirk6i=mirk6i)
         nb = self.lib.oracle_jacobian(C.byref(self.info), C.byref(o), _p(params, C.c_double),
                                       C.c_int(N), _p(mesh, C.c_double), _p(y, C.c_double),
                                       _p(S, C.c_double), _p(R, C.c_double),
                                       _p(nodes, C.c_int32), _p(blocks, C.c_double))
         return S, R, nodes[:nb].copy(), blocks[:nb].copy()
 
-    def newton_step(self, params, mesh, y, order=4, bc_jac_exact=0):
+    def newton_step(self, params, mesh, y, order=4, bc_jac_exact=0, mirk6i=0):
         params, mesh, y = self._prep(params, mesh, y)
         N, M = len(mesh), self.M
         d = np.zeros(N * M)
-        o = self.options(order=order, bc_jac_exact=bc_jac_exact)
+        o = self.options(order=order, bc_jac_exact=bc_jac_exact, mirk6i=mirk6i)
         rc = self.lib.oracle_newton_step(C.byref(self.info), C.byref(o), _p(params, C.c_double),
                                          C.c_int(N), _p(mesh, C.c_double), _p(y, C.c_double),
                                          _p(d, C.c_double))
@@ -189,17 +195,17 @@ class Oracle:
             raise RuntimeError("singular system")
         return d.reshape(N, M)
 
-    def defect(self, params, mesh, y, order=4):
+    def defect(self, params, mesh, y, order=4, mirk6i=0):
         params, mesh, y = self._prep(params, mesh, y)
         N = len(mesh)
         err = np.zeros(N - 1)
-        o = self.options(order=order)
+        o = self.options(order=order, mirk6i=mirk6i)
         dn = self.lib.oracle_defect(C.byref(self.info), C.byref(o), _p(params, C.c_double),
                                     C.c_int(N), _p(mesh, C.c_double), _p(y, C.c_double),
                                     _p(err, C.c_double))
         return err, dn
 
-    def interpolate(self, order, mesh, y, K, KI, ts, deriv=0):
+    def interpolate(self, order, mesh, y, K, KI, ts, deriv=0, mirk6i=0):
         mesh = np.ascontiguousarray(mesh, dtype=np.float64)
         N = len(mesh)
         y = np.ascontiguousarray(y[:N], dtype=np.float64)
@@ -207,7 +213,7 @@ class Oracle:
         KI = np.ascontiguousarray(KI[:N - 1], dtype=np.float64)
         ts = np.ascontiguousarray(np.atleast_1d(ts), dtype=np.float64)
         out = np.zeros((len(ts), self.M))
-        self.lib.oracle_interpolate(C.c_int(order), C.c_int(N), _p(mesh, C.c_double),
+        self.lib.oracle_interpolate(C.c_int(7 if mirk6i else order), C.c_int(N), _p(mesh, C.c_double),
                                     _p(y, C.c_double), _p(K, C.c_double), _p(KI, C.c_double),
                                     C.c_int(len(ts)), _p(ts, C.c_double), C.c_int(deriv),
                                     _p(out, C.c_double))

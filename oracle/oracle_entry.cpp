@@ -74,7 +74,7 @@ int oracle_solve_batch(const ProblemInfo* info, const Options* opt, int n_inst,
                        int32_t* rounds, double* defect, double* resid, double* K_out,
                        double* KI_out) {
     if (info->M != MM) return -1;
-    const Tableau tb = make_tableau(opt->order);
+    const Tableau tb = make_tableau(opt->order, opt->mirk6i);
     if (tb.order == 0) return -2;
     std::vector<int64_t> y0_off(n_inst + 1, 0);
     for (int i = 0; i < n_inst; ++i)
@@ -129,7 +129,7 @@ int oracle_solve_batch(const ProblemInfo* info, const Options* opt, int n_inst,
 // ordering, K ((N-1) x s x M). Returns ||F||_inf.
 double oracle_residual(const ProblemInfo* info, const Options* opt, const double* params, int N,
                        const double* mesh, const double* y, double* F_out, double* K_out) {
-    const Tableau tb = make_tableau(opt->order);
+    const Tableau tb = make_tableau(opt->order, opt->mirk6i);
     InstanceSolver<MM> sv(tb, *opt, *info, params);
     sv.N = N;
     sv.mesh.assign(mesh, mesh + N);
@@ -147,7 +147,7 @@ double oracle_residual(const ProblemInfo* info, const Options* opt, const double
 int oracle_jacobian(const ProblemInfo* info, const Options* opt, const double* params, int N,
                     const double* mesh, const double* y, double* S_out, double* R_out,
                     int32_t* bc_nodes, double* bc_blocks) {
-    const Tableau tb = make_tableau(opt->order);
+    const Tableau tb = make_tableau(opt->order, opt->mirk6i);
     InstanceSolver<MM> sv(tb, *opt, *info, params);
     sv.N = N;
     sv.mesh.assign(mesh, mesh + N);
@@ -168,7 +168,7 @@ int oracle_jacobian(const ProblemInfo* info, const Options* opt, const double* p
 // One Newton step direction: solves J delta = -F at (mesh, y). Returns 0 on success.
 int oracle_newton_step(const ProblemInfo* info, const Options* opt, const double* params, int N,
                        const double* mesh, const double* y, double* delta_out) {
-    const Tableau tb = make_tableau(opt->order);
+    const Tableau tb = make_tableau(opt->order, opt->mirk6i);
     InstanceSolver<MM> sv(tb, *opt, *info, params);
     sv.N = N;
     sv.mesh.assign(mesh, mesh + N);
@@ -186,7 +186,7 @@ int oracle_newton_step(const ProblemInfo* info, const Options* opt, const double
 // Defect estimate on (mesh, y): per-interval max |defect| and the norm.
 double oracle_defect(const ProblemInfo* info, const Options* opt, const double* params, int N,
                      const double* mesh, const double* y, double* err_out) {
-    const Tableau tb = make_tableau(opt->order);
+    const Tableau tb = make_tableau(opt->order, opt->mirk6i);
     InstanceSolver<MM> sv(tb, *opt, *info, params);
     sv.N = N;
     sv.mesh.assign(mesh, mesh + N);
@@ -200,17 +200,17 @@ double oracle_defect(const ProblemInfo* info, const Options* opt, const double* 
 }
 
 // Interpolant u(t) (deriv 0) or u'(t) (deriv 1) of a solved instance given its mesh,
-// solution and stages (interpolation.jl:17-204).
+// solution and stages (interpolation.jl:17-204). order: 2..6, or 7 for MIRK6I.
 void oracle_interpolate(int order, int N, const double* mesh, const double* y, const double* K,
                         const double* KI, int n_t, const double* ts, int deriv, double* out) {
-    const Tableau tb = make_tableau(order);
+    const Tableau tb = order == 7 ? make_tableau(6, 1) : make_tableau(order);
     const int S = tb.s, NS = std::max(1, tb.s_star - tb.s), ns = tb.s_star - tb.s;
     for (int k = 0; k < n_t; ++k) {
         const int i = interval_of(mesh, N, ts[k]);
         const double dt = mesh[i + 1] - mesh[i];
         const double tau = (ts[k] - mesh[i]) / dt;
         double w[9], wp[9];
-        interp_weights(order, tau, w, wp);
+        interp_weights(tb.scheme, tau, w, wp);
         const double* wv = deriv ? wp : w;
         for (int m = 0; m < MM; ++m) {
             double acc = 0;

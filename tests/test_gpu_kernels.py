@@ -40,18 +40,24 @@ def _cases(problems, name, n_inst=6, seed=3, order=4):
 
 
 CASES = [("pendulum", 4), ("pendulum", 6), ("singular_perturbation", 6), ("multipoint", 4),
-         ("torus", 4), ("pendulum", 2), ("pendulum", 3), ("pendulum", 5)]
+         ("torus", 4), ("pendulum", 2), ("pendulum", 3), ("pendulum", 5),
+         ("pendulum", "6I"), ("singular_perturbation", "6I")]
+
+
+def _kw(order):
+    """Solver / oracle keywords of a case's scheme: MIRK2-6, or "6I" for MIRK6I."""
+    return dict(order=6, mirk6i=1) if order == "6I" else dict(order=order)
 
 
 @pytest.mark.parametrize("name,order", CASES)
 def test_k1_residual_matches_oracle(pkg, problems, name, order):
     p, params, meshes, ys = _cases(problems, name, order=order)
-    sv = pkg.BatchSolver(p, order=order)
+    sv = pkg.BatchSolver(p, **_kw(order))
     out = sv.eval_stage(0, params, meshes, ys)
     o = _oracle(p)
     off = out["offsets"]
     for q in range(len(meshes)):
-        F, K, nrm = o.residual(params[q], meshes[q], ys[q], order=order)
+        F, K, nrm = o.residual(params[q], meshes[q], ys[q], **_kw(order))
         N, M = len(meshes[q]), p.M
         La = p.La if p.twopoint else M
         colloc = F[La:La + (N - 1) * M].reshape(N - 1, M)
@@ -69,12 +75,12 @@ def test_k1_residual_matches_oracle(pkg, problems, name, order):
 def test_k2_jacobian_blocks_match_oracle(pkg, problems, name, order):
     # FP32 forward-mode blocks against the FP64 oracle: relative 2e-5 of the block scale
     p, params, meshes, ys = _cases(problems, name, order=order)
-    sv = pkg.BatchSolver(p, order=order)
+    sv = pkg.BatchSolver(p, **_kw(order))
     out = sv.eval_stage(1, params, meshes, ys)
     o = _oracle(p)
     off = out["offsets"]
     for q in range(len(meshes)):
-        S, R, nodes, blocks = o.jacobian(params[q], meshes[q], ys[q], order=order)
+        S, R, nodes, blocks = o.jacobian(params[q], meshes[q], ys[q], **_kw(order))
         N = len(meshes[q])
         gS = out["S"][off[q]:off[q] + N - 1]
         gR = out["R"][off[q]:off[q] + N - 1]
@@ -94,8 +100,8 @@ def _apply_jacobian(p, S, R, nodes, blocks, delta):
 
 
 def _backward_error(p, o, params, mesh, y, delta, order):
-    F, K, _ = o.residual(params, mesh, y, order=order)
-    S, R, nodes, blocks = o.jacobian(params, mesh, y, order=order)
+    F, K, _ = o.residual(params, mesh, y, **_kw(order))
+    S, R, nodes, blocks = o.jacobian(params, mesh, y, **_kw(order))
     N, M = len(mesh), p.M
     La = p.La if p.twopoint else M
     Fc = F[La:La + (N - 1) * M].reshape(N - 1, M)
@@ -111,13 +117,13 @@ def test_k3_newton_direction_fp64_matches_oracle(pkg, problems, name, order):
     # FP64 factorisation: the structured cyclic reduction agrees with the oracle's
     # sequential elimination to roundoff times the systems' conditioning
     p, params, meshes, ys = _cases(problems, name, order=order)
-    sv = pkg.BatchSolver(p, order=order, jac_precision=64)
+    sv = pkg.BatchSolver(p, jac_precision=64, **_kw(order))
     out = sv.eval_stage(2, params, meshes, ys)
     assert (out["norm"] == 0).all(), "singular system reported"
     o = _oracle(p)
     off = out["offsets"]
     for q in range(len(meshes)):
-        d = o.newton_step(params[q], meshes[q], ys[q], order=order)
+        d = o.newton_step(params[q], meshes[q], ys[q], **_kw(order))
         N = len(meshes[q])
         got = out["delta"][off[q]:off[q] + N]
         assert np.abs(got - d).max() <= 1e-8 * max(1.0, np.abs(d).max()), (q, np.abs(got - d).max())
@@ -130,7 +136,7 @@ def test_k3_newton_direction_fp32_backward_stable(pkg, problems, name, order):
     # residual of J δ = -F (evaluated in FP64 with the oracle's Jacobian) is at FP32
     # roundoff relative to |J||δ| + |F|; the forward error then follows the conditioning
     p, params, meshes, ys = _cases(problems, name, order=order)
-    sv = pkg.BatchSolver(p, order=order, jac_precision=32)
+    sv = pkg.BatchSolver(p, jac_precision=32, **_kw(order))
     out = sv.eval_stage(2, params, meshes, ys)
     assert (out["norm"] == 0).all(), "singular system reported"
     o = _oracle(p)
@@ -145,12 +151,12 @@ def test_k3_newton_direction_fp32_backward_stable(pkg, problems, name, order):
 @pytest.mark.parametrize("name,order", CASES)
 def test_k4_defect_matches_oracle(pkg, problems, name, order):
     p, params, meshes, ys = _cases(problems, name, order=order)
-    sv = pkg.BatchSolver(p, order=order)
+    sv = pkg.BatchSolver(p, **_kw(order))
     out = sv.eval_stage(3, params, meshes, ys)
     o = _oracle(p)
     off = out["offsets"]
     for q in range(len(meshes)):
-        err, dn = o.defect(params[q], meshes[q], ys[q], order=order)
+        err, dn = o.defect(params[q], meshes[q], ys[q], **_kw(order))
         N = len(meshes[q])
         got = out["err"][off[q]:off[q] + N - 1]
         assert np.abs(got - err).max() <= 1e-10 * max(1.0, np.abs(err).max())

@@ -294,3 +294,48 @@ def test_reference_style_solve(pkg, problems):
         n = int(refs["n_nodes"][i])
         assert s.successful and len(s.t) == n
         assert np.abs(s.u - refs["y"][i, :n]).max() <= 1e-6
+
+
+def test_mirk6i_golden_gpu(pkg, problems):
+    # MIRK6I through the reference's golden tests on the GPU: affineness
+    # (mirk_basic_tests.jl:113-116) and the observed order 6 (:134-137)
+    for name in ("affine", "affine_twopoint"):
+        p = problems.ALL[name]
+        res = pkg.BatchSolver(p, order=6, mirk6i=1).solve(np.zeros((1, 0)), [25], [[0, 5.0]], [p.u0])
+        assert res.retcode[0] == RET_SUCCESS
+        m, y = res.solution(0)
+        assert np.abs(np.diff(y[:, 0]) + 0.2).max() + abs(y[0, 0] - 5) < 1e-2
+    p = problems.LINEAR
+    sv = pkg.BatchSolver(p, order=6, mirk6i=1, adaptive=0, jac_precision=64, max_newton=20)
+    errs = []
+    for n in (40, 20, 10):
+        res = sv.solve(np.zeros((1, 0)), [n], [[0, 5.0]], [p.u0])
+        m, y = res.solution(0)
+        errs.append(np.abs(y - problems.linear_analytic(m)).max())
+    est = np.log2(np.array(errs[1:]) / np.array(errs[:-1])).mean()
+    assert abs(est - 6) < 0.4, (errs, est)
+
+
+def test_mirk6i_pendulum_parity_fp64(pkg, problems):
+    # MIRK6I adaptive solves of the pendulum family against the oracle: same retcodes, the
+    # oracle's final meshes, solutions within max(abstol, 1e-9 |u|), dense output equal to
+    # the oracle's interpolant of the same stages
+    p = problems.PENDULUM
+    params, nint, tsp, y0 = problems.pendulum_family(128, seed=91)
+    sv = pkg.BatchSolver(p, order=6, mirk6i=1, jac_precision=64, want_stages=1)
+    res = sv.solve(params, nint, tsp, y0)
+    o = _oracle(p)
+    ref = o.solve_batch(params, nint, tsp, y0, order=6, mirk6i=1)
+    assert (res.retcode == ref["retcode"]).all()
+    same, errs = _parity_report(res, ref)
+    assert same.mean() >= 0.99, same.mean()
+    u = np.array([np.abs(ref["y"][i, :ref["n_nodes"][i]]).max() for i in range(len(nint))])
+    assert (errs[same] <= np.maximum(1e-6, 1e-9 * u[same])).all(), errs[same].max()
+    tq = tsp[:, :1] + (tsp[:, 1:] - tsp[:, :1]) * np.linspace(0.013, 0.987, 7)[None, :]
+    for deriv in (0, 1):
+        d = sv.dense(tq, deriv=deriv)
+        for i in range(0, len(nint), 9):
+            m, y = res.solution(i)
+            K, KI = res.stages(i)
+            want = o.interpolate(6, m, y, K, KI, tq[i], deriv=deriv, mirk6i=1)
+            assert np.abs(d[i] - want).max() <= 1e-10 * max(1.0, np.abs(want).max())

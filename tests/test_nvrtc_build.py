@@ -1,5 +1,5 @@
 """The kernels compile through NVRTC for sm_103a exactly as bvp_create compiles them (same
-source assembly and options), for every MIRK order, both Jacobian precisions, standard and
+source assembly and options), for every MIRK order and MIRK6I, both Jacobian precisions, standard and
 two-point problems, the larger-state family and a problem with a singular term. NVRTC runs on
 the CPU, so this catches JIT-only compile errors without a GPU."""
 import pytest
@@ -13,6 +13,7 @@ CASES = [
     ("pendulum", 2, 32), ("pendulum", 3, 32), ("pendulum", 5, 64), ("pendulum", 6, 32),
     ("multipoint", 4, 32), ("affine_twopoint", 3, 64), ("torus", 4, 32),
     ("lane_emden", 6, 64), ("nonlinear32", 6, 32), ("nonlinear32", 4, 64), ("nonlinear32", 3, 32), ("mathieu", 4, 32),
+    ("pendulum", 6, 32, 1), ("singular_perturbation", 6, 64, 1), ("nonlinear32", 6, 32, 1),
 ]
 
 
@@ -21,7 +22,7 @@ def test_kernels_compile_with_nvrtc(pkg, problems):
         pytest.skip("libnvrtc not found")
     from concurrent.futures import ThreadPoolExecutor   # NVRTC releases the GIL
     with ThreadPoolExecutor(max_workers=8) as ex:
-        futs = {case: ex.submit(pkg._lib.nvrtc_check, problems.ALL[case[0]], case[1], case[2]) for case in CASES}
+        futs = {case: ex.submit(pkg._lib.nvrtc_check, problems.ALL[case[0]], *case[1:]) for case in CASES}
         for case, f in futs.items():
             f.result()   # raises with the NVRTC log for the failing case
 

@@ -190,3 +190,55 @@ def test_mathieu_eigenvalue(problems):
     N = int(r["n_nodes"][0])
     lam = r["y"][0, :N, 2]
     assert np.abs(lam - 17.09658).max() < 1e-4
+
+
+# MIRK6I (mirk_tableaus.jl:154-194, interpolation.jl:583-693): the reference runs it through
+# the same golden tests as MIRK2-6 (mirk_basic_tests.jl:113-116, 134-137, 241-266).
+@pytest.mark.parametrize("name", ["affine", "affine_twopoint"])
+def test_affineness_mirk6i(problems, name):
+    p = problems.ALL[name]
+    o, r, N = _solve1(p, dt=0.2, order=6, mirk6i=1)
+    assert r["retcode"][0] == RET_SUCCESS
+    u1 = r["y"][0, :N, 0]
+    assert np.abs(np.diff(u1) + 0.2).max() + abs(u1[0] - 5) < 1e-2
+
+
+@pytest.mark.parametrize("name", ["linear", "linear_twopoint"])
+def test_convergence_order_mirk6i(problems, name):
+    p = problems.ALL[name]
+    errs = []
+    for dt in (1 / 8, 1 / 4, 1 / 2):
+        o, r, N = _solve1(p, dt=dt, order=6, mirk6i=1, adaptive=0, max_newton=20)
+        assert r["retcode"][0] == RET_SUCCESS
+        t = r["mesh"][0, :N]
+        errs.append(np.abs(r["y"][0, :N] - problems.linear_analytic(t)).max())
+    errs = np.array(errs)
+    est = np.log2(errs[1:] / errs[:-1]).mean()
+    assert abs(est - 6) < 0.4, (errs, est)
+
+
+def test_interpolation_twopoint_mirk6i(problems):
+    p = problems.TWOPOINT_INTERP
+    o, r, N = _solve1(p, dt=0.001, params=(1.0,), order=6, mirk6i=1)
+    assert r["retcode"][0] == RET_SUCCESS
+    mesh, y, K, KI = r["mesh"][0, :N], r["y"][0], r["K"][0], r["KI"][0]
+    assert KI.shape[1] == 3
+    u, du = problems.twopoint_interp_analytic(np.array([0.001]))
+    assert np.abs(o.interpolate(6, mesh, y, K, KI, [0.001], mirk6i=1) - u).max() < 1e-6
+    u4, du4 = problems.twopoint_interp_analytic(np.array([0.04]))
+    assert np.abs(o.interpolate(6, mesh, y, K, KI, [0.04], mirk6i=1) - u4).max() < 1e-6
+    assert np.abs(o.interpolate(6, mesh, y, K, KI, [0.04], deriv=1, mirk6i=1) - du4).max() < 1e-6
+
+
+def test_mirk6i_interpolant_consistency(problems):
+    # the continuous extension reproduces the discrete step: at τ = 1 it equals y_{i+1} and its
+    # derivative at τ = 0, 1 equals f at the nodes (the weights satisfy w(1) = b, w'(0) = e1, w'(1) = e2)
+    p = problems.LINEAR
+    o, r, N = _solve1(p, dt=0.1, order=6, mirk6i=1, adaptive=0)
+    mesh, y, K, KI = r["mesh"][0, :N], r["y"][0], r["K"][0], r["KI"][0]
+    for i in (0, 3, N - 2):
+        h = mesh[i + 1] - mesh[i]
+        ends = o.interpolate(6, mesh, y, K, KI, [mesh[i] + 0.999999999 * h], mirk6i=1)[0]
+        assert np.abs(ends - y[i + 1]).max() < 1e-8
+        d0 = o.interpolate(6, mesh, y, K, KI, [mesh[i] + 1e-12 * h], deriv=1, mirk6i=1)[0]
+        assert np.abs(d0 - K[i, 0]).max() < 1e-8

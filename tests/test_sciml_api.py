@@ -98,3 +98,15 @@ def test_ensemble_and_dense_output(sciml, problems):
     sciml.solve(sciml.EnsembleProblem(p, params=params, tspans=tsp), sciml.MIRK6(), dt=0.1, _solver_cls=FakeSolver)
     with pytest.raises(ValueError, match="another batch"):
         sols[0](0.3)
+
+
+def test_mirk6i_algorithm_reaches_the_solver(sciml, problems):
+    # MIRK6I() (exported by the reference, BoundaryValueDiffEqMIRK.jl:179) selects the order-6
+    # scheme with its own tableau and interpolant
+    p = problems.PENDULUM
+    params, nint, tsp, y0 = problems.pendulum_family(3, seed=1)
+    sciml.solve(sciml.EnsembleProblem(p, params=params, tspans=tsp), sciml.MIRK6I(), dt=0.1, _solver_cls=FakeSolver)
+    kw = FakeSolver.created[-1].kw
+    assert kw["order"] == 6 and kw["mirk6i"] == 1
+    with pytest.raises(ValueError):
+        sciml.MIRK(4, mirk6i=True)
