@@ -106,6 +106,15 @@ BVP_DEV double warp_sum(double v) {
     return v;
 }
 BVP_DEV bool warp_any(bool b) { return __any_sync(FULL, b) != 0; }
+// a / b for 1 <= b <= 1e30 (the defect's |f| + 1 scaling): an FP32 reciprocal and one FP64
+// correction step, relative error ~1e-14 (the square of the reciprocal's), in a few FP64
+// operations instead of a full division; other b divide exactly.
+BVP_DEV double div_scaled(double a, double b) {
+    if (!(b >= 1.0 && b <= 1e30)) return a / b;
+    const double r = double(__frcp_rn(float(b)));
+    const double q = a * r;
+    return fma(fma(-b, q, a), r, q);
+}
 BVP_DEV double dinf() { return __longlong_as_double(0x7ff0000000000000LL); }
 
 // lower_bound(mesh, t) - 1 clamped to [0, N-2]: the reference's interval()
@@ -1303,7 +1312,7 @@ BVP_DEV double defect(const Args& a, const Inst& I) {
             call_f<double, double>(fz, z, I.p, mesh[i] + (smp ? 1.0 - tau_star() : tau_star()) * h[i]);
             double e = 0.0;
 #pragma unroll
-            for (int m = 0; m < M; ++m) e = fmax(e, fabs((zp[m] - fz[m]) / (fabs(fz[m]) + 1.0)));
+            for (int m = 0; m < M; ++m) e = fmax(e, fabs(div_scaled(zp[m] - fz[m], fabs(fz[m]) + 1.0)));
             est[smp] = e;
         }
         const double ei = est[0] > est[1] ? est[0] : est[1];
@@ -1317,19 +1326,24 @@ BVP_DEV double defect(const Args& a, const Inst& I) {
 }
 
 // ---- mesh selection (adaptivity.jl:23-75, 250-304) -------------------------------------------
-// half_mesh! of buffer src into buffer dst
+// half_mesh! of buffer src into buffer dst. Each new node's old interval (the one the
+// reference's interval() finds for it, lower_bound - 1 clamped) goes to iold as a hint for
+// the solution transfer.
 BVP_DEV void half_mesh(const Args& a, Inst& I, int src, int dst) {
     const double* m0 = mesh_of(a, I, src);
     const double* h0 = h_of(a, I, src);
     double* m1 = mesh_of(a, I, dst);
     double* h1 = h_of(a, I, dst);
+    int* io = a.iold + I.nb;
     const int n = I.N - 1;
     for (int i = lane_id(); i <= n; i += 32) {
         m1[2 * i] = m0[i];
+        io[2 * i] = i > 0 ? i - 1 : 0;
         if (i < n) {
             m1[2 * i + 1] = (m0[i + 1] + m0[i]) / 2.0;
             h1[2 * i] = h0[i] / 2.0;
             h1[2 * i + 1] = h0[i] / 2.0;
+            io[2 * i + 1] = i;
         }
     }
     __syncwarp();
@@ -1337,24 +1351,53 @@ BVP_DEV void half_mesh(const Args& a, Inst& I, int src, int dst) {
 
 BVP_DEV long round_even(double x) { return (long)rint(x); }
 
-// Returns 1 on success (new mesh in buffer cur^1, newN set), 0 on Failure.
+// x^(1/(p+1)), the selector's ŝ = (err/abstol)^(1/(p+1)) (adaptivity.jl:43): an FP32 seed
+// refined by two Newton steps on y^(p+1) = x in FP64 (the derivative's reciprocal taken in
+// FP32: the first step leaves ~1e-14, the second the FP64 roundoff of y^(p+1)), a dozen FP64
+// operations instead of a double-precision pow. Zero, extreme and non-finite arguments go
+// to pow.
+BVP_DEV double root_p1(double x) {
+    constexpr int P = ORD + 1;
+    if (!(x >= 1e-30 && x <= 1e30)) return pow(x, 1.0 / P);
+    double y = double(powf(float(x), 1.0f / float(P)));
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        double ypm1 = y;
+#pragma unroll
+        for (int k = 2; k < P; ++k) ypm1 *= y;                 // y^(P-1)
+        const double r = fma(ypm1, y, -x);                     // y^P - x
+        const float c = 1.0f / (float(P) * float(ypm1));
+        y = fma(-r, double(c), y);
+    }
+    return y;
+}
+
+// Returns 1 on success (new mesh in buffer cur^1, newN set, iold hints written), 0 on Failure.
+//
+// redistribute! (adaptivity.jl:250-278) places Nsub - 1 interior points so that each
+// subinterval holds the same share ζ = Σ ŝ / Nsub of the piecewise-constant density ŝ_k / h_k.
+// The reference walks the mesh sequentially; here the cumulative density is a warp scan
+// (each lane a contiguous block of old intervals, running sums inside the block), point j
+// lies in the old interval k whose cumulative range (C_k, C_k+1] holds j ζ, at
+// t_k + (j ζ - C_k) h_k / ŝ_k. The point indices per interval come from floor(C / ζ) with a
+// running maximum across the warp, so every point 1..Nsub-1 is placed exactly once even
+// where the block sums round differently from the running sums. The positions agree with
+// the sequential walk to rounding (same formula, different association).
 BVP_DEV int mesh_selector(const Args& a, Inst& I, int& newN) {
     const int lane = lane_id();
     const int n = I.N - 1;
     const double* h0 = h_of(a, I, I.cur);
     double* e = a.err + I.nb;
-    const double ex = 1.0 / (ORD + 1);
-    double r1 = -dinf(), r2 = 0.0;
+    const double inv_tol = 1.0 / a.abstol;
+    double r1 = -dinf(), r2p = 0.0;
     for (int i = lane; i < n; i += 32) {
-        const double sh = pow(e[i] / a.abstol, ex);
+        const double sh = root_p1(e[i] * inv_tol);
         e[i] = sh;
         r1 = fmax(r1, sh);
+        r2p += sh;
     }
-    __syncwarp();
     r1 = warp_max(r1);
-    // the reference sums sequentially; keep that order
-    if (lane == 0) for (int i = 0; i < n; ++i) r2 += e[i];
-    r2 = __shfl_sync(FULL, r2, 0);
+    const double r2 = warp_sum(r2p);
     const double r3 = r2 / (I.N - 1);
     long n_pred = round_even(1.3 * r2 + 1);
     const double n_ = 0.1 * n;
@@ -1367,87 +1410,158 @@ BVP_DEV int mesh_selector(const Args& a, Inst& I, int& newN) {
         return 1;
     }
     const long lb = I.N / 2, ub = 4L * (I.N - 1);
-    long Nsub = n_pred < lb ? lb : n_pred;
-    Nsub = Nsub > ub ? ub : Nsub;
-    if (Nsub > a.max_sub || Nsub + 1 > I.cap) return 0;
-    for (int i = lane; i < n; i += 32) e[i] /= h0[i];
-    __syncwarp();
+    long Nl = n_pred < lb ? lb : n_pred;
+    Nl = Nl > ub ? ub : Nl;
+    if (Nl > a.max_sub || Nl + 1 > I.cap) return 0;
+    const int Nsub = int(Nl);
     const double* om = mesh_of(a, I, I.cur);
     double* nm = mesh_of(a, I, dst);
     double* nh = h_of(a, I, dst);
-    if (lane == 0) {
-        // redistribute! (adaptivity.jl:250-278), sequential as in the reference
-        double tot = 0.0;
-        for (int k = 0; k < n; ++k) tot += e[k] * h0[k];
-        const double zeta = tot / double(Nsub);
-        nm[0] = om[0];
-        double t = om[0], integral = 0.0;
-        int k = 0, i = 0;
-        long guard = 4L * (n + Nsub) + 64;  // each pass advances k or places a point
-        while (k < n && --guard > 0) {
-            const double next_piece = e[k] * (om[k + 1] - t);
-            const double int_next = integral + next_piece;
-            if (int_next > zeta) {
-                const double pt = (zeta - integral) / e[k] + t;
-                if (i + 1 < Nsub) nm[i + 1] = pt;
-                t = pt; ++i; integral = 0.0;
-            } else {
-                integral = int_next; t = om[k + 1]; ++k;
-            }
+    int* io = a.iold + I.nb;
+    double* cbeg = a.F + I.nb * M;         // C_k per old interval (the residual is recomputed next round)
+    // 1. block sums of ŝ and their exclusive scan
+    const int per = (n + 31) >> 5;
+    const int k0 = min(lane * per, n), k1 = min(k0 + per, n);
+    double bsum = 0.0;
+    for (int k = k0; k < k1; ++k) bsum += e[k];
+    double incl = bsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const double tot = __shfl_sync(FULL, incl, 31);
+    const double zeta = tot / double(Nsub);
+    const double izeta = double(Nsub) / tot;
+    double base = __shfl_up_sync(FULL, incl, 1);
+    if (lane == 0) base = 0.0;
+    auto jof = [&](double c) {
+        const double q = floor(c * izeta);
+        return q >= double(Nsub - 1) ? Nsub - 1 : (q > 0.0 ? int(q) : 0);
+    };
+    // 2. first point index of each lane's block: running maximum of the block ends' indices
+    double cend = base;
+    for (int k = k0; k < k1; ++k) cend += e[k];
+    int jm = k1 > k0 ? jof(cend) : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULL, jm, o);
+        if (lane >= o) jm = max(jm, t);
+    }
+    int jlo = __shfl_up_sync(FULL, jm, 1);
+    if (lane == 0) jlo = 0;
+    // 3. each old interval's points: their interval in iold, C_k and h_k / ŝ_k for the positions
+    double c = base;
+    for (int k = k0; k < k1; ++k) {
+        const double P = e[k];
+        const double cn = c + P;
+        const int jhi = max(jlo, jof(cn));
+        if (jhi > jlo) {
+            cbeg[k * M] = c;
+            e[k] = P > 0.0 ? h0[k] / P : 0.0;
+            for (int j = jlo + 1; j <= jhi; ++j) io[j] = k;
         }
-        nm[Nsub] = om[n];
+        jlo = jhi;
+        c = cn;
+    }
+    if (lane == 0) { io[0] = 0; io[Nsub] = n - 1; }
+    __syncwarp();
+    // 4. the points
+    for (int j = lane; j <= Nsub; j += 32) {
+        double pt;
+        if (j == 0) pt = om[0];
+        else if (j == Nsub) pt = om[n];
+        else {
+            const int k = io[j];
+            pt = fma(fma(double(j), zeta, -cbeg[k * M]), e[k], om[k]);
+            pt = fmin(fmax(pt, om[k]), om[k + 1]);
+        }
+        nm[j] = pt;
     }
     __syncwarp();
     for (int q = lane; q < Nsub; q += 32) nh[q] = nm[q + 1] - nm[q];
     __syncwarp();
-    newN = int(Nsub + 1);
+    newN = Nsub + 1;
     return 1;
 }
 
-// New solution on mesh buffer cur^1 from the old interpolant (adaptivity.jl:6-13 as
-// called in mirk.jl:366-371). With transfer_inplace the reference's in-place update is
-// reproduced: node j reads y[i_old] after nodes < j were already overwritten.
+// New solution on mesh buffer cur^1 from the old interpolant (adaptivity.jl:6-13 as called in
+// mirk.jl:366-371). With transfer_inplace the reference's in-place update is reproduced:
+// node j reads y[i_old] after nodes < j were already overwritten, so its base is the new value
+// of node i_old when i_old < j and the old one otherwise. Lanes take 32 consecutive nodes at a
+// time; a base inside the same 32 comes from that lane by shuffles, in dependency order (each
+// node depends on an earlier one, so the chain ends), which reproduces the sequential values
+// exactly. The old interval of each node is the mesh selector's hint, checked against the
+// interval() rule (lower_bound - 1, clamped) and searched for when it does not hold.
 BVP_DEV void transfer(const Args& a, Inst& I, int newN) {
     const int lane = lane_id();
     const int src = I.cur, dst = I.cur ^ 1;
+    const int No = I.N;
     const double* om = mesh_of(a, I, src);
     const double* oh = h_of(a, I, src);
     const double* nm = mesh_of(a, I, dst);
     const double* oy = y_of(a, I, src);
     double* ny = y_of(a, I, dst);
-    double* inc = a.inc + I.nb * M;
-    int* io = a.iold + I.nb;
-    for (int j = lane; j < newN; j += 32) {
-        const double t = nm[j];
-        const int i = interval_of(om, I.N, t);
-        const double dt = oh[i];
-        const double tau = (t - om[i]) / dt;
-        double w[SS], wp[SS];
-        interp_weights_rt(tau, w, wp);
-        const double* Kg = a.K + (I.nb + i) * (S * M);
-        const double* KIg = a.KI + (I.nb + i) * (NSXA * M);
+    const int* io = a.iold + I.nb;
+    const bool inplace = a.transfer_inplace != 0;
+    for (int c0 = 0; c0 < newN; c0 += 32) {
+        const int j = c0 + lane;
+        const bool act = j < newN;
+        double v[M];
+        int i = 0;
+        if (act) {
+            const double t = nm[j];
+            i = io[j];
+            const bool hint = i >= 0 && i <= No - 2 && (i == 0 || om[i] < t) && (i == No - 2 || t <= om[i + 1]);
+            if (!hint) i = interval_of(om, No, t);
+            const double dt = oh[i];
+            const double tau = (t - om[i]) / dt;
+            double w[SS], wp[SS];
+            interp_weights_rt(tau, w, wp);
+            const double* Kg = a.K + (I.nb + i) * (S * M);
+            const double* KIg = a.KI + (I.nb + i) * (NSXA * M);
 #pragma unroll
-        for (int m = 0; m < M; ++m) {
-            double acc = Kg[m] * w[0];
+            for (int m = 0; m < M; ++m) {
+                double acc = Kg[m] * w[0];
 #pragma unroll
-            for (int r = 1; r < S; ++r) acc += Kg[r * M + m] * w[r];
+                for (int r = 1; r < S; ++r) acc += Kg[r * M + m] * w[r];
 #pragma unroll
-            for (int qq = 0; qq < NSX; ++qq) acc += KIg[qq * M + m] * w[S + qq];
-            if (a.transfer_inplace) inc[j * M + m] = acc * dt;
-            else ny[j * M + m] = acc * dt + oy[i * M + m];
+                for (int qq = 0; qq < NSX; ++qq) acc += KIg[qq * M + m] * w[S + qq];
+                v[m] = acc * dt;
+            }
         }
-        io[j] = i;
-    }
-    __syncwarp();
-    if (a.transfer_inplace && lane == 0) {
-        for (int j = 0; j < newN; ++j) {
-            const int i = io[j];
-            const double* base = (i < j) ? ny + i * M : oy + i * M;
+        if (!inplace) {
+            if (act) {
 #pragma unroll
-            for (int m = 0; m < M; ++m) ny[j * M + m] = inc[j * M + m] + base[m];
+                for (int m = 0; m < M; ++m) ny[j * M + m] = v[m] + oy[i * M + m];
+            }
+        } else {
+            double val[M];
+            bool done = !act || i >= j || i < c0;
+            if (act) {
+                const double* b = i >= j ? oy + i * M : ny + i * M;
+#pragma unroll
+                for (int m = 0; m < M; ++m) val[m] = done ? v[m] + b[m] : 0.0;
+            }
+            const int from = (i - c0) & 31;
+            while (__any_sync(FULL, !done)) {
+                const int sd = __shfl_sync(FULL, int(done), from);
+                double sv[M];
+#pragma unroll
+                for (int m = 0; m < M; ++m) sv[m] = __shfl_sync(FULL, act ? val[m] : 0.0, from);
+                if (!done && sd) {
+#pragma unroll
+                    for (int m = 0; m < M; ++m) val[m] = v[m] + sv[m];
+                    done = true;
+                }
+            }
+            if (act) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) ny[j * M + m] = val[m];
+            }
         }
+        __syncwarp();
     }
-    __syncwarp();
 }
 
 // ---- one instance, whole adaptive solve (solve!, mirk.jl:286-388) -----------------------------

@@ -195,6 +195,20 @@ class Oracle:
             raise RuntimeError("singular system")
         return d.reshape(N, M)
 
+    def collocation_root(self, params, mesh, y, order=4, mirk6i=0, max_steps=8):
+        """The exact root of the collocation equations on a fixed mesh, reached from y by
+        Newton steps with the exact Jacobian (the BC rows chained through the interpolant's
+        stages); used to measure how far an accepted iterate (||F||_inf <= abstol) lies from
+        the discrete solution it approximates."""
+        params, mesh, y = self._prep(params, mesh, y)
+        y = y.copy()
+        for _ in range(max_steps):
+            d = self.newton_step(params, mesh, y, order=order, bc_jac_exact=1, mirk6i=mirk6i)
+            y += d
+            if np.abs(d).max() <= 1e-14 * max(1.0, np.abs(y).max()):
+                break
+        return y
+
     def defect(self, params, mesh, y, order=4, mirk6i=0):
         params, mesh, y = self._prep(params, mesh, y)
         N = len(mesh)
