@@ -668,9 +668,12 @@ void bvp_mlp_destroy(bvp_mlp* n) {
 }  // extern "C"
 
 // ---- forward without allocation ------------------------------------------------------------
-// bvp_mlp_forward_noalloc runs the forward's kernels on scratch carved from this static
-// device array instead of the network's cudaMalloc'd activation buffers: two BF16 activation
-// buffers used in turn (layer input / layer output) and one FP32 pre-activation buffer.
+// bvp_mlp_forward_noalloc: a network the fused kernel takes (every width <= 256 and, past the
+// input, a multiple of 8) runs k_mlp_forward_fused, which needs no scratch beyond shared
+// memory. Any other network runs the layer-by-layer kernels on scratch carved from this
+// static device array instead of the network's cudaMalloc'd activation buffers: two BF16
+// activation buffers used in turn (layer input / layer output) and one FP32 pre-activation
+// buffer.
 static __device__ __align__(256) unsigned char bvp_mlp_static_scratch[BVP_MLP_NOALLOC_SCRATCH_BYTES];
 
 namespace {
@@ -683,6 +686,11 @@ size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
 
 extern "C" bvp_status bvp_mlp_forward_noalloc(bvp_mlp* n, int32_t B, const float* d_x, float* d_y, void* stream) {
     if (!n || B < 1 || !d_x || !d_y) return BVP_ERR_INVALID;
+    const cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : n->stream;
+    if (n->fused) {
+        infer(n, B, d_x, d_y, s);
+        return cudaGetLastError() == cudaSuccess ? BVP_OK : BVP_ERR_CUDA;
+    }
     int wmax = 0;
     for (int v : n->w) wmax = std::max(wmax, v);
     const size_t hb = round256(size_t(B) * wmax * sizeof(bf16)), zb = round256(size_t(B) * wmax * sizeof(float));
@@ -704,7 +712,6 @@ extern "C" bvp_status bvp_mlp_forward_noalloc(bvp_mlp* n, int32_t B, const float
     bf16* hin = reinterpret_cast<bf16*>(scr);
     bf16* hout = reinterpret_cast<bf16*>(scr + hb);
     float* Z = reinterpret_cast<float*>(scr + 2 * hb);
-    const cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int L = n->L;
     const float* nrm = n->d_norm;
     const long long w0 = n->w[0], wL = n->w[L];

@@ -1483,10 +1483,12 @@ bvp_status bvp_dense_output(bvp_handle* h, int32_t nq, const double* tq, int32_t
     if (nq < 1 || !tq || !out) return fail(h, BVP_ERR_INVALID, "invalid arguments");
     const int n = h->last_n, M = h->L.M;
     DevBuf dt, dout;
-    if (!ensure_dev(dt, size_t(n) * nq * 8) || !ensure_dev(dout, size_t(n) * nq * M * 8))
-        return fail(h, BVP_ERR_NOMEM, "device allocation failed");
     bvp_status s = BVP_OK;
     do {
+        if (!ensure_dev(dt, size_t(n) * nq * 8) || !ensure_dev(dout, size_t(n) * nq * M * 8)) {
+            s = fail(h, BVP_ERR_NOMEM, "device allocation failed");
+            break;
+        }
         if (cudaMemcpyAsync(dt.p, tq, size_t(n) * nq * 8, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "H2D"); break; }
         int nqq = nq, dv = deriv;
         const double* tp = static_cast<const double*>(dt.p);
@@ -1506,8 +1508,8 @@ bvp_status bvp_dense_output(bvp_handle* h, int32_t nq, const double* tq, int32_t
         if (cudaMemcpyAsync(out, dout.p, size_t(n) * nq * M * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "D2H"); break; }
         if (cudaStreamSynchronize(h->stream) != cudaSuccess) { s = fail(h, BVP_ERR_CUDA, "sync"); break; }
     } while (0);
-    cudaFree(dt.p);
-    cudaFree(dout.p);
+    if (dt.p) cudaFree(dt.p);
+    if (dout.p) cudaFree(dout.p);
     return s;
 }
 

@@ -113,8 +113,9 @@ class MLP:
         self._check(st, "bvp_mlp_forward_device")
 
     def forward_noalloc(self, d_x, d_y, batch, stream=None):
-        """forward_device on the library's static scratch (bvp_mlp_forward_noalloc): no
-        device allocation; batch x widest layer is bounded by BVP_MLP_NOALLOC_SCRATCH_BYTES."""
+        """forward_device without any device allocation (bvp_mlp_forward_noalloc): the fused
+        kernel when the network fits it, else the layer-by-layer kernels on the library's static
+        scratch, where batch x widest layer is bounded by BVP_MLP_NOALLOC_SCRATCH_BYTES."""
         def ptr(v):
             return C.c_void_p(v.data_ptr() if hasattr(v, "data_ptr") else int(v))
         st = self.lib.bvp_mlp_forward_noalloc(self.h, batch, ptr(d_x), ptr(d_y), C.c_void_p(stream) if stream else None)

@@ -191,19 +191,24 @@ bvp_status bvp_mlp_train(bvp_mlp* net, int32_t n, const float* x, const float* t
                          int32_t batch, float lr, uint64_t seed, float* last_loss);
 /* Device-pointer forward on the given stream (cudaStream_t as void*); no synchronisation. */
 bvp_status bvp_mlp_forward_device(bvp_mlp* net, int32_t batch, const float* d_x, float* d_y, void* stream);
-/* The same forward as bvp_mlp_forward_device (same kernels, same results) for callers that
- * must not allocate device memory during the call: a serving loop that runs under a fixed
- * memory budget, or code that enqueues work where cudaMalloc would synchronise the device.
- * It has no counterpart in the reference. Its scratch (two BF16 activation buffers and one
- * FP32 pre-activation buffer of batch x widest-layer elements, each rounded up to 256
- * bytes) is carved from one static device array of BVP_MLP_NOALLOC_SCRATCH_BYTES; a batch
- * that does not fit returns BVP_ERR_TOO_LARGE before any work (4096 rows of a 256-wide
- * network fit exactly). Nothing in the scratch needs to start at zero: every element the
- * call reads is written earlier in the same call. The first call on a device looks up the
- * array's address with that device current (module set-up) and caches it; make that first
- * call before any stream capture. The scratch is shared by every call on a device: calls
- * that overlap in time (different streams or threads) race; calls on one stream are
- * ordered and safe. Devices 0..63. */
+/* The forward of bvp_mlp_forward_device, with the same results, for callers that must not
+ * allocate device memory during the call: a serving loop that runs under a fixed memory
+ * budget, or code that enqueues work where cudaMalloc would synchronise the device. It has
+ * no counterpart in the reference. A network every one of whose widths is at most 256 (and,
+ * past the input, a multiple of 8) runs the single fused kernel bvp_mlp_forward_device runs
+ * for it, which needs no scratch, for any batch. Any other network runs the layer-by-layer
+ * kernels bvp_mlp_forward_device runs for it, on scratch (two BF16 activation buffers and
+ * one FP32 pre-activation buffer of batch x widest-layer elements, each rounded up to 256
+ * bytes) carved from one static device array of BVP_MLP_NOALLOC_SCRATCH_BYTES; a batch that
+ * does not fit returns BVP_ERR_TOO_LARGE before any work (8 MiB holds 4096 rows of a
+ * 256-wide network, 2048 of a 512-wide one). Nothing in the scratch needs to start at zero:
+ * every element the call reads is written earlier in the same call. A null stream means the
+ * network's own stream, as for bvp_mlp_forward_device. The first call on a device looks up
+ * the array's address with that device current (module set-up) and caches it for the
+ * process; make that first call before any stream capture. The cached address does not
+ * survive cudaDeviceReset (the library does not see the reset; use a new process). The
+ * scratch is shared by every call on a device: calls that overlap in time (different
+ * streams or threads) race; calls on one stream are ordered and safe. Devices 0..63. */
 #define BVP_MLP_NOALLOC_SCRATCH_BYTES (8u << 20)
 bvp_status bvp_mlp_forward_noalloc(bvp_mlp* net, int32_t batch, const float* d_x, float* d_y, void* stream);
 /* Resample guesses given on a uniform grid of n_grid points over each instance's tspan
