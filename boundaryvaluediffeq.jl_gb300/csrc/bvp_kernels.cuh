@@ -1587,8 +1587,9 @@ BVP_DEV void init_instance(const Args& a, Inst& I) {
         // the initial mesh (separately rounded products and sum, as the host resampling does)
         const int G = a.n_grid;
         const float* gq = a.y0_grid + (long long)I.q * G * M;
+        const double inv_n = 1.0 / double(n);
         for (int j = lane; j <= n; j += 32) {
-            const double sg = __dmul_rn(double(j) / double(n), double(G - 1));
+            const double sg = __dmul_rn(__dmul_rn(double(j), inv_n), double(G - 1));
             int i0 = int(floor(sg));
             i0 = i0 < 0 ? 0 : (i0 > G - 2 ? G - 2 : i0);
             const double f = sg - i0;
@@ -1762,7 +1763,9 @@ extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::
         bvp::Inst I = bvp::make_inst(a, a.order[k]);
         if (bvp::SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
         I.dns = s_dns[w];
+        const long long c0 = a.inst_cost ? clock64() : 0;
         bvp::solve_instance(a, I);
+        if (a.inst_cost && lane == 0) a.inst_cost[I.q] = float(clock64() - c0) * (1.0f / 2000.0f);
     }
 }
 
@@ -1933,7 +1936,8 @@ extern "C" __global__ void bvp_convert_params(const double* p, bvp::JT* pj, long
 // behind them and finish while the machine drains (measured on the 4096-instance pendulum
 // batch: about 11% less time than largest-first).
 extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_init, int max_sub, int* cap,
-                                                            long long* node_off, int* order, int* counter) {
+                                                            long long* node_off, int* order, int* counter,
+                                                            const float* cost_tab) {
     constexpr int NB = 4096;
     __shared__ int hist[NB];
     __shared__ long long wsum[32];
@@ -1974,10 +1978,19 @@ extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_
         if (tid == 0) carry += wsum[31];
         __syncthreads();
     }
-    for (int q = tid; q < n; q += blockDim.x) {
-        const int key = n_init[q] < NB - 1 ? n_init[q] : NB - 1;
-        atomicAdd(&hist[key], 1);
-    }
+    // sort key: the learned cost (longest first) when the handle has a cost table, else the
+    // initial interval count (coarsest first)
+    const float cmax = cost_tab ? cost_tab[BVP_COST_BUCKETS] : 0.0f;
+    auto key_of = [&](int q) {
+        const int ni = n_init[q];
+        if (cmax > 0.0f) {
+            const float c = cost_tab[min(ni >> 3, BVP_COST_BUCKETS - 1)];
+            const int kq = int(fminf(fmaxf(c / cmax, 0.0f), 1.0f) * float(NB - 1));
+            return NB - 1 - kq;
+        }
+        return ni < NB - 1 ? ni : NB - 1;
+    };
+    for (int q = tid; q < n; q += blockDim.x) atomicAdd(&hist[key_of(q)], 1);
     __syncthreads();
     if (warp == 0) {
         constexpr int PER = NB / 32;
@@ -1998,8 +2011,54 @@ extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_
     }
     __syncthreads();
     for (int q = tid; q < n; q += blockDim.x) {
-        const int key = n_init[q] < NB - 1 ? n_init[q] : NB - 1;
-        const int pos = atomicAdd(&hist[key], 1);
+        const int pos = atomicAdd(&hist[key_of(q)], 1);
         order[pos] = q;
     }
+}
+
+// The work-order autotuner's update after a solve that recorded its instances' times: the
+// mean time per initial-size bucket, blended half and half with the table's earlier value
+// where the table has one; a bucket without instances takes the value of the nearest measured
+// bucket below it (above it, before the first); the largest value goes to
+// tab[BVP_COST_BUCKETS]. One block.
+extern "C" __global__ void __launch_bounds__(1024) bvp_learn_costs(int n, const int* n_init, const float* cost,
+                                                                   float* tab, int blend) {
+    __shared__ float s_sum[BVP_COST_BUCKETS];
+    __shared__ int s_cnt[BVP_COST_BUCKETS];
+    const int tid = threadIdx.x;
+    for (int b = tid; b < BVP_COST_BUCKETS; b += blockDim.x) { s_sum[b] = 0.0f; s_cnt[b] = 0; }
+    __syncthreads();
+    for (int q = tid; q < n; q += blockDim.x) {
+        const int b = min(n_init[q] >> 3, BVP_COST_BUCKETS - 1);
+        atomicAdd(&s_sum[b], cost[q]);
+        atomicAdd(&s_cnt[b], 1);
+    }
+    __syncthreads();
+    for (int b = tid; b < BVP_COST_BUCKETS; b += blockDim.x) {
+        if (s_cnt[b] > 0) {
+            const float m = s_sum[b] / float(s_cnt[b]);
+            s_sum[b] = (blend && tab[b] > 0.0f) ? 0.5f * (tab[b] + m) : m;
+        } else {
+            s_sum[b] = blend ? tab[b] : 0.0f;
+            s_cnt[b] = s_sum[b] > 0.0f ? 1 : 0;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float last = 0.0f, mx = 0.0f;
+        int seen = -1;
+        for (int b = 0; b < BVP_COST_BUCKETS; ++b) {
+            if (s_cnt[b] > 0) {
+                if (seen < 0) for (int c = 0; c < b; ++c) s_sum[c] = s_sum[b];   // leading gap
+                last = s_sum[b];
+                seen = b;
+                mx = fmaxf(mx, last);
+            } else if (seen >= 0) {
+                s_sum[b] = last;                                              // trailing and inner gaps
+            }
+        }
+        tab[BVP_COST_BUCKETS] = mx;
+    }
+    __syncthreads();
+    for (int b = tid; b < BVP_COST_BUCKETS; b += blockDim.x) tab[b] = s_sum[b];
 }

@@ -204,8 +204,9 @@ __global__ void k_resample(int n_inst, int n_grid, int M, const float* grid, con
     const int n = nint[q];
     const float* gq = grid + (long long)q * n_grid * M;
     double* out = y0 + off[q] * M;
+    const double inv_n = 1.0 / double(n);
     for (int j = threadIdx.x; j <= n; j += blockDim.x) {
-        const double s = __dmul_rn(double(j) / double(n), double(n_grid - 1));
+        const double s = __dmul_rn(__dmul_rn(double(j), inv_n), double(n_grid - 1));
         int i0 = int(floor(s));
         i0 = i0 < 0 ? 0 : (i0 > n_grid - 2 ? n_grid - 2 : i0);
         const double f = s - i0;

@@ -77,7 +77,13 @@ struct BvpArgs {
     BvpInstState* host_st;
     unsigned long long* out_cursor;
     bvp_i64 host_cap;              // points the host arrays hold
+    float* inst_cost;              // per instance: solve time (SM cycles / 2000), recorded while
+                                   // the handle learns its work order (null: not recorded)
 };
+
+// Work-order cost table of the fused solve: the mean solve time of the instances whose initial
+// interval count falls in each bucket (n_init >> 3), learned from a handle's first solves.
+#define BVP_COST_BUCKETS 512
 
 // Launch arguments of the larger-state kernels (M > 8, bvp_large.cuh): one instance per CTA or
 // per grid row, the Newton and mesh rounds driven from the host.

@@ -54,7 +54,13 @@ struct bvp_handle_s {
     cudaStream_t stream = nullptr;
     cudaLibrary_t lib = nullptr;
     cudaKernel_t k_fused = nullptr, k_stage = nullptr, k_pack = nullptr, k_probe = nullptr, k_offsets = nullptr,
-                 k_convert = nullptr, k_prep = nullptr, k_dense = nullptr;
+                 k_convert = nullptr, k_prep = nullptr, k_dense = nullptr, k_learn = nullptr;
+    // work-order autotuner of the fused solve: the first solves of at least kLearnMin instances
+    // record every instance's solve time; bvp_learn_costs folds them into a cost table per
+    // initial-size bucket, and bvp_prep orders later solves longest first from it
+    DevBuf d_inst_cost, d_cost_tab;
+    int learn_left = 3;
+    bool have_tab = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     // larger-state path (M > 8, bvp_large.cuh)
     bool large = false;
@@ -268,6 +274,7 @@ static bvp_status compile_and_load(bvp_handle* h) {
     CU(cudaLibraryGetKernel(&h->k_convert, h->lib, "bvp_convert_params"));
     CU(cudaLibraryGetKernel(&h->k_prep, h->lib, "bvp_prep"));
     CU(cudaLibraryGetKernel(&h->k_dense, h->lib, "bvp_dense"));
+    CU(cudaLibraryGetKernel(&h->k_learn, h->lib, "bvp_learn_costs"));
     return BVP_OK;
 }
 
@@ -456,6 +463,8 @@ static int fused_grid(bvp_handle* h, int n) {
 // Launches prep + conversion + fused solve on the handle's stream.
 static bvp_status prepare_host_outputs(bvp_handle* h, int n, long long pts_guess, BvpArgs& a);
 
+static constexpr int kLearnMin = 256;   // smallest batch the work-order autotuner learns from
+
 static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode, const double* d_params,
                                const int* d_n_init, const double* d_tspans, const double* d_y0,
                                const long long* d_y0_off, const float* d_grid = nullptr, int n_grid = 0,
@@ -464,6 +473,17 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
     fill_args(h, a, n, tot, y0_mode, d_params, d_n_init, d_tspans, d_y0, d_y0_off);
     a.y0_grid = d_grid;
     a.n_grid = n_grid;
+    const bool learn = h->learn_left > 0 && n >= kLearnMin;
+    if (learn) {
+        if (!h->d_cost_tab.p) {
+            if (!ensure_dev(h->d_cost_tab, (BVP_COST_BUCKETS + 1) * sizeof(float)))
+                return fail(h, BVP_ERR_NOMEM, "cost table allocation failed");
+            CU(cudaMemsetAsync(h->d_cost_tab.p, 0, (BVP_COST_BUCKETS + 1) * sizeof(float), h->stream));
+        }
+        if (!ensure_dev(h->d_inst_cost, size_t(n) * sizeof(float)))
+            return fail(h, BVP_ERR_NOMEM, "cost record allocation failed");
+        a.inst_cost = static_cast<float*>(h->d_inst_cost.p);
+    }
     if (host_pts > 0) {
         bvp_status s = prepare_host_outputs(h, n, host_pts, a);
         if (s != BVP_OK) return s;
@@ -484,7 +504,8 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
         bvp_i64* off = static_cast<bvp_i64*>(h->d_node_off.p);
         int* ord = static_cast<int*>(h->d_order.p);
         int* ctr = static_cast<int*>(h->d_counter.p);
-        void* args[] = {&nn, &ni, &ms, &cap, &off, &ord, &ctr};
+        const float* tab = h->have_tab ? static_cast<const float*>(h->d_cost_tab.p) : nullptr;
+        void* args[] = {&nn, &ni, &ms, &cap, &off, &ord, &ctr, &tab};
         CU(cudaLaunchKernel((const void*)h->k_prep, dim3(1), dim3(1024), args, 0, h->stream));
     }
     CU(cudaEventRecord(h->ev[1], h->stream));
@@ -493,6 +514,16 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
         CU(cudaLaunchKernel((const void*)h->k_fused, dim3(fused_grid(h, n)), dim3(128), args, 0, h->stream));
     }
     CU(cudaEventRecord(h->ev[2], h->stream));
+    if (learn) {
+        int nn = n, blend = h->have_tab ? 1 : 0;
+        const int* ni = d_n_init;
+        const float* cost = a.inst_cost;
+        float* tab = static_cast<float*>(h->d_cost_tab.p);
+        void* args[] = {&nn, &ni, &cost, &tab, &blend};
+        CU(cudaLaunchKernel((const void*)h->k_learn, dim3(1), dim3(1024), args, 0, h->stream));
+        h->have_tab = true;
+        --h->learn_left;
+    }
     h->last_n = n;
     h->last_tot = tot;
     h->stages_ok = h->opt.want_stages != 0;
@@ -1516,6 +1547,21 @@ bvp_status bvp_dense_output(bvp_handle* h, int32_t nq, const double* tq, int32_t
 bvp_status bvp_get_tuning(bvp_handle* h, int32_t* threads) {
     if (!h || !threads) return BVP_ERR_INVALID;
     threads[0] = (h->large && h->l_tuned) ? h->l_threads : 0;
+    return BVP_OK;
+}
+
+bvp_status bvp_get_work_order(bvp_handle* h, int32_t* learned, float* costs, int32_t n_costs) {
+    if (!h || !learned) return BVP_ERR_INVALID;
+    *learned = h->have_tab ? 1 : 0;
+    if (costs && n_costs > 0) {
+        const int k = std::min(n_costs, BVP_COST_BUCKETS + 1);
+        if (!h->have_tab) {
+            std::fill(costs, costs + k, 0.0f);
+        } else {
+            CU(cudaMemcpyAsync(costs, h->d_cost_tab.p, size_t(k) * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+            CU(cudaStreamSynchronize(h->stream));
+        }
+    }
     return BVP_OK;
 }
 

@@ -233,6 +233,16 @@ class BatchSolver:
         self._check(self.lib.bvp_get_tuning(self.h, i32(t)), "bvp_get_tuning")
         return {"linsolve_threads": int(t[0])}
 
+    def work_order(self):
+        """(learned, costs): whether the fused solve's work order comes from the handle's learned
+        cost table, and the table (mean solve time per initial-size bucket of 8 intervals, the
+        maximum last)."""
+        learned = np.zeros(1, np.int32)
+        costs = np.zeros(513, np.float32)
+        self._check(self.lib.bvp_get_work_order(self.h, i32(learned), costs.ctypes.data_as(C.POINTER(C.c_float)),
+                                                len(costs)), "bvp_get_work_order")
+        return bool(learned[0]), costs
+
     def stream_ptr(self) -> int:
         return int(self.lib.bvp_stream(self.h) or 0)
 

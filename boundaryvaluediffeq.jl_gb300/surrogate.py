@@ -131,7 +131,7 @@ def resample_host(grid, n_intervals):
     out = []
     G = grid.shape[1]
     for g, n in zip(grid, n_intervals):
-        s = np.arange(n + 1) / n * (G - 1)
+        s = np.arange(n + 1) * (1.0 / n) * (G - 1)    # j (1/n) (G-1), rounded as the device rounds it
         i0 = np.clip(np.floor(s).astype(int), 0, G - 2)
         f = (s - i0)[:, None]
         out.append((1 - f) * g[i0] + f * g[i0 + 1])

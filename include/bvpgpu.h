@@ -241,6 +241,16 @@ bvp_status bvp_last_timing(bvp_handle* h, double* ms2);
  * Newton step of a state dimension above 8 has run). */
 bvp_status bvp_get_tuning(bvp_handle* h, int32_t* threads);
 
+/* The fused solve's work order (no reference counterpart: the reference solves one problem at
+ * a time). One warp carries one instance, so a batch ends when its slowest instances end; the
+ * handle's first three solves of at least 256 instances record every instance's solve time
+ * and fold it into a table of mean times per initial-size bucket (initial intervals / 8, 512
+ * buckets), and later solves start the instances the table predicts to be longest first
+ * (before any table: coarsest initial mesh first). The order changes no result. *learned: 1
+ * once the table exists; costs (if not NULL): the first n_costs of the 512 bucket costs and,
+ * at index 512, their maximum (relative units). */
+bvp_status bvp_get_work_order(bvp_handle* h, int32_t* learned, float* costs, int32_t n_costs);
+
 /* The handle's CUDA stream (cudaStream_t as void*). */
 void* bvp_stream(bvp_handle* h);
 

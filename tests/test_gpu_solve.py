@@ -339,3 +339,26 @@ def test_mirk6i_pendulum_parity_fp64(pkg, problems):
             K, KI = res.stages(i)
             want = o.interpolate(6, m, y, K, KI, tq[i], deriv=deriv, mirk6i=1)
             assert np.abs(d[i] - want).max() <= 1e-10 * max(1.0, np.abs(want).max())
+
+
+def test_learned_work_order_changes_no_result(pkg, problems):
+    # the work-order autotuner: after the handle's first solves of >= 256 instances the fused
+    # solve starts the instances its cost table predicts to be longest first; every instance's
+    # result is the same bit for bit as under the initial (coarsest-first) order
+    p = problems.PENDULUM
+    params, nint, tsp, y0 = problems.pendulum_family(1024, seed=97)
+    fresh = pkg.BatchSolver(p, order=4)
+    assert fresh.work_order()[0] is False
+    ref = fresh.solve(params, nint, tsp, y0)
+    tuned = pkg.BatchSolver(p, order=4)
+    for _ in range(3):
+        tuned.solve(params, nint, tsp, y0)
+    learned, costs = tuned.work_order()
+    assert learned and costs[512] > 0 and (costs[:512] > 0).all()
+    # coarse initial meshes (several mesh rounds) cost more than the single-round middle sizes
+    assert costs[32 // 8] > costs[96 // 8]
+    res = tuned.solve(params, nint, tsp, y0)
+    for f in ("retcode", "n_nodes", "newton_iters", "rounds"):
+        assert np.array_equal(getattr(res, f), getattr(ref, f))
+    for i in range(len(nint)):
+        assert np.array_equal(res.solution(i)[1], ref.solution(i)[1])
