@@ -180,6 +180,42 @@ def cpu_baseline(params, nint, tsp, y0, seconds=2.0):
             "sample": f"{n_done // len(nint)} full passes over the {len(nint)}-instance batch ({dt:.1f} s wall)"}
 
 
+def parity_block(pkg, sv, sur, params, nint, tsp, y0, n=256):
+    """The error of the timed form's results against FP64 CPU references, on the first n
+    instances of the batch, computed after timing (the oracle checks; it is never timed here):
+    the GPU solve as the step runs it (surrogate guess, plain fallback) against the oracle
+    solved from the same guesses (retcodes, final meshes, node differences where the meshes
+    match), both against a tight solution (the oracle at abstol 1e-10, MIRK6), and the
+    reference's acceptance tests (||F||_inf, defect) of every GPU result in FP64."""
+    from oracle.oracle import Oracle
+    p = pkg.problems.PENDULUM
+    params, nint, tsp, y0 = params[:n], nint[:n], tsp[:n], y0[:n]
+    res, nfb = sv.solve_warm(sur.net, params.astype(np.float32), GRID, params, nint, tsp, y0)
+    o = Oracle(p.source, p.M, p.n_params, bc_t=p.bc_t)
+    threads = os.cpu_count() or 1
+    ref = o.solve_batch(params, nint, tsp, sur.guess(params, nint), y0_mode=1, nthreads=threads)
+    tight = o.solve_batch(params, nint, tsp, y0, order=6, abstol=1e-10, want_stages=True, nthreads=threads)
+    same, diffs, eg, er, resid, defect = 0, [], [], [], [], []
+    for i in range(n):
+        m, y = res.solution(i)
+        resid.append(o.residual(params[i], m, y)[2])
+        defect.append(o.defect(params[i], m, y)[1])
+        Nt, N = int(tight["n_nodes"][i]), int(ref["n_nodes"][i])
+        mt, mr, yr = tight["mesh"][i, :Nt], ref["mesh"][i, :N], ref["y"][i, :N]
+        eg.append(np.abs(y - o.interpolate(6, mt, tight["y"][i], tight["K"][i], tight["KI"][i], m)).max())
+        er.append(np.abs(yr - o.interpolate(6, mt, tight["y"][i], tight["K"][i], tight["KI"][i], mr)).max())
+        if len(m) == N and np.abs(m - mr).max() <= 1e-9:
+            same += 1
+            diffs.append(np.abs(y - yr).max())
+    q = lambda v: {"p50": float(np.median(v)), "max": float(np.max(v))}
+    return {"sample": f"first {n} instances of the timed batch, after timing", "fallback": int(nfb),
+            "retcode_match": float((res.retcode == ref["retcode"]).mean()), "same_mesh": same / n,
+            "node_diff_on_same_mesh": q(diffs) if diffs else None,
+            "within_1e-6_on_same_mesh": float((np.array(diffs) <= 1e-6).mean()) if diffs else None,
+            "error_vs_tight_solution": {"gpu": q(eg), "oracle": q(er)},
+            "acceptance_fp64": {"max_resid": float(max(resid)), "max_defect": float(max(defect)), "abstol": 1e-6}}
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -538,6 +574,7 @@ def main():
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(params, nint, tsp, y0)
+        line["parity"] = parity_block(pkg, sv, sur, params, nint, tsp, y0)
     print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist
