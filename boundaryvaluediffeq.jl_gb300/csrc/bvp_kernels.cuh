@@ -140,6 +140,7 @@ struct Inst {
     double* scr;
     int* iscr;
     JT* dns;               // per-warp shared memory for the separator system
+    JT* trec;              // per-warp shared memory for the shuffle tree's elimination records (or null)
 };
 
 BVP_DEV double* mesh_of(const Args& a, const Inst& I, int b) { return a.mesh + b * a.tot + I.nb; }
@@ -912,6 +913,12 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
 #define BVP_TREE_UNROLL 1
 #endif
 constexpr int TREE_UNROLL = BVP_TREE_UNROLL;  // shuffle-tree levels unrolled (1: one copy of each step)
+// The shuffle tree's elimination records stay in shared memory when they fit: at level s the
+// combining lanes of a group are 2^(s+1) apart, so lane >> (s+1) numbers them without
+// collisions across groups, and the five levels need 16 + 8 + 4 + 2 + 1 = 31 slots. The lane
+// that writes a record at level s is the one that reads it back in the unwind.
+constexpr int TREE_SLOTS = 31;
+BVP_DEV int tree_slot(int s, int lane) { return (32 - (32 >> s)) + (lane >> (s + 1)); }
 
 // S_c = ∂r_c/∂y_c and R_c = ∂r_c/∂y_{c+1} of interval c by forward mode (2M tangents), the same
 // blocks jacobian_blocks writes. With NODE_SHARE, node holds f at y_c with its tangents in the
@@ -1008,7 +1015,8 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
         const int bp = __shfl_down_sync(FULL, bnode, step);
         xs[s] = bnode;
         if (active && (t % (2 * step)) == 0 && t + step < L) {
-            bad |= !eliminate_pair(A, B, g, Ap, Bp, gp, a.rec + (I.nb + bnode) * RECW, A, B, g);
+            JT* rdst = I.trec ? I.trec + tree_slot(s, lane) * RECW : a.rec + (I.nb + bnode) * RECW;
+            bad |= !eliminate_pair(A, B, g, Ap, Bp, gp, rdst, A, B, g);
             bnode = bp;
         }
     }
@@ -1056,13 +1064,23 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     dense_ok = __shfl_sync(FULL, dense_ok, 0);
     __syncwarp();
     if (warp_any(bad) || !dense_ok) return false;
-    // 4a. unwind the tree: every lane gets δ at its block ends
+    // 4a. unwind the tree: every lane gets δ at its block ends (the group roots read them from
+    //     the separator solve's shared-memory rows, else from δ)
     JT da[M], db[M];
     if (active && t == 0) {
+        if constexpr (SMEM_DENSE) {
+            const int n = nk * M;
 #pragma unroll
-        for (int m = 0; m < M; ++m) {
-            da[m] = a.delta[(I.nb + na) * M + m];
-            db[m] = a.delta[(I.nb + nbk) * M + m];
+            for (int m = 0; m < M; ++m) {
+                da[m] = I.dns[(seg * M + m) * DLD + n];
+                db[m] = I.dns[((seg + 1) * M + m) * DLD + n];
+            }
+        } else {
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                da[m] = a.delta[(I.nb + na) * M + m];
+                db[m] = a.delta[(I.nb + nbk) * M + m];
+            }
         }
     }
 #pragma unroll TREE_UNROLL
@@ -1071,7 +1089,7 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
         const bool comb = active && (t % (2 * step)) == 0 && t + step < L;
         JT dx[M];
         if (comb) {
-            back_solve(a.rec + (I.nb + xs[s]) * RECW, da, db, dx);
+            back_solve(I.trec ? I.trec + tree_slot(s, lane) * RECW : a.rec + (I.nb + xs[s]) * RECW, da, db, dx);
             JT* dg = a.delta + (I.nb + xs[s]) * M;
 #pragma unroll
             for (int m = 0; m < M; ++m) dg[m] = dx[m];
@@ -1152,6 +1170,9 @@ BVP_DEV void refresh_yj(const Args& a, const Inst& I) {
     __syncwarp();
 }
 
+#ifndef BVP_FP32_SWITCH
+#define BVP_FP32_SWITCH 100.0   // the FP32 phase ends when the FP32 residual falls to this times abstol
+#endif
 // Mixed-precision Newton: the iterations run on the FP32 residual (stages in FP32, node
 // differences in FP64, roundoff about h|K| eps32) until it falls to 100 abstol or stops
 // improving near that level; the last steps then take the FP64 residual as right-hand side,
@@ -1167,7 +1188,7 @@ BVP_DEV bool newton_attempt(const Args& a, Inst& I, bool linesearch, int& iters,
     iters = 0;
     refresh_yj(a, I);
     bool f32 = F32_PHASE_OK && a.fp32_phase && !linesearch;
-    const double switch_tol = 100.0 * a.abstol;
+    const double switch_tol = BVP_FP32_SWITCH * a.abstol;
     // One residual evaluation per pass of this loop (a single inlined copy of each residual
     // kernel); `why` says what the evaluation is for.
     enum { R_START, R_SWITCH, R_STEP, R_TRIAL };
@@ -1727,6 +1748,7 @@ BVP_DEV Inst make_inst(const Args& a, int q) {
     I.scr = a.scr + (long long)q * SCRW;
     I.iscr = a.iscr + (long long)q * ISCRW;
     I.dns = nullptr;
+    I.trec = nullptr;
     I.N = 0;
     I.cur = 0;
     return I;
@@ -1745,6 +1767,8 @@ constexpr bool SCR_SMEM = WARPS_PER_BLOCK * (SCRW * 8 + ISCRW * 4) <= 40 * 1024;
 constexpr int SM_SCRW = SCR_SMEM ? SCRW : 1;
 constexpr int SM_ISCRW = SCR_SMEM ? ISCRW : 1;
 constexpr int SM_DNS = SMEM_DENSE ? NDENSE * DLD : 1;
+constexpr bool TREC_SMEM = WARPS_PER_BLOCK * TREE_SLOTS * RECW * int(sizeof(JT)) <= 16 * 1024;
+constexpr int SM_TREC = TREC_SMEM ? TREE_SLOTS * RECW : 1;
 }  // namespace bvp
 
 // Persistent fused solve: each warp repeatedly takes the next instance from the work
@@ -1753,6 +1777,7 @@ extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::
     __shared__ double s_scr[bvp::WARPS_PER_BLOCK][bvp::SM_SCRW];
     __shared__ int s_iscr[bvp::WARPS_PER_BLOCK][bvp::SM_ISCRW];
     __shared__ bvp::JT s_dns[bvp::WARPS_PER_BLOCK][bvp::SM_DNS];
+    __shared__ bvp::JT s_trec[bvp::WARPS_PER_BLOCK][bvp::SM_TREC];
     const int lane = bvp::lane_id();
     const int w = threadIdx.x >> 5;
     while (true) {
@@ -1763,6 +1788,7 @@ extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::
         bvp::Inst I = bvp::make_inst(a, a.order[k]);
         if (bvp::SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
         I.dns = s_dns[w];
+        if (bvp::TREC_SMEM) I.trec = s_trec[w];
         const long long c0 = a.inst_cost ? clock64() : 0;
         bvp::solve_instance(a, I);
         if (a.inst_cost && lane == 0) a.inst_cost[I.q] = float(clock64() - c0) * (1.0f / 2000.0f);
@@ -1777,6 +1803,7 @@ extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, i
     __shared__ double s_scr[bvp::WARPS_PER_BLOCK][bvp::SM_SCRW];
     __shared__ int s_iscr[bvp::WARPS_PER_BLOCK][bvp::SM_ISCRW];
     __shared__ bvp::JT s_dns[bvp::WARPS_PER_BLOCK][bvp::SM_DNS];
+    __shared__ bvp::JT s_trec[bvp::WARPS_PER_BLOCK][bvp::SM_TREC];
     const int lane = bvp::lane_id();
     const int w = threadIdx.x >> 5;
     while (true) {
@@ -1785,6 +1812,7 @@ extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, i
         k = __shfl_sync(bvp::FULL, k, 0);
         if (k >= a.n_inst) break;
         bvp::Inst I = bvp::make_inst(a, a.order[k]);
+        if (bvp::TREC_SMEM) I.trec = s_trec[w];
         double* g_scr = I.scr;
         int* g_iscr = I.iscr;
         if (bvp::SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
