@@ -479,9 +479,9 @@ def main():
     from bvdiffeq_gb300._lib import f64, i32, Results
     n = n_inst
     out = {k: np.zeros(n, np.int32) for k in ("retcode", "n_nodes", "newton_iters", "rounds")}
-    outd = {k: np.zeros(n) for k in ("defect", "resid")}
+    outd = {k: np.zeros(n) for k in ("defect", "resid", "global_err")}
     cr = Results(i32(out["retcode"]), i32(out["n_nodes"]), i32(out["newton_iters"]), i32(out["rounds"]),
-                 f64(outd["defect"]), f64(outd["resid"]))
+                 f64(outd["defect"]), f64(outd["resid"]), f64(outd["global_err"]))
     pa, na, ta, ya = (np.ascontiguousarray(params), np.ascontiguousarray(nint, dtype=np.int32),
                       np.ascontiguousarray(tsp), np.ascontiguousarray(y0))
     fa = np.ascontiguousarray(feats)

@@ -10,3 +10,5 @@ from .solver import BatchSolver, BatchResult, BVPError, RET_SUCCESS, RET_FAILURE
 from .surrogate import MLP, Surrogate, resample_host  # noqa: F401
 from . import sciml  # noqa: F401
 from .sciml import solve, EnsembleProblem, MIRK2, MIRK3, MIRK4, MIRK5, MIRK6, MIRK6I  # noqa: F401
+from .sciml import (DefectControl, GlobalErrorControl, SequentialErrorControl, HybridErrorControl,  # noqa: F401
+                    HOErrorControl, REErrorControl)

@@ -86,9 +86,10 @@ def _nvrtc():
     return None
 
 
-def nvrtc_check(problem, order: int, jac_bits: int = 32, mirk6i: int = 0) -> None:
+def nvrtc_check(problem, order: int, jac_bits: int = 32, mirk6i: int = 0, global_ctl: int = 0) -> None:
     """Compile the problem's kernels with NVRTC exactly as bvp_create does (same source
-    assembly and options, no GPU needed); raises with the NVRTC log on failure."""
+    assembly and options, no GPU needed; global_ctl: the build with the error controllers other
+    than DefectControl); raises with the NVRTC log on failure."""
     lib = _nvrtc()
     if lib is None:
         return
@@ -100,7 +101,7 @@ def nvrtc_check(problem, order: int, jac_bits: int = 32, mirk6i: int = 0) -> Non
             f"-DBVP_ORDER={order}", f"-DBVP_TWOPOINT={int(problem.twopoint)}", f"-DBVP_NBC={nbc}",
             f"-DBVP_LA={problem.La if problem.twopoint else 0}",
             "-DBVP_JT=" + ("double" if jac_bits == 64 else "float"), f"-DBVP_MIRK6I={int(bool(mirk6i))}",
-            f"-DBVP_SINGULAR={int('BVP_SING' in problem.source)}"]
+            f"-DBVP_SINGULAR={int('BVP_SING' in problem.source)}"] + (["-DBVP_GLOBAL_CTL=1"] if global_ctl else [])
     names = [fn.encode() for fn in EMBED]
     bodies = [open(os.path.join(CSRC, fn), "rb").read() for fn in EMBED]
     prog = C.c_void_p()
@@ -195,13 +196,21 @@ class Options(C.Structure):
                 ("bc_jac_exact", C.c_int32), ("linesearch_fallback", C.c_int32),
                 ("stall_steps", C.c_int32), ("jac_precision", C.c_int32), ("want_stages", C.c_int32),
                 ("fp32_phase", C.c_int32), ("abstol", C.c_double), ("defect_threshold", C.c_double),
-                ("divergence_factor", C.c_double), ("mirk6i", C.c_int32)]
+                ("divergence_factor", C.c_double), ("mirk6i", C.c_int32),
+                ("controller", C.c_int32), ("global_method", C.c_int32),
+                ("hybrid_de", C.c_double), ("hybrid_ge", C.c_double)]
+
+
+# bvp_controller and bvp_global_method
+CONTROLLERS = {"defect": 0, "global": 1, "sequential": 2, "hybrid": 3}
+GLOBAL_METHODS = {"HO": 0, "RE": 1}
 
 
 class Results(C.Structure):
     _fields_ = [("retcode", C.POINTER(C.c_int32)), ("n_nodes", C.POINTER(C.c_int32)),
                 ("newton_iters", C.POINTER(C.c_int32)), ("rounds", C.POINTER(C.c_int32)),
-                ("defect", C.POINTER(C.c_double)), ("resid", C.POINTER(C.c_double))]
+                ("defect", C.POINTER(C.c_double)), ("resid", C.POINTER(C.c_double)),
+                ("global_err", C.POINTER(C.c_double))]
 
 
 EXPORTS = ("bvp_default_options", "bvp_create", "bvp_solve_batch", "bvp_solve_batch_device",

@@ -71,6 +71,15 @@ constexpr int NDENSE = KMAX * M;
 
 enum : int { RET_SUCCESS = 0, RET_FAILURE = 1, RET_MAXITERS = 2 };
 
+// error controllers (Core/src/calc_errors.jl:54-139); the paths other than DefectControl are
+// compiled in only with BVP_GLOBAL_CTL, so the defect-controlled kernel stays as it is
+#ifndef BVP_GLOBAL_CTL
+#define BVP_GLOBAL_CTL 0
+#endif
+constexpr bool GLOBAL_CTL = BVP_GLOBAL_CTL != 0;
+enum : int { CTL_DEFECT = 0, CTL_GLOBAL = 1, CTL_SEQUENTIAL = 2, CTL_HYBRID = 3 };
+enum : int { GLOBAL_HO = 0, GLOBAL_RE = 1 };
+
 // ---- launch arguments (shared with the host runtime) ------------------------------------
 using InstState = BvpInstState;
 using Args = BvpArgs;
@@ -1372,13 +1381,13 @@ BVP_DEV void half_mesh(const Args& a, Inst& I, int src, int dst) {
 
 BVP_DEV long round_even(double x) { return (long)rint(x); }
 
-// x^(1/(p+1)), the selector's ŝ = (err/abstol)^(1/(p+1)) (adaptivity.jl:43): an FP32 seed
-// refined by two Newton steps on y^(p+1) = x in FP64 (the derivative's reciprocal taken in
-// FP32: the first step leaves ~1e-14, the second the FP64 roundoff of y^(p+1)), a dozen FP64
-// operations instead of a double-precision pow. Zero, extreme and non-finite arguments go
-// to pow.
-BVP_DEV double root_p1(double x) {
-    constexpr int P = ORD + 1;
+// x^(1/P), the selector's ŝ = (err/abstol)^(1/(p+1)) (adaptivity.jl:43; 1/p for the global
+// error, adaptivity.jl:96): an FP32 seed refined by two Newton steps on y^P = x in FP64 (the
+// derivative's reciprocal taken in FP32: the first step leaves ~1e-14, the second the FP64
+// roundoff of y^P), a dozen FP64 operations instead of a double-precision pow. Zero, extreme
+// and non-finite arguments go to pow.
+template <int P>
+BVP_DEV double root_n(double x) {
     if (!(x >= 1e-30 && x <= 1e30)) return pow(x, 1.0 / P);
     double y = double(powf(float(x), 1.0f / float(P)));
 #pragma unroll
@@ -1392,6 +1401,12 @@ BVP_DEV double root_p1(double x) {
     }
     return y;
 }
+BVP_DEV double root_p1(double x) { return root_n<ORD + 1>(x); }
+
+// which errors make the selector's ŝ: the defect's (DefectControl, and SequentialErrorControl
+// before its defect passes), the global estimate's to 1/(p+1) (SequentialErrorControl after),
+// to 1/p (GlobalErrorControl), or the sum of both terms (HybridErrorControl, 207-209)
+enum : int { SEL_DEFECT = 0, SEL_GLOBAL_P1 = 1, SEL_GLOBAL_P = 2, SEL_HYBRID = 3 };
 
 // Returns 1 on success (new mesh in buffer cur^1, newN set, iold hints written), 0 on Failure.
 //
@@ -1404,15 +1419,26 @@ BVP_DEV double root_p1(double x) {
 // running maximum across the warp, so every point 1..Nsub-1 is placed exactly once even
 // where the block sums round differently from the running sums. The positions agree with
 // the sequential walk to rounding (same formula, different association).
-BVP_DEV int mesh_selector(const Args& a, Inst& I, int& newN) {
+// The selectors of the global-error controllers (adaptivity.jl:77-243) differ from the
+// defect's only in ŝ (sel) and in ρ = 2.
+BVP_DEV int mesh_selector(const Args& a, Inst& I, int& newN, int sel = SEL_DEFECT, double rho = 1.0) {
     const int lane = lane_id();
     const int n = I.N - 1;
     const double* h0 = h_of(a, I, I.cur);
     double* e = a.err + I.nb;
+    const double* g = a.gerr + I.nb;
     const double inv_tol = 1.0 / a.abstol;
     double r1 = -dinf(), r2p = 0.0;
     for (int i = lane; i < n; i += 32) {
-        const double sh = root_p1(e[i] * inv_tol);
+        double sh;
+        if constexpr (GLOBAL_CTL) {
+            if (sel == SEL_DEFECT) sh = root_p1(e[i] * inv_tol);
+            else if (sel == SEL_GLOBAL_P1) sh = root_p1(g[i] * inv_tol);
+            else if (sel == SEL_GLOBAL_P) sh = root_n<ORD>(g[i] * inv_tol);
+            else sh = root_p1(e[i] * inv_tol) + root_p1(g[i] * inv_tol);
+        } else {
+            sh = root_p1(e[i] * inv_tol);
+        }
         e[i] = sh;
         r1 = fmax(r1, sh);
         r2p += sh;
@@ -1424,7 +1450,7 @@ BVP_DEV int mesh_selector(const Args& a, Inst& I, int& newN) {
     const double n_ = 0.1 * n;
     if (fabs(double(n_pred - n)) < n_) n_pred = round_even(n + n_);
     const int dst = I.cur ^ 1;
-    if (r1 <= 1.0 * r3) {
+    if (r1 <= rho * r3) {
         if (2L * n > a.max_sub || 2 * n + 1 > I.cap) return 0;
         half_mesh(a, I, I.cur, dst);
         newN = 2 * n + 1;
@@ -1647,30 +1673,190 @@ BVP_DEV void finalize_stages(const Args& a, Inst& I) {
     __syncwarp();
 }
 
+// ---- global error estimates (adaptivity.jl:463-567) ------------------------------------------
+// The second solve of a global estimate, on buffer cur^1 from the current solution:
+// REErrorControl on the halved mesh (halve_sol, adaptivity.jl:310-332: the old nodes at the
+// even 0-based positions, each midpoint node the mean of its neighbours), HOErrorControl on
+// the same mesh in the module compiled for MIRK(p+2) (phase 2). The new cache takes
+// mesh_dt = diff(mesh) (mirk.jl:75-76); the Newton outcome is not consulted (adaptivity.jl:
+// 530-531, 547-549) and its iterations are not the instance's. Returns false when the halved
+// mesh does not fit the instance's capacity.
+BVP_DEV bool second_solve(const Args& a, Inst& I, bool halve) {
+    const int lane = lane_id();
+    const int n = I.N - 1;
+    const int Nn = halve ? 2 * n + 1 : I.N;
+    if (Nn > I.cap) return false;
+    const double* m0 = mesh_of(a, I, I.cur);
+    const double* y0 = y_of(a, I, I.cur);
+    double* m1 = mesh_of(a, I, I.cur ^ 1);
+    double* h1 = h_of(a, I, I.cur ^ 1);
+    double* y1 = y_of(a, I, I.cur ^ 1);
+    const int st = halve ? 2 : 1;
+    for (int i = lane; i <= n; i += 32) {
+        m1[st * i] = m0[i];
+#pragma unroll
+        for (int m = 0; m < M; ++m) y1[st * i * M + m] = y0[i * M + m];
+        if (halve && i < n) {
+            m1[2 * i + 1] = (m0[i + 1] + m0[i]) / 2.0;
+#pragma unroll
+            for (int m = 0; m < M; ++m) y1[(2 * i + 1) * M + m] = (y0[(i + 1) * M + m] + y0[i * M + m]) / 2.0;
+        }
+    }
+    __syncwarp();
+    for (int q = lane; q < Nn - 1; q += 32) h1[q] = m1[q + 1] - m1[q];
+    __syncwarp();
+    const int c0 = I.cur, N0 = I.N;
+    I.cur ^= 1;
+    I.N = Nn;
+    mesh_setup(a, I);
+    InstState t;
+    t.N = Nn; t.cur = I.cur; t.retcode = RET_FAILURE; t.newton_iters = 0; t.rounds = 0; t.flags = 0;
+    t.defect = 0.0; t.resid = 0.0; t.global_err = 0.0;
+    newton(a, I, t);
+    I.cur = c0;
+    I.N = N0;
+    return true;
+}
+
+// The estimate from the second solve's nodes (buffer cur^1, every st-th of them at the current
+// nodes): err_j = max_m |(y_high - y) / (1 + |y|)| at each current node, each interval keeps
+// the larger of its end nodes' errors (GE_subinterval!, adaptivity.jl:557-567), the norm is
+// their maximum (NaN when any is), times 2^p / (2^p - 1) for Richardson extrapolation
+// (adaptivity.jl:534). The current solution's stages are then evaluated again for the
+// transfer: the second solve overwrote K, and GlobalErrorControl has no defect pass to
+// leave the extra stages.
+BVP_DEV double global_finish(const Args& a, Inst& I, int st) {
+    const int lane = lane_id();
+    const double* yl = y_of(a, I, I.cur);
+    const double* yh = y_of(a, I, I.cur ^ 1);
+    double* g = a.gerr + I.nb;
+    auto node_err = [&](int j) {
+        double e = 0.0;
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            const double lo = yl[j * M + m];
+            const double v = fabs((yh[st * j * M + m] - lo) / (1.0 + fabs(lo)));
+            e = (isnan(v) || v > e) ? v : e;
+        }
+        return e;
+    };
+    double gn = 0.0;
+    bool bad = false;
+    for (int i = lane; i < I.N - 1; i += 32) {
+        const double e0 = node_err(i), e1 = node_err(i + 1);
+        const double gi = e0 >= e1 ? e0 : e1;
+        g[i] = gi;
+        bad |= isnan(gi);
+        gn = fmax(gn, gi);
+    }
+    __syncwarp();
+    gn = warp_max(gn);
+    if (warp_any(bad)) gn = __longlong_as_double(0x7ff8000000000000LL);
+    if (a.global_method == GLOBAL_RE) {
+        const double p2 = double(1 << ORD);
+        gn = gn * p2 / (p2 - 1.0);
+    }
+    finalize_stages(a, I);
+    return gn;
+}
+
+// An instance stops for its MIRK(p+2) solve: its state goes to st[q], its id to the pause list.
+BVP_DEV void pause_instance(const Args& a, const Inst& I, InstState& s) {
+    s.N = I.N;
+    s.cur = I.cur;
+    if (lane_id() == 0) {
+        a.st[I.q] = s;
+        a.pause_list[atomicAdd(a.pause_count, 1)] = I.q;
+    }
+    __syncwarp();
+}
+
+// Phase 2 (the module of order p+2): the second solve of the HOErrorControl estimate.
+BVP_DEV void polish_instance(const Args& a, Inst& I) {
+    const InstState s = a.st[I.q];
+    I.N = s.N;
+    I.cur = s.cur;
+    second_solve(a, I, false);
+}
+
 BVP_DEV void solve_instance(const Args& a, Inst& I) {
     InstState s;
-    s.retcode = RET_FAILURE; s.newton_iters = 0; s.rounds = 0; s.flags = 0;
-    s.defect = __longlong_as_double(0x7ff8000000000000LL);
-    s.resid = s.defect;
-    init_instance(a, I);
+    // phase 1: the instance stopped after its Newton solve (and defect) of this round for the
+    // MIRK(p+2) solve, which left its nodes in buffer cur^1
+    bool resumed = GLOBAL_CTL && a.phase == 1;
+    if (resumed) {
+        s = a.st[I.q];
+        I.N = s.N;
+        I.cur = s.cur;
+    } else {
+        s.retcode = RET_FAILURE; s.newton_iters = 0; s.rounds = 0; s.flags = 0;
+        s.defect = __longlong_as_double(0x7ff8000000000000LL);
+        s.resid = s.defect;
+        s.global_err = s.defect;
+        init_instance(a, I);
+    }
     int info_ok = 1;
     bool maxed = false;
     while (true) {
-        ++s.rounds;
-        mesh_setup(a, I);
         double error_norm = 2 * a.abstol;
-        const bool nl_ok = newton(a, I, s);
-        if (!a.adaptive) { s.retcode = nl_ok ? RET_SUCCESS : RET_FAILURE; info_ok = nl_ok; break; }
-        bool ok = nl_ok;
-        if (ok) {
-            error_norm = defect(a, I);
-            s.defect = error_norm;
-            ok = !(error_norm > a.defect_threshold) && !isnan(error_norm);
+        bool ok = true;
+        int sel = SEL_DEFECT;
+        if (!resumed) {
+            ++s.rounds;
+            mesh_setup(a, I);
+            const bool nl_ok = newton(a, I, s);
+            if (!a.adaptive) { s.retcode = nl_ok ? RET_SUCCESS : RET_FAILURE; info_ok = nl_ok; break; }
+            ok = nl_ok;
+            if constexpr (!GLOBAL_CTL) {
+                if (ok) {
+                    error_norm = defect(a, I);
+                    s.defect = error_norm;
+                    ok = !(error_norm > a.defect_threshold) && !isnan(error_norm);
+                }
+            } else if (ok) {
+                // error_estimate! for the controller (adaptivity.jl:361-503)
+                const int ctl = a.controller;
+                if (ctl != CTL_GLOBAL) {
+                    error_norm = defect(a, I);
+                    s.defect = error_norm;
+                    if (ctl != CTL_HYBRID) ok = !(error_norm > a.defect_threshold);
+                }
+                // SequentialErrorControl takes the global estimate once the defect is within
+                // abstol (464-482); HybridErrorControl ignores the defect threshold (485-503)
+                const bool glob = ok && (ctl == CTL_GLOBAL || ctl == CTL_HYBRID ||
+                                         (ctl == CTL_SEQUENTIAL && error_norm <= a.abstol));
+                if (glob) {
+                    if (a.global_method == GLOBAL_HO) {
+                        pause_instance(a, I, s);
+                        return;
+                    }
+                    if (!second_solve(a, I, true)) {
+                        s.flags |= 2;
+                        error_norm = __longlong_as_double(0x7ff8000000000000LL);
+                    } else {
+                        const double gn = global_finish(a, I, 2);
+                        s.global_err = gn;
+                        error_norm = ctl == CTL_HYBRID ? a.hybrid_de * error_norm + a.hybrid_ge * gn : gn;
+                        sel = ctl == CTL_GLOBAL ? SEL_GLOBAL_P : (ctl == CTL_HYBRID ? SEL_HYBRID : SEL_GLOBAL_P1);
+                    }
+                }
+                // a norm that is not finite counts as a failed round, for every controller
+                if (!isfinite(error_norm)) ok = false;
+            }
+        } else {
+            resumed = false;
+            const int ctl = a.controller;
+            const double gn = global_finish(a, I, 1);
+            s.global_err = gn;
+            error_norm = ctl == CTL_HYBRID ? a.hybrid_de * s.defect + a.hybrid_ge * gn : gn;
+            sel = ctl == CTL_GLOBAL ? SEL_GLOBAL_P : (ctl == CTL_HYBRID ? SEL_HYBRID : SEL_GLOBAL_P1);
+            ok = isfinite(error_norm);
         }
         if (ok) {
             if (error_norm > a.abstol) {
                 int newN = 0;
-                info_ok = mesh_selector(a, I, newN);
+                const double rho = (GLOBAL_CTL && a.controller != CTL_DEFECT) ? 2.0 : 1.0;
+                info_ok = mesh_selector(a, I, newN, sel, rho);
                 if (info_ok) {
                     transfer(a, I, newN);
                     I.cur ^= 1;
@@ -1789,6 +1975,10 @@ extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::
         if (bvp::SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
         I.dns = s_dns[w];
         if (bvp::TREC_SMEM) I.trec = s_trec[w];
+        if (bvp::GLOBAL_CTL && a.phase == 2) {
+            bvp::polish_instance(a, I);
+            continue;
+        }
         const long long c0 = a.inst_cost ? clock64() : 0;
         bvp::solve_instance(a, I);
         if (a.inst_cost && lane == 0) a.inst_cost[I.q] = float(clock64() - c0) * (1.0f / 2000.0f);
@@ -1957,14 +2147,15 @@ extern "C" __global__ void bvp_convert_params(const double* p, bvp::JT* pj, long
         pj[k] = bvp::JT(p[k]);
 }
 
-// One block: node capacities (max(n, max_sub) + 1), their exclusive prefix sum (arena
-// offsets), and the work order: coarsest initial mesh first. A coarse initial mesh is the
+// One block: node capacities (cap_scale max(n, max_sub) + 1; cap_scale 2 leaves room for the
+// halved mesh of REErrorControl's second solve), their exclusive prefix sum (arena offsets),
+// and the work order: coarsest initial mesh first. A coarse initial mesh is the
 // likeliest to need further mesh rounds, each a new Newton solve, so those instances carry
 // the longest chains of dependent work and start first; the single-round fine meshes fill in
 // behind them and finish while the machine drains (measured on the 4096-instance pendulum
 // batch: about 11% less time than largest-first).
-extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_init, int max_sub, int* cap,
-                                                            long long* node_off, int* order, int* counter,
+extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_init, int max_sub, int cap_scale,
+                                                            int* cap, long long* node_off, int* order, int* counter,
                                                             const float* cost_tab) {
     constexpr int NB = 4096;
     __shared__ int hist[NB];
@@ -1979,7 +2170,7 @@ extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_
         long long c = 0;
         if (q < n) {
             const int ni = n_init[q];
-            c = (ni > max_sub ? ni : max_sub) + 1;
+            c = (long long)cap_scale * (ni > max_sub ? ni : max_sub) + 1;
             cap[q] = int(c);
         }
         long long v = c;

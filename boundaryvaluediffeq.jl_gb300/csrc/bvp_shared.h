@@ -24,6 +24,7 @@ struct BvpInstState {
     int flags;          // bit0: line-search fallback used, bit1: capacity guard hit
     double defect;
     double resid;
+    double global_err;  // last global error estimate (global, sequential and hybrid controllers)
 };
 
 struct BvpArgs {
@@ -79,6 +80,16 @@ struct BvpArgs {
     bvp_i64 host_cap;              // points the host arrays hold
     float* inst_cost;              // per instance: solve time (SM cycles / 2000), recorded while
                                    // the handle learns its work order (null: not recorded)
+    // error control (compiled in with BVP_GLOBAL_CTL): 0 DefectControl, 1 GlobalErrorControl,
+    // 2 SequentialErrorControl, 3 HybridErrorControl; the global estimate by 0 HOErrorControl
+    // (a MIRK(p+2) solve on the same mesh, in the module compiled for that order) or
+    // 1 REErrorControl (the same method on the halved mesh)
+    int controller, global_method;
+    double hybrid_de, hybrid_ge;
+    double* gerr;                  // [tot] per-interval global error estimates
+    int phase;                     // 0 new solves; 1 resume after the MIRK(p+2) solve; 2 that solve
+    int* pause_list;               // phase 0/1: instances stopping for the MIRK(p+2) solve, appended
+    int* pause_count;              //   at *pause_count
 };
 
 // Work-order cost table of the fused solve: the mean solve time of the instances whose initial

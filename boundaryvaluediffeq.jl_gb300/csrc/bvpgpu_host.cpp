@@ -61,6 +61,15 @@ struct bvp_handle_s {
     DevBuf d_inst_cost, d_cost_tab;
     int learn_left = 3;
     bool have_tab = false;
+    // error controllers other than DefectControl (fused path): the global estimates per interval,
+    // and for HOErrorControl the module compiled for MIRK(p+2), its stage array, the two lists
+    // of instances waiting for its solve and their counts (pinned for the host's loop)
+    bool glob = false, ho = false;
+    BvpLayout L_hi{};
+    cudaLibrary_t lib_hi = nullptr;
+    cudaKernel_t k_fused_hi = nullptr, k_probe_hi = nullptr;
+    DevBuf d_gerr, d_K_hi, d_pause;
+    HostBuf h_pause;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     // larger-state path (M > 8, bvp_large.cuh)
     bool large = false;
@@ -197,26 +206,34 @@ void bvp_default_options(bvp_options* o) {
     o->defect_threshold = 0.1;
     o->divergence_factor = 1e3;
     o->mirk6i = 0;
+    o->controller = BVP_CTL_DEFECT;
+    o->global_method = BVP_GLOBAL_HO;
+    o->hybrid_de = 1.0;
+    o->hybrid_ge = 1.0;
 }
 
 const char* bvp_last_error(bvp_handle* h) { return h ? h->err.c_str() : "null handle"; }
 
 void* bvp_stream(bvp_handle* h) { return h ? static_cast<void*>(h->stream) : nullptr; }
 
-static bvp_status compile_and_load(bvp_handle* h) {
+// NVRTC build of the problem's module for one MIRK order (the cubin is cached on disk under a
+// hash of the sources and options). global_ctl compiles in the error controllers other than
+// DefectControl.
+static bvp_status build_cubin(bvp_handle* h, int order, int mirk6i, int global_ctl, std::vector<char>& cubin) {
     const bvp_problem_desc& d = h->desc;
     const bvp_options& o = h->opt;
     std::vector<std::string> opts = {
         "--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true",
-        "-DBVP_M=" + std::to_string(d.M), "-DBVP_ORDER=" + std::to_string(o.order),
+        "-DBVP_M=" + std::to_string(d.M), "-DBVP_ORDER=" + std::to_string(order),
         "-DBVP_TWOPOINT=" + std::to_string(d.twopoint),
         "-DBVP_NBC=" + std::to_string(d.twopoint ? 2 : d.n_bc_pts),
         "-DBVP_LA=" + std::to_string(d.twopoint ? d.La : 0),
         std::string("-DBVP_JT=") + (o.jac_precision == 64 ? "double" : "float"),
-        std::string("-DBVP_MIRK6I=") + (o.mirk6i ? "1" : "0"),
+        std::string("-DBVP_MIRK6I=") + (mirk6i ? "1" : "0"),
         // a source with BVP_SING has a singular term S y / t (the problem's singular_term)
         std::string("-DBVP_SINGULAR=") + (h->source.find("BVP_SING") != std::string::npos ? "1" : "0"),
     };
+    if (global_ctl) opts.push_back("-DBVP_GLOBAL_CTL=1");
     const bool large = d.M > 8;
     const std::string src = std::string("#include \"bvp_prelude.cuh\"\n#line 1 \"problem_source\"\n") +
                             h->source + (large ? "\n#include \"bvp_large.cuh\"\n" : "\n#include \"bvp_kernels.cuh\"\n");
@@ -226,7 +243,6 @@ static bvp_status compile_and_load(bvp_handle* h) {
     char name[64];
     std::snprintf(name, sizeof(name), "/bvp_%016llx.cubin", (unsigned long long)key);
     const std::string path = cache_dir() + name;
-    std::vector<char> cubin;
     if (!read_file(path, cubin)) {
         nvrtcProgram prog;
         if (nvrtcCreateProgram(&prog, src.c_str(), "bvp_problem.cu", kEmbedCount, kEmbedSources,
@@ -250,6 +266,14 @@ static bvp_status compile_and_load(bvp_handle* h) {
         nvrtcDestroyProgram(&prog);
         write_file_atomic(path, cubin);
     }
+    return BVP_OK;
+}
+
+static bvp_status compile_and_load(bvp_handle* h) {
+    const bool large = h->desc.M > 8;
+    std::vector<char> cubin;
+    bvp_status bs = build_cubin(h, h->opt.order, h->opt.mirk6i, h->glob ? 1 : 0, cubin);
+    if (bs != BVP_OK) return bs;
     CU(cudaLibraryLoadData(&h->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
     if (large) {
         h->large = true;
@@ -275,6 +299,15 @@ static bvp_status compile_and_load(bvp_handle* h) {
     CU(cudaLibraryGetKernel(&h->k_prep, h->lib, "bvp_prep"));
     CU(cudaLibraryGetKernel(&h->k_dense, h->lib, "bvp_dense"));
     CU(cudaLibraryGetKernel(&h->k_learn, h->lib, "bvp_learn_costs"));
+    if (h->ho) {
+        // HOErrorControl's second solve: the same problem with MIRK(p+2) (adaptivity.jl:552-555)
+        std::vector<char> cubin_hi;
+        bs = build_cubin(h, h->opt.order + 2, 0, 1, cubin_hi);
+        if (bs != BVP_OK) return bs;
+        CU(cudaLibraryLoadData(&h->lib_hi, cubin_hi.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+        CU(cudaLibraryGetKernel(&h->k_fused_hi, h->lib_hi, "bvp_solve_fused"));
+        CU(cudaLibraryGetKernel(&h->k_probe_hi, h->lib_hi, "bvp_layout_probe"));
+    }
     return BVP_OK;
 }
 
@@ -302,8 +335,16 @@ bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bv
     else if (!(o.abstol > 0)) why = "abstol must be > 0";
     else if (o.max_subintervals < 1) why = "max_subintervals must be >= 1";
     else if (o.jac_precision != 32 && o.jac_precision != 64) why = "jac_precision must be 32 or 64";
+    else if (o.controller < BVP_CTL_DEFECT || o.controller > BVP_CTL_HYBRID) why = "controller must be 0..3";
+    else if (o.global_method != BVP_GLOBAL_HO && o.global_method != BVP_GLOBAL_RE) why = "global_method must be 0 or 1";
+    else if (o.controller != BVP_CTL_DEFECT && d.M > 8) why = "error controllers other than DefectControl take M <= 8";
+    else if (o.controller != BVP_CTL_DEFECT && o.global_method == BVP_GLOBAL_HO && (o.order + 2 > 6 || o.mirk6i))
+        why = "HOErrorControl solves with MIRK(order + 2): orders 2, 3 and 4";
     if (!why.empty()) { delete h; return BVP_ERR_INVALID; }
     h->L = bvp_make_layout(d.M, o.order, d.twopoint ? 2 : d.n_bc_pts, d.twopoint, o.mirk6i);
+    h->glob = o.adaptive && o.controller != BVP_CTL_DEFECT;
+    h->ho = h->glob && o.global_method == BVP_GLOBAL_HO;
+    if (h->ho) h->L_hi = bvp_make_layout(d.M, o.order + 2, d.twopoint ? 2 : d.n_bc_pts, d.twopoint, 0);
     h->js = o.jac_precision == 64 ? 8 : 4;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -366,6 +407,21 @@ bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bv
         got[4] != int(sizeof(BvpArgs)) || got[5] != int(sizeof(BvpInstState)) ||
         got[6] != L.NSXA || got[7] != L.S)
         return fail(h, BVP_ERR_STATE, "host/device layout mismatch");
+    if (h->ho) {
+        DevBuf probe2;
+        if (!ensure_dev(probe2, 16 * sizeof(int))) return fail(h, BVP_ERR_NOMEM, "probe alloc");
+        int* p2 = static_cast<int*>(probe2.p);
+        void* args2[] = {&p2};
+        CU(cudaLaunchKernel((const void*)h->k_probe_hi, dim3(1), dim3(1), args2, 0, h->stream));
+        int got2[16] = {0};
+        CU(cudaMemcpyAsync(got2, probe2.p, sizeof(got2), cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaStreamSynchronize(h->stream));
+        cudaFree(probe2.p);
+        const BvpLayout& H = h->L_hi;
+        if (got2[0] != H.SCRW || got2[1] != H.ISCRW || got2[4] != int(sizeof(BvpArgs)) ||
+            got2[5] != int(sizeof(BvpInstState)) || got2[7] != H.S)
+            return fail(h, BVP_ERR_STATE, "host/device layout mismatch (MIRK(p+2) module)");
+    }
     return BVP_OK;
 }
 
@@ -383,7 +439,8 @@ static bvp_status ensure_arena(bvp_handle* h, long long tot, int n, long long y0
               ensure_dev(h->d_delta, T * M * js) &&
               ensure_dev(h->d_yj, T * M * js) && ensure_dev(h->d_Fj, T * M * js) &&
               ensure_dev(h->d_tj, T * js) && ensure_dev(h->d_hj, T * js) &&
-              ensure_dev(h->d_scr, size_t(n) * L.SCRW * 8) && ensure_dev(h->d_iscr, size_t(n) * L.ISCRW * 4) &&
+              ensure_dev(h->d_scr, size_t(n) * std::max(L.SCRW, h->ho ? h->L_hi.SCRW : 0) * 8) &&
+              ensure_dev(h->d_iscr, size_t(n) * L.ISCRW * 4) &&
               ensure_dev(h->d_st, size_t(n) * sizeof(BvpInstState)) && ensure_dev(h->d_order, size_t(n) * 4) &&
               ensure_dev(h->d_cap, size_t(n) * 4) && ensure_dev(h->d_node_off, size_t(n) * 8) &&
               ensure_dev(h->d_counter, 16) &&
@@ -393,6 +450,10 @@ static bvp_status ensure_arena(bvp_handle* h, long long tot, int n, long long y0
               ensure_dev(h->d_y0, size_t(std::max<long long>(y0_vals, 1)) * 8) &&
               ensure_dev(h->d_y0_off, size_t(n + 1) * 8) && ensure_dev(h->d_out_off, size_t(n + 1) * 8) &&
               ensure_dev(h->d_norm, size_t(n) * 8);
+    if (ok && h->glob) ok = ensure_dev(h->d_gerr, T * 8);
+    if (ok && h->ho)
+        ok = ensure_dev(h->d_K_hi, T * h->L_hi.S * M * 8) && ensure_dev(h->d_pause, (size_t(2) * n + 2) * 4) &&
+             ensure_host(h->h_pause, 16);
     if (!ok) return fail(h, BVP_ERR_NOMEM, "device allocation failed");
     return BVP_OK;
 }
@@ -451,6 +512,23 @@ static void fill_args(bvp_handle* h, BvpArgs& a, int n, long long tot, int y0_mo
     a.scr = static_cast<double*>(h->d_scr.p);
     a.iscr = static_cast<int*>(h->d_iscr.p);
     a.st = static_cast<BvpInstState*>(h->d_st.p);
+    a.controller = h->glob ? o.controller : BVP_CTL_DEFECT;
+    a.global_method = o.global_method;
+    a.hybrid_de = o.hybrid_de;
+    a.hybrid_ge = o.hybrid_ge;
+    a.gerr = static_cast<double*>(h->d_gerr.p);
+    a.phase = 0;
+    if (h->ho) {
+        a.pause_count = static_cast<int*>(h->d_pause.p);
+        a.pause_list = a.pause_count + 2;
+    }
+}
+
+// Node capacity of an instance: room for max(n, max_subintervals) intervals, twice that when
+// REErrorControl solves on the halved mesh.
+static int cap_scale(const bvp_handle* h) { return (h->glob && h->opt.global_method == BVP_GLOBAL_RE) ? 2 : 1; }
+static long long cap_nodes(const bvp_handle* h, long long ni) {
+    return cap_scale(h) * std::max<long long>(ni, h->opt.max_subintervals) + 1;
 }
 
 static int fused_grid(bvp_handle* h, int n) {
@@ -465,6 +543,52 @@ static bvp_status prepare_host_outputs(bvp_handle* h, int n, long long pts_guess
 
 static constexpr int kLearnMin = 256;   // smallest batch the work-order autotuner learns from
 
+// HOErrorControl: instances stop after each round's Newton solve (and defect) and wait in a list
+// for their MIRK(p+2) solve on the same mesh, which the module of that order runs (phase 2, its
+// own stage array, the solution arrays shared); the solve's module then resumes them (phase 1)
+// from the global estimate to the next round, where they may stop again. One host
+// synchronisation per mesh round reads how many stopped.
+static bvp_status ho_rounds(bvp_handle* h, const BvpArgs& a0, int n) {
+    int* cnt = static_cast<int*>(h->d_pause.p);
+    int* lists[2] = {cnt + 2, cnt + 2 + n};
+    int* hc = static_cast<int*>(h->h_pause.p);
+    int cur = 0;
+    for (int round = 0; round <= h->opt.max_rounds + 1; ++round) {
+        CU(cudaMemcpyAsync(hc, cnt + cur, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaStreamSynchronize(h->stream));
+        const int c = *hc;
+        if (c <= 0) return BVP_OK;
+        if (c > n) return fail(h, BVP_ERR_STATE, "pause list overflow");
+        BvpArgs a2 = a0;
+        a2.phase = 2;
+        a2.n_inst = c;
+        a2.order = lists[cur];
+        a2.K = static_cast<double*>(h->d_K_hi.p);
+        a2.inst_cost = nullptr;
+        a2.host_mesh = nullptr;
+        CU(cudaMemsetAsync(a0.work_counter, 0, sizeof(int), h->stream));
+        {
+            void* args[] = {&a2};
+            CU(cudaLaunchKernel((const void*)h->k_fused_hi, dim3(fused_grid(h, c)), dim3(128), args, 0, h->stream));
+        }
+        BvpArgs a1 = a0;
+        a1.phase = 1;
+        a1.n_inst = c;
+        a1.order = lists[cur];
+        a1.pause_list = lists[cur ^ 1];
+        a1.pause_count = cnt + (cur ^ 1);
+        a1.inst_cost = nullptr;
+        CU(cudaMemsetAsync(a0.work_counter, 0, sizeof(int), h->stream));
+        CU(cudaMemsetAsync(a1.pause_count, 0, sizeof(int), h->stream));
+        {
+            void* args[] = {&a1};
+            CU(cudaLaunchKernel((const void*)h->k_fused, dim3(fused_grid(h, c)), dim3(128), args, 0, h->stream));
+        }
+        cur ^= 1;
+    }
+    return fail(h, BVP_ERR_STATE, "HOErrorControl rounds did not end");
+}
+
 static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode, const double* d_params,
                                const int* d_n_init, const double* d_tspans, const double* d_y0,
                                const long long* d_y0_off, const float* d_grid = nullptr, int n_grid = 0,
@@ -473,7 +597,8 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
     fill_args(h, a, n, tot, y0_mode, d_params, d_n_init, d_tspans, d_y0, d_y0_off);
     a.y0_grid = d_grid;
     a.n_grid = n_grid;
-    const bool learn = h->learn_left > 0 && n >= kLearnMin;
+    // the learned order times whole solves; with the MIRK(p+2) solves between launches it is not learned
+    const bool learn = h->learn_left > 0 && n >= kLearnMin && !h->ho;
     if (learn) {
         if (!h->d_cost_tab.p) {
             if (!ensure_dev(h->d_cost_tab, (BVP_COST_BUCKETS + 1) * sizeof(float)))
@@ -499,19 +624,25 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
     }
     {
         int nn = n, ms = h->opt.max_subintervals;
+        int cs = cap_scale(h);
         const int* ni = d_n_init;
         int* cap = static_cast<int*>(h->d_cap.p);
         bvp_i64* off = static_cast<bvp_i64*>(h->d_node_off.p);
         int* ord = static_cast<int*>(h->d_order.p);
         int* ctr = static_cast<int*>(h->d_counter.p);
         const float* tab = h->have_tab ? static_cast<const float*>(h->d_cost_tab.p) : nullptr;
-        void* args[] = {&nn, &ni, &ms, &cap, &off, &ord, &ctr, &tab};
+        void* args[] = {&nn, &ni, &ms, &cs, &cap, &off, &ord, &ctr, &tab};
         CU(cudaLaunchKernel((const void*)h->k_prep, dim3(1), dim3(1024), args, 0, h->stream));
     }
     CU(cudaEventRecord(h->ev[1], h->stream));
+    if (h->ho) CU(cudaMemsetAsync(a.pause_count, 0, 2 * sizeof(int), h->stream));
     {
         void* args[] = {&a};
         CU(cudaLaunchKernel((const void*)h->k_fused, dim3(fused_grid(h, n)), dim3(128), args, 0, h->stream));
+    }
+    if (h->ho) {
+        bvp_status s = ho_rounds(h, a, n);
+        if (s != BVP_OK) return s;
     }
     CU(cudaEventRecord(h->ev[2], h->stream));
     if (learn) {
@@ -618,6 +749,7 @@ static bvp_status finish(bvp_handle* h, bvp_results* out) {
             if (out->rounds) out->rounds[q] = st[q].rounds;
             if (out->defect) out->defect[q] = st[q].defect;
             if (out->resid) out->resid[q] = st[q].resid;
+            if (out->global_err) out->global_err[q] = st[q].global_err;
         }
     }
     h->have_results = true;
@@ -682,6 +814,7 @@ static bvp_status finish_host(bvp_handle* h, bvp_results* out) {
             if (out->rounds) out->rounds[q] = st[q].rounds;
             if (out->defect) out->defect[q] = st[q].defect;
             if (out->resid) out->resid[q] = st[q].resid;
+            if (out->global_err) out->global_err[q] = st[q].global_err;
         }
     }
     h->have_results = true;
@@ -1248,7 +1381,7 @@ static bvp_status solve_large(bvp_handle* h, int n, const double* params, const 
         const LargeInst& L = I[q];
         BvpInstState& st = h->st[q];
         st.N = L.N; st.cur = 0; st.retcode = L.retcode; st.newton_iters = L.newton_total; st.rounds = L.rounds;
-        st.flags = L.flags; st.defect = L.defect; st.resid = L.resid;
+        st.flags = L.flags; st.defect = L.defect; st.resid = L.resid; st.global_err = std::nan("");
         const long long o0 = h->offsets[q];
         std::memcpy(hm + o0, L.mesh.data(), size_t(L.N) * 8);
         CU(cudaMemcpyAsync(hy + o0 * M, static_cast<const double*>(h->d_y.p) + L.off * M, size_t(L.N) * M * 8,
@@ -1282,6 +1415,7 @@ static bvp_status solve_large(bvp_handle* h, int n, const double* params, const 
             if (out->rounds) out->rounds[q] = st.rounds;
             if (out->defect) out->defect[q] = st.defect;
             if (out->resid) out->resid[q] = st.resid;
+            if (out->global_err) out->global_err[q] = st.global_err;
         }
     }
     return BVP_OK;
@@ -1301,7 +1435,7 @@ bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const
         if (ni < 1) return fail(h, BVP_ERR_INVALID, "n_intervals must be >= 1");
         if (!(tspans[2 * q + 1] > tspans[2 * q])) return fail(h, BVP_ERR_INVALID, "tspan must satisfy t0 < t1");
         pts += ni + 1;
-        tot += std::max(ni, h->opt.max_subintervals) + 1;
+        tot += cap_nodes(h, ni);
         y0_vals += (y0_mode == 1) ? (long long)(ni + 1) * M : M;
     }
     bvp_status s = ensure_arena(h, tot, n, y0_vals);
@@ -1351,7 +1485,7 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
         if (ni < 1) return fail(h, BVP_ERR_INVALID, "n_intervals must be >= 1");
         if (!(tspans[2 * q + 1] > tspans[2 * q])) return fail(h, BVP_ERR_INVALID, "tspan must satisfy t0 < t1");
         pts += ni + 1;
-        tot += std::max(ni, h->opt.max_subintervals) + 1;
+        tot += cap_nodes(h, ni);
         y0_vals += (long long)(ni + 1) * M;
     }
     (void)y0_vals;
@@ -1444,6 +1578,7 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
             if (out->rounds) out->rounds[q] = st.rounds;
             if (out->defect) out->defect[q] = st.defect;
             if (out->resid) out->resid[q] = st.resid;
+            if (out->global_err) out->global_err[q] = st.global_err;
         }
     }
     return BVP_OK;
@@ -1456,7 +1591,7 @@ bvp_status bvp_solve_batch_device(bvp_handle* h, int32_t n, const double* d_para
     if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: only bvp_solve_batch is available");
     if (n < 1 || !d_n_intervals || !d_tspans || !d_y0 || max_intervals < 1 || (y0_mode == 1 && !d_y0_off))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
-    const long long tot = (long long)n * (std::max<int>(max_intervals, h->opt.max_subintervals) + 1);
+    const long long tot = (long long)n * cap_nodes(h, max_intervals);
     bvp_status s = ensure_arena(h, tot, n, 1);
     if (s != BVP_OK) return s;
     const double* dp = d_params ? d_params : static_cast<const double*>(h->d_params.p);
@@ -1476,7 +1611,7 @@ bvp_status bvp_solve_batch_device_grid(bvp_handle* h, int32_t n, const double* d
     if (n < 1 || !d_n_intervals || !d_tspans || !d_grid || n_grid < 2 || max_intervals < 1 ||
         (h->desc.n_params > 0 && !d_params))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
-    const long long tot = (long long)n * (std::max<int>(max_intervals, h->opt.max_subintervals) + 1);
+    const long long tot = (long long)n * cap_nodes(h, max_intervals);
     bvp_status s = ensure_arena(h, tot, n, 1);
     if (s != BVP_OK) return s;
     s = launch_solve(h, n, tot, 2, d_params, d_n_intervals, d_tspans, static_cast<const double*>(h->d_y0.p),
@@ -1500,6 +1635,7 @@ bvp_status bvp_fetch_results(bvp_handle* h, bvp_results* out) {
                 if (out->rounds) out->rounds[q] = st.rounds;
                 if (out->defect) out->defect[q] = st.defect;
                 if (out->resid) out->resid[q] = st.resid;
+                if (out->global_err) out->global_err[q] = st.global_err;
             }
         }
         return BVP_OK;
@@ -1692,15 +1828,18 @@ void bvp_destroy(bvp_handle* h) {
                       &h->d_out_y, &h->d_out_K, &h->d_out_KI, &h->d_norm, &h->d_feat, &h->d_grid,
                       // the larger-state path's per-instance arrays
                       &h->d_bcres, &h->d_G, &h->d_lnorm, &h->d_lsq, &h->d_ldnorm, &h->d_lbad,
-                      &h->d_active, &h->d_N, &h->d_newN};
+                      &h->d_active, &h->d_N, &h->d_newN,
+                      // work-order tables and the error controllers' arrays
+                      &h->d_inst_cost, &h->d_cost_tab, &h->d_gerr, &h->d_K_hi, &h->d_pause};
     for (DevBuf* b : devs)
         if (b->p) cudaFree(b->p);
-    HostBuf* hosts[] = {&h->h_in, &h->h_st, &h->h_off, &h->h_mesh, &h->h_y, &h->h_K, &h->h_KI};
+    HostBuf* hosts[] = {&h->h_in, &h->h_st, &h->h_off, &h->h_mesh, &h->h_y, &h->h_K, &h->h_KI, &h->h_pause};
     for (HostBuf* b : hosts)
         if (b->p) cudaFreeHost(b->p);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
     if (h->lib) cudaLibraryUnload(h->lib);
+    if (h->lib_hi) cudaLibraryUnload(h->lib_hi);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }

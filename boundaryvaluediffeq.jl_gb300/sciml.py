@@ -45,6 +45,66 @@ class MIRK:
             raise ValueError("jac_precision must be 32 or 64")
 
 
+@dataclass(frozen=True)
+class HOErrorControl:
+    """The global error from a MIRK(p+2) solve on the same mesh (calc_errors.jl:99-110)."""
+
+
+@dataclass(frozen=True)
+class REErrorControl:
+    """The global error by Richardson extrapolation from the halved mesh (calc_errors.jl:113-127)."""
+
+
+@dataclass(frozen=True)
+class DefectControl:
+    """DefectControl(; defect_threshold = 0.1) (calc_errors.jl:54-60): the default controller."""
+    defect_threshold: float = 0.1
+
+
+@dataclass(frozen=True)
+class GlobalErrorControl:
+    """GlobalErrorControl(; method = HOErrorControl()) (calc_errors.jl:67-73)."""
+    method: object = HOErrorControl()
+
+
+@dataclass(frozen=True)
+class SequentialErrorControl:
+    """SequentialErrorControl(; defect, global_error) (calc_errors.jl:80-87): the defect first,
+    the global error once the defect is within abstol."""
+    defect: DefectControl = DefectControl()
+    global_error: GlobalErrorControl = GlobalErrorControl()
+
+
+@dataclass(frozen=True)
+class HybridErrorControl:
+    """HybridErrorControl(; DE = 1.0, GE = 1.0, defect, global_error) (calc_errors.jl:93-107):
+    the norm DE * defect + GE * global error."""
+    DE: float = 1.0
+    GE: float = 1.0
+    defect: DefectControl = DefectControl()
+    global_error: GlobalErrorControl = GlobalErrorControl()
+
+
+def _controller_options(c) -> dict:
+    """The C ABI's controller fields for a controller object."""
+    def method(g):
+        if isinstance(g.method, HOErrorControl):
+            return 0
+        if isinstance(g.method, REErrorControl):
+            return 1
+        raise TypeError(f"unknown global error method {g.method!r}")
+    if isinstance(c, DefectControl):
+        return dict(controller=0, defect_threshold=c.defect_threshold)
+    if isinstance(c, GlobalErrorControl):
+        return dict(controller=1, global_method=method(c))
+    if isinstance(c, SequentialErrorControl):
+        return dict(controller=2, global_method=method(c.global_error), defect_threshold=c.defect.defect_threshold)
+    if isinstance(c, HybridErrorControl):
+        return dict(controller=3, global_method=method(c.global_error), hybrid_de=float(c.DE),
+                    hybrid_ge=float(c.GE), defect_threshold=c.defect.defect_threshold)
+    raise TypeError(f"unknown error controller {c!r}")
+
+
 def MIRK2(**kw): return MIRK(2, **kw)  # noqa: E704
 def MIRK3(**kw): return MIRK(3, **kw)  # noqa: E704
 def MIRK4(**kw): return MIRK(4, **kw)  # noqa: E704
@@ -123,14 +183,16 @@ def _n_intervals(tspan, dt) -> int:
 _CACHE: dict = {}
 
 
-def _solver(problem, alg: MIRK, abstol, adaptive, dense, solver_cls):
-    key = (problem.name, problem.source, alg, float(abstol), int(adaptive), int(dense), solver_cls)
+def _solver(problem, alg: MIRK, abstol, adaptive, dense, solver_cls, controller=None):
+    key = (problem.name, problem.source, alg, float(abstol), int(adaptive), int(dense), solver_cls, controller)
     sv = _CACHE.get(key)
     if sv is None:
+        opts = dict(defect_threshold=alg.defect_threshold)
+        if controller is not None:
+            opts.update(_controller_options(controller))
         sv = solver_cls(problem, order=alg.order, abstol=abstol, jac_precision=alg.jac_precision,
                         adaptive=int(adaptive), want_stages=int(dense),
-                        max_subintervals=alg.max_num_subintervals, defect_threshold=alg.defect_threshold,
-                        mirk6i=int(alg.mirk6i))
+                        max_subintervals=alg.max_num_subintervals, mirk6i=int(alg.mirk6i), **opts)
         _CACHE[key] = sv
     return sv
 
@@ -148,10 +210,12 @@ def _to_solutions(res, solver, dense):
 
 
 def solve(prob, alg: MIRK, *, dt: float, abstol: float = 1e-6, adaptive: bool = True, p=None, u0=None,
-          dense: bool = True, _solver_cls=BatchSolver):
-    """solve(prob, MIRKn(); dt, abstol) for one problem, or for an EnsembleProblem (one batched
-    call over its trajectories). ``u0`` is a constant guess (M values) or per-node guesses on
-    the initial uniform mesh ((n + 1) x M); ``p`` the parameters."""
+          dense: bool = True, controller=None, _solver_cls=BatchSolver):
+    """solve(prob, MIRKn(); dt, abstol, controller) for one problem, or for an EnsembleProblem
+    (one batched call over its trajectories). ``u0`` is a constant guess (M values) or per-node
+    guesses on the initial uniform mesh ((n + 1) x M); ``p`` the parameters; ``controller`` one
+    of DefectControl() (the default), GlobalErrorControl(), SequentialErrorControl(),
+    HybridErrorControl() (mirk.jl:50-51)."""
     if isinstance(prob, EnsembleProblem):
         base = prob.problem
         n = prob.trajectories or (len(prob.params) if prob.params is not None else 1)
@@ -162,7 +226,7 @@ def solve(prob, alg: MIRK, *, dt: float, abstol: float = 1e-6, adaptive: bool = 
         y0 = (np.tile(np.asarray(base.u0, dtype=np.float64), (n, 1)) if prob.u0 is None
               else np.asarray(prob.u0, dtype=np.float64).reshape(n, base.M))
         nint = np.array([_n_intervals(ts, dt) for ts in tsp], np.int32)
-        sv = _solver(base, alg, abstol, adaptive, dense, _solver_cls)
+        sv = _solver(base, alg, abstol, adaptive, dense, _solver_cls, controller)
         res = sv.solve(params, nint, tsp, y0, y0_mode=0)
         return _to_solutions(res, sv, dense)
     n = _n_intervals(prob.tspan, dt)
@@ -176,10 +240,11 @@ def solve(prob, alg: MIRK, *, dt: float, abstol: float = 1e-6, adaptive: bool = 
         y0, mode = guess, 1
     else:
         raise ValueError(f"u0 must hold {prob.M} values or ({n + 1}, {prob.M}) per-node values")
-    sv = _solver(prob, alg, abstol, adaptive, dense, _solver_cls)
+    sv = _solver(prob, alg, abstol, adaptive, dense, _solver_cls, controller)
     res = sv.solve(params, np.array([n], np.int32), np.asarray([prob.tspan], dtype=np.float64), y0, y0_mode=mode)
     return _to_solutions(res, sv, dense)[0]
 
 
 __all__ = ["solve", "MIRK", "MIRK2", "MIRK3", "MIRK4", "MIRK5", "MIRK6", "MIRK6I", "EnsembleProblem", "BVPSolution",
-           "RET_SUCCESS", "RET_MAXITERS"]
+           "DefectControl", "GlobalErrorControl", "SequentialErrorControl", "HybridErrorControl",
+           "HOErrorControl", "REErrorControl", "RET_SUCCESS", "RET_MAXITERS"]

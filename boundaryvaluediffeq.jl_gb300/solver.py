@@ -45,6 +45,7 @@ class BatchResult:
     K_packed: np.ndarray | None = None
     KI_packed: np.ndarray | None = None
     order: int = 4
+    global_err: np.ndarray | None = None    # last global error estimate (NaN under DefectControl)
 
     @property
     def mesh(self):
@@ -92,6 +93,11 @@ class BatchSolver:
         o = _lib.Options()
         self.lib.bvp_default_options(C.byref(o))
         o.order, o.abstol, o.jac_precision = order, abstol, jac_precision
+        # controller="defect" | "global" | "sequential" | "hybrid", global_method="HO" | "RE"
+        if isinstance(opts.get("controller"), str):
+            opts["controller"] = _lib.CONTROLLERS[opts["controller"]]
+        if isinstance(opts.get("global_method"), str):
+            opts["global_method"] = _lib.GLOBAL_METHODS[opts["global_method"]]
         for k, v in opts.items():
             if not hasattr(o, k):
                 raise KeyError(k)
@@ -123,9 +129,9 @@ class BatchSolver:
     def _results(self, n):
         r = dict(retcode=np.zeros(n, np.int32), n_nodes=np.zeros(n, np.int32),
                  newton_iters=np.zeros(n, np.int32), rounds=np.zeros(n, np.int32),
-                 defect=np.zeros(n), resid=np.zeros(n))
+                 defect=np.zeros(n), resid=np.zeros(n), global_err=np.zeros(n))
         cr = _lib.Results(i32(r["retcode"]), i32(r["n_nodes"]), i32(r["newton_iters"]),
-                          i32(r["rounds"]), f64(r["defect"]), f64(r["resid"]))
+                          i32(r["rounds"]), f64(r["defect"]), f64(r["resid"]), f64(r["global_err"]))
         return r, cr
 
     def _collect(self, r):

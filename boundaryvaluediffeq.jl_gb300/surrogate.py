@@ -207,7 +207,9 @@ def merge_results(base, sub, idx, M):
     sols_m, sols_y = [], []
     j = {int(q): k for k, q in enumerate(idx)}
     fields = {}
-    for name in ("retcode", "n_nodes", "newton_iters", "rounds", "defect", "resid"):
+    for name in ("retcode", "n_nodes", "newton_iters", "rounds", "defect", "resid", "global_err"):
+        if getattr(base, name) is None or getattr(sub, name) is None:
+            continue
         arr = getattr(base, name).copy()
         arr[idx] = getattr(sub, name)
         fields[name] = arr

@@ -73,7 +73,29 @@ typedef struct {
     int32_t mirk6i;               /* 1 with order 6: MIRK6I, the order-6 scheme with Lobatto-point
                                      stages and its own interpolant (mirk_tableaus.jl:154-194,
                                      interpolation.jl:583-693; BoundaryValueDiffEqMIRK.jl:179) */
+    int32_t controller;           /* bvp_controller: the __init kwarg `controller`
+                                     (Core/src/calc_errors.jl:54-139); M <= 8 */
+    int32_t global_method;        /* bvp_global_method of the global estimate (the controller's
+                                     GlobalErrorControl(method = ...)) */
+    double hybrid_de, hybrid_ge;  /* HybridErrorControl(DE, GE) */
 } bvp_options;
+
+/* Error controllers (lib/BoundaryValueDiffEqCore/src/calc_errors.jl:54-139, the error
+ * estimates of lib/BoundaryValueDiffEqMIRK/src/adaptivity.jl:361-567). With HOErrorControl the
+ * solve synchronises with the host once per mesh round (the MIRK(p+2) solves run between
+ * launches), also in bvp_solve_batch_device. */
+typedef enum {
+    BVP_CTL_DEFECT = 0,      /* DefectControl: the defect of the continuous extension (default) */
+    BVP_CTL_GLOBAL = 1,      /* GlobalErrorControl: the global error estimate alone */
+    BVP_CTL_SEQUENTIAL = 2,  /* SequentialErrorControl: the defect, then the global estimate
+                                once the defect is within abstol */
+    BVP_CTL_HYBRID = 3       /* HybridErrorControl: DE * defect + GE * global */
+} bvp_controller;
+
+typedef enum {
+    BVP_GLOBAL_HO = 0,       /* HOErrorControl: MIRK(p+2) on the same mesh (orders 2, 3, 4) */
+    BVP_GLOBAL_RE = 1        /* REErrorControl: Richardson extrapolation from the halved mesh */
+} bvp_global_method;
 
 /* Per-instance outputs of a batch (caller-owned arrays of n_inst entries; any may be NULL). */
 typedef struct {
@@ -83,6 +105,7 @@ typedef struct {
     int32_t* rounds;        /* outer mesh rounds */
     double* defect;         /* last defect norm */
     double* resid;          /* last ||F||_inf */
+    double* global_err;     /* last global error estimate (controllers other than DefectControl) */
 } bvp_results;
 
 typedef struct bvp_handle_s bvp_handle;

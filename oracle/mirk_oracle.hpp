@@ -61,6 +61,12 @@ struct Options {
     double defect_threshold;   // reference default 0.1 (calc_errors.jl:54-60)
     double divergence_factor;
     int32_t mirk6i;            // 1 with order 6: MIRK6I (mirk_tableaus.jl:154-194)
+    // error controller (Core/src/calc_errors.jl:54-139): 0 DefectControl, 1 GlobalErrorControl,
+    // 2 SequentialErrorControl, 3 HybridErrorControl; the global estimate's method: 0
+    // HOErrorControl (MIRK(p+2) on the same mesh), 1 REErrorControl (same method, halved mesh)
+    int32_t controller;
+    int32_t global_method;
+    double hybrid_de, hybrid_ge;   // HybridErrorControl's DE and GE weights
 };
 
 inline void fill_default_options(Options* o) {
@@ -68,7 +74,14 @@ inline void fill_default_options(Options* o) {
     o->max_rounds = 64; o->transfer_inplace = 1; o->bc_jac_exact = 0;
     o->linesearch_fallback = 1; o->stall_steps = 32; o->nthreads = 0;
     o->abstol = 1e-6; o->defect_threshold = 0.1; o->divergence_factor = 1e3; o->mirk6i = 0;
+    o->controller = 0; o->global_method = 0; o->hybrid_de = 1.0; o->hybrid_ge = 1.0;
 }
+
+enum Controller : int32_t { CTL_DEFECT = 0, CTL_GLOBAL = 1, CTL_SEQUENTIAL = 2, CTL_HYBRID = 3 };
+enum GlobalMethod : int32_t { GLOBAL_HO = 0, GLOBAL_RE = 1 };
+
+// Julia's max over values that may be NaN: NaN wins (Base.max, used by maximum).
+inline double julia_max(double a, double b) { return (std::isnan(a) || std::isnan(b)) ? NAN : std::max(a, b); }
 
 // Julia's round(Int, x): round half to even (the default rounding mode of rint).
 inline long round_even(double x) { return (long)std::nearbyint(x); }
@@ -122,6 +135,7 @@ struct InstanceSolver {
     using DualU = Dual<M>;  // tangents along one BC evaluation point
 
     const Tableau& tb;
+    const Tableau* tb_hi = nullptr;    // MIRK(p+2), for the HOErrorControl estimate
     const Options& op;
     const ProblemInfo& pi;
     const double* p;
@@ -136,6 +150,7 @@ struct InstanceSolver {
     int newton_total = 0, rounds = 0, retcode = RET_FAILURE, newton_last = 0;
     double last_defect = std::numeric_limits<double>::quiet_NaN();
     double last_resid = std::numeric_limits<double>::quiet_NaN();
+    double last_global = std::numeric_limits<double>::quiet_NaN();   // last global error norm
 
     InstanceSolver(const Tableau& t, const Options& o, const ProblemInfo& info, const double* params)
         : tb(t), op(o), pi(info), p(params) {}
@@ -584,15 +599,83 @@ struct InstanceSolver {
         return dn;
     }
 
-    // Stages of the final solution for dense output (interpolation.jl:17-204 reads the
-    // cache's K and extra stages of the last residual / defect evaluation).
-    void finalize_stages() {
-        residual();
+    // --- the interpolant's extra stages at the current solution (interp_setup!,
+    // interpolation.jl:337-372)
+    void interp_setup() {
         const int S = tb.s, NS = std::max(1, ns());
         KI.assign(size_t(N - 1) * NS * M, 0.0);
         for (int i = 0; i < N - 1; ++i)
             interp_stages_interval<double>(i, &y[i * M], &y[(i + 1) * M], &K[size_t(i) * S * M],
                                            &KI[size_t(i) * NS * M]);
+    }
+
+    // Stages of the final solution for dense output (interpolation.jl:17-204 reads the
+    // cache's K and extra stages of the last residual / defect evaluation).
+    void finalize_stages() {
+        residual();
+        interp_setup();
+    }
+
+    // --- global error estimate (adaptivity.jl:508-567). A second, non-adaptive solve starts
+    // from the current solution: REErrorControl on the halved mesh with the same method
+    // (halve_sol, adaptivity.jl:310-332: the old nodes at the even 0-based positions, each new
+    // midpoint node the mean of its neighbours), HOErrorControl with MIRK(p+2) on the same mesh
+    // (__high_order_method, adaptivity.jl:552-555). The new cache takes mesh_dt = diff(mesh)
+    // (mirk.jl:75-76), and the outcome of its Newton solve is not consulted. At each current
+    // node err_j = max_m |(y_high - y) / (1 + |y|)|, each interval keeps the larger of its two
+    // end nodes' errors (GE_subinterval!, adaptivity.jl:557-567), the norm is their maximum,
+    // times 2^p / (2^p - 1) for Richardson extrapolation (adaptivity.jl:534). The estimate is
+    // taken against the low-order solution as it stands before the second solve (the
+    // estimators' documented formulas, calc_errors.jl:99-128).
+    std::vector<double> gerr;   // per interval
+    double global_estimate() {
+        const bool re = op.global_method == GLOBAL_RE;
+        InstanceSolver<M> hs(re ? tb : *tb_hi, op, pi, p);
+        const int n = N - 1;
+        if (re) {
+            hs.N = 2 * n + 1;
+            hs.mesh.assign(hs.N, 0.0);
+            hs.y.assign(size_t(hs.N) * M, 0.0);
+            for (int i = 0; i <= n; ++i) {
+                hs.mesh[2 * i] = mesh[i];
+                for (int m = 0; m < M; ++m) hs.y[size_t(2 * i) * M + m] = y[size_t(i) * M + m];
+            }
+            for (int i = 0; i < n; ++i) {
+                hs.mesh[2 * i + 1] = (hs.mesh[2 * i + 2] + hs.mesh[2 * i]) / 2.0;
+                for (int m = 0; m < M; ++m)
+                    hs.y[size_t(2 * i + 1) * M + m] =
+                        (hs.y[size_t(2 * i + 2) * M + m] + hs.y[size_t(2 * i) * M + m]) / 2.0;
+            }
+        } else {
+            hs.N = N;
+            hs.mesh = mesh;
+            hs.y = y;
+        }
+        hs.h.resize(hs.N - 1);
+        for (int q = 0; q + 1 < hs.N; ++q) hs.h[q] = hs.mesh[q + 1] - hs.mesh[q];
+        hs.newton();
+        const int stride = re ? 2 : 1;
+        std::vector<double> en(N);
+        for (int j = 0; j < N; ++j) {
+            double e = 0.0;
+            for (int m = 0; m < M; ++m) {
+                const double lo = y[size_t(j) * M + m];
+                e = julia_max(e, std::fabs((hs.y[size_t(stride * j) * M + m] - lo) / (1.0 + std::fabs(lo))));
+            }
+            en[j] = e;
+        }
+        gerr.assign(n, 0.0);
+        double g = 0.0;
+        for (int i = 0; i < n; ++i) {
+            gerr[i] = en[i] >= en[i + 1] ? en[i] : en[i + 1];
+            g = julia_max(g, gerr[i]);
+        }
+        if (re) {
+            const double p2 = double(1 << tb.order);
+            g = g * p2 / (p2 - 1.0);
+        }
+        last_global = g;
+        return g;
     }
 
     // --- half_mesh! (adaptivity.jl:287-301)
@@ -637,13 +720,25 @@ struct InstanceSolver {
         N = Nsub + 1;
     }
 
-    // --- mesh_selector!(DefectControl) (adaptivity.jl:23-75); returns false on Failure.
-    bool mesh_selector(std::vector<double>& old_mesh, std::vector<double>& old_h) {
+    // --- mesh_selector! (adaptivity.jl:23-243); returns false on Failure. ŝ per interval from
+    // the controller's errors: DefectControl (defect / abstol)^(1/(p+1)) with ρ = 1 (23-75);
+    // GlobalErrorControl (global / abstol)^(1/p), ρ = 2 (77-125); SequentialErrorControl the
+    // errors of this round's estimate (the global ones when the defect passed) to 1/(p+1),
+    // ρ = 2 (127-177); HybridErrorControl the sum of the defect and global terms, each to
+    // 1/(p+1), ρ = 2 (179-243).
+    bool mesh_selector(std::vector<double>& old_mesh, std::vector<double>& old_h,
+                       int ctl = CTL_DEFECT, bool seq_global = false) {
         const int n = N - 1;
-        const double safety = 1.3, rho = 1.0;
+        const double safety = 1.3, rho = ctl == CTL_DEFECT ? 1.0 : 2.0;
         const int ub = 4 * (N - 1), lb = N / 2;
         std::vector<double> s_hat(n);
-        for (int i = 0; i < n; ++i) s_hat[i] = std::pow(err_max[i] / op.abstol, 1.0 / (tb.order + 1));
+        const double e1 = 1.0 / (tb.order + 1);
+        for (int i = 0; i < n; ++i) {
+            if (ctl == CTL_DEFECT) s_hat[i] = std::pow(err_max[i] / op.abstol, e1);
+            else if (ctl == CTL_GLOBAL) s_hat[i] = std::pow(gerr[i] / op.abstol, 1.0 / tb.order);
+            else if (ctl == CTL_SEQUENTIAL) s_hat[i] = std::pow((seq_global ? gerr : err_max)[i] / op.abstol, e1);
+            else s_hat[i] = std::pow(err_max[i] / op.abstol, e1) + std::pow(gerr[i] / op.abstol, e1);
+        }
         double r1 = -INFINITY, r2 = 0;
         for (int i = 0; i < n; ++i) { r1 = std::max(r1, s_hat[i]); r2 += s_hat[i]; }
         const double r3 = r2 / (N - 1);
@@ -709,18 +804,42 @@ struct InstanceSolver {
 #endif
             if (!op.adaptive) { retcode = nl_ok ? RET_SUCCESS : RET_FAILURE; return; }
             bool ok = nl_ok;
+            bool seq_global = false;
             if (ok) {
-                error_norm = defect_estimate();
+                // error_estimate! for the controller (adaptivity.jl:361-503). A norm that is not
+                // finite counts as a failed round, for every controller.
+                if (op.controller == CTL_DEFECT) {
+                    error_norm = defect_estimate();
+                    ok = !(error_norm > op.defect_threshold);
+                } else if (op.controller == CTL_GLOBAL) {
+                    // the global estimate alone (361-368); the transfer below reads the
+                    // interpolant's extra stages at this solution
+                    error_norm = global_estimate();
+                    interp_setup();
+                } else if (op.controller == CTL_SEQUENTIAL) {
+                    // the defect first, the global estimate once the defect is within abstol
+                    // (464-482)
+                    error_norm = defect_estimate();
+                    ok = !(error_norm > op.defect_threshold);
+                    if (ok && error_norm <= op.abstol) {
+                        seq_global = true;
+                        error_norm = global_estimate();
+                    }
+                } else {
+                    // DE * defect + GE * global; the defect threshold does not apply (485-503)
+                    const double dn = defect_estimate();
+                    const double gn = global_estimate();
+                    error_norm = op.hybrid_de * dn + op.hybrid_ge * gn;
+                }
 #ifdef BVP_TRACE
-                fprintf(stderr, "   defect=%.3e\n", error_norm);
+                fprintf(stderr, "   error=%.3e\n", error_norm);
 #endif
-                ok = !(error_norm > op.defect_threshold);
-                if (std::isnan(error_norm)) ok = false;
+                if (!std::isfinite(error_norm)) ok = false;
             }
             if (ok) {
                 if (error_norm > op.abstol) {
                     std::vector<double> om, oh;
-                    if (mesh_selector(om, oh)) {
+                    if (mesh_selector(om, oh, op.controller, seq_global)) {
                         transfer(om, oh);
                         info_ok = 1;
                     } else {

@@ -42,7 +42,13 @@ class Options(C.Structure):
         ("stall_steps", C.c_int32), ("nthreads", C.c_int32),
         ("abstol", C.c_double), ("defect_threshold", C.c_double),
         ("divergence_factor", C.c_double), ("mirk6i", C.c_int32),
+        ("controller", C.c_int32), ("global_method", C.c_int32),
+        ("hybrid_de", C.c_double), ("hybrid_ge", C.c_double),
     ]
+
+
+CONTROLLERS = {"defect": 0, "global": 1, "sequential": 2, "hybrid": 3}
+GLOBAL_METHODS = {"HO": 0, "RE": 1}
 
 
 def stage_counts(order: int, mirk6i: int = 0):
@@ -109,6 +115,10 @@ class Oracle:
     def options(self, **kw) -> Options:
         o = Options()
         self.lib.oracle_default_options(C.byref(o))
+        if isinstance(kw.get("controller"), str):
+            kw["controller"] = CONTROLLERS[kw["controller"]]
+        if isinstance(kw.get("global_method"), str):
+            kw["global_method"] = GLOBAL_METHODS[kw["global_method"]]
         for k, v in kw.items():
             if not hasattr(o, k):
                 raise KeyError(k)
@@ -133,7 +143,7 @@ class Oracle:
             retcode=np.zeros(n, np.int32), n_nodes=np.zeros(n, np.int32),
             mesh=np.zeros((n, cap_nodes)), y=np.zeros((n, cap_nodes, M)),
             newton_iters=np.zeros(n, np.int32), rounds=np.zeros(n, np.int32),
-            defect=np.zeros(n), resid=np.zeros(n),
+            defect=np.zeros(n), resid=np.zeros(n), global_err=np.zeros(n),
         )
         K = KI = None
         if want_stages:
@@ -146,7 +156,9 @@ class Oracle:
             _p(out["mesh"], C.c_double), _p(out["y"], C.c_double),
             _p(out["newton_iters"], C.c_int32), _p(out["rounds"], C.c_int32),
             _p(out["defect"], C.c_double), _p(out["resid"], C.c_double),
-            _p(K, C.c_double), _p(KI, C.c_double))
+            _p(K, C.c_double), _p(KI, C.c_double), _p(out["global_err"], C.c_double))
+        if rc == -3:
+            raise ValueError("HOErrorControl needs MIRK(order + 2): orders 2, 3 and 4 only")
         if rc != 0:
             raise RuntimeError(f"oracle_solve_batch failed: {rc}")
         if want_stages:

@@ -72,10 +72,14 @@ int oracle_solve_batch(const ProblemInfo* info, const Options* opt, int n_inst,
                        int y0_mode, const double* y0, int cap_nodes, int32_t* retcode,
                        int32_t* n_nodes, double* mesh_out, double* y_out, int32_t* newton_iters,
                        int32_t* rounds, double* defect, double* resid, double* K_out,
-                       double* KI_out) {
+                       double* KI_out, double* global_err) {
     if (info->M != MM) return -1;
     const Tableau tb = make_tableau(opt->order, opt->mirk6i);
     if (tb.order == 0) return -2;
+    // HOErrorControl solves with MIRK(p+2) (adaptivity.jl:552-555): MIRK4, MIRK5, MIRK6 exist
+    const bool ho = opt->adaptive && opt->controller != CTL_DEFECT && opt->global_method == GLOBAL_HO;
+    const Tableau tb_hi = ho ? make_tableau(opt->order + 2) : Tableau();
+    if (ho && (opt->mirk6i || opt->order + 2 > 6)) return -3;
     std::vector<int64_t> y0_off(n_inst + 1, 0);
     for (int i = 0; i < n_inst; ++i)
         y0_off[i + 1] = y0_off[i] + (y0_mode == 1 ? int64_t(n_intervals[i] + 1) * MM : MM);
@@ -87,6 +91,7 @@ int oracle_solve_batch(const ProblemInfo* info, const Options* opt, int n_inst,
 #endif
     for (int q = 0; q < n_inst; ++q) {
         InstanceSolver<MM> sv(tb, *opt, *info, params + size_t(q) * info->n_params);
+        if (ho) sv.tb_hi = &tb_hi;
         const int n = n_intervals[q];
         sv.N = n + 1;
         sv.mesh.resize(n + 1);
@@ -109,6 +114,7 @@ int oracle_solve_batch(const ProblemInfo* info, const Options* opt, int n_inst,
         rounds[q] = sv.rounds;
         defect[q] = sv.last_defect;
         resid[q] = sv.last_resid;
+        if (global_err) global_err[q] = sv.last_global;
         const int nc = std::min(sv.N, cap_nodes);
         if (sv.N > cap_nodes) retcode[q] = 3;
         for (int i = 0; i < nc; ++i) {

@@ -1,6 +1,7 @@
 """The kernels compile through NVRTC for sm_103a exactly as bvp_create compiles them (same
 source assembly and options), for every MIRK order and MIRK6I, both Jacobian precisions, standard and
-two-point problems, the larger-state family and a problem with a singular term. NVRTC runs on
+two-point problems, the larger-state family, a problem with a singular term, and the build
+with the global-error controllers. NVRTC runs on
 the CPU, so this catches JIT-only compile errors without a GPU."""
 import pytest
 
@@ -14,6 +15,8 @@ CASES = [
     ("multipoint", 4, 32), ("affine_twopoint", 3, 64), ("torus", 4, 32),
     ("lane_emden", 6, 64), ("nonlinear32", 6, 32), ("nonlinear32", 4, 64), ("nonlinear32", 3, 32), ("mathieu", 4, 32),
     ("pendulum", 6, 32, 1), ("singular_perturbation", 6, 64, 1), ("nonlinear32", 6, 32, 1),
+    # the build with the global-error controllers (BVP_GLOBAL_CTL), and the MIRK(p+2) module of HO
+    ("torus", 4, 64, 0, 1), ("pendulum", 6, 32, 0, 1),
 ]
 
 

@@ -242,3 +242,53 @@ def test_mirk6i_interpolant_consistency(problems):
         assert np.abs(ends - y[i + 1]).max() < 1e-8
         d0 = o.interpolate(6, mesh, y, K, KI, [mesh[i] + 1e-12 * h], deriv=1, mirk6i=1)[0]
         assert np.abs(d0 - K[i, 0]).max() < 1e-8
+
+
+# ---- error controllers (Core/src/calc_errors.jl:54-139; adaptivity.jl:77-243, 361-567) ------
+GLOBAL_CASES = [("global", "HO"), ("global", "RE"), ("sequential", "HO"), ("sequential", "RE"),
+                ("hybrid", "HO"), ("hybrid", "RE")]
+
+
+@pytest.mark.parametrize("ctl,gm", [("defect", "HO")] + GLOBAL_CASES)
+def test_error_control_adaptivity(problems, ctl, gm):
+    # mirk_basic_tests.jl:414-434: the pendulum with its BCs at pi/4 and pi/2, MIRK4, dt = 0.05,
+    # abstol 1e-5, under each controller (GlobalErrorControl() defaults to HOErrorControl)
+    p = problems.PENDULUM
+    o, r, N = _solve1(p, dt=0.05, params=(9.81, 0.0, 0.0), order=4, abstol=1e-5, controller=ctl, global_method=gm)
+    assert r["retcode"][0] == RET_SUCCESS
+    m, y = r["mesh"][0, :N], r["y"][0, :N]
+    assert o.residual((9.81, 0.0, 0.0), m, y)[2] <= 1e-5
+    assert np.abs(y[:, 0]).max() < 3.0
+
+
+@pytest.mark.parametrize("order", [3, 4, 5, 6])
+def test_richardson_estimate_controls_the_error(problems, order):
+    # GlobalErrorControl(method = REErrorControl()) on the linear problem (exact solution known):
+    # the accepted estimate is within abstol, and so is the error it estimates, in the
+    # estimator's measure |y - u| / (1 + |y|) (calc_errors.jl:113-127)
+    p = problems.LINEAR
+    o, r, N = _solve1(p, n=10, order=order, controller="global", global_method="RE")
+    assert r["retcode"][0] == RET_SUCCESS
+    m, y = r["mesh"][0, :N], r["y"][0, :N]
+    rel = np.abs((y - problems.linear_analytic(m)) / (1 + np.abs(y))).max()
+    assert r["global_err"][0] <= 1e-6 and rel <= 2e-6, (r["global_err"][0], rel)
+    assert math.isnan(r["defect"][0])            # no defect pass under GlobalErrorControl
+
+
+@pytest.mark.parametrize("ctl,gm", GLOBAL_CASES)
+def test_global_controllers_converge_on_the_torus(problems, ctl, gm):
+    # mirk_basic_tests.jl:726-756's geodesic under the other controllers
+    p = problems.TORUS
+    a1, a2 = (0.5, -1.2), (-0.5, 0.3)
+    o, r, N = _solve1(p, dt=0.05, params=a1 + a2, order=4, controller=ctl, global_method=gm)
+    assert r["retcode"][0] == RET_SUCCESS
+    y = r["y"][0, :N]
+    assert np.abs(y[0, :2] - a1).max() < 1e-6 and np.abs(y[-1, :2] - a2).max() < 1e-6
+    assert r["global_err"][0] <= 1e-6 or (ctl == "hybrid" and r["global_err"][0] <= 2e-6)
+
+
+def test_ho_error_control_needs_mirk_p_plus_2(problems):
+    # __high_order_method (adaptivity.jl:552-555) names MIRK(p+2): no MIRK7 or MIRK8 exists
+    p = problems.LINEAR
+    with pytest.raises(ValueError, match="order"):
+        _solve1(p, n=10, order=5, controller="global", global_method="HO")
