@@ -220,7 +220,7 @@ EXPORTS = ("bvp_default_options", "bvp_create", "bvp_solve_batch", "bvp_solve_ba
            "bvp_mlp_get_params", "bvp_mlp_set_normalization", "bvp_mlp_forward", "bvp_mlp_loss_grad",
            "bvp_mlp_train", "bvp_mlp_forward_device", "bvp_mlp_forward_noalloc", "bvp_resample_guess_device",
            "bvp_mlp_destroy",
-           "bvp_solve_batch_warm",
+           "bvp_solve_batch_warm", "bvp_solve_batch_device_warm",
            "bvp_last_timing", "bvp_get_tuning", "bvp_get_work_order", "bvp_stream", "bvp_last_error",
            "bvp_destroy")
 
@@ -282,6 +282,8 @@ def load_library(path: str | None = None):
     lib.bvp_solve_batch_warm.argtypes = [vp, vp, i32, i32, f32p, i32, f64p, i32p, f64p, f64p,
                                          C.POINTER(Results), i32p]
     lib.bvp_solve_batch_warm.restype = C.c_int
+    lib.bvp_solve_batch_device_warm.argtypes = [vp, vp, i32, vp, i32, vp, vp, vp, i32]
+    lib.bvp_solve_batch_device_warm.restype = C.c_int
     lib.bvp_last_timing.argtypes = [vp, f64p]
     lib.bvp_last_timing.restype = C.c_int
     lib.bvp_get_tuning.argtypes = [vp, i32p]

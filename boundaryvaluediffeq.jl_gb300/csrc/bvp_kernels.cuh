@@ -2211,22 +2211,36 @@ extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_
     };
     for (int q = tid; q < n; q += blockDim.x) atomicAdd(&hist[key_of(q)], 1);
     __syncthreads();
-    if (warp == 0) {
-        constexpr int PER = NB / 32;
+    {
+        // exclusive scan of the histogram by the whole block: each thread a run of NB / 1024
+        // bins, a warp scan of the run sums, then the warps' totals
+        constexpr int PER = NB / 1024;
+        int v[PER];
         int s = 0;
-        for (int k = 0; k < PER; ++k) s += hist[lane * PER + k];
+#pragma unroll
+        for (int k = 0; k < PER; ++k) { v[k] = hist[tid * PER + k]; s += v[k]; }
         int incl = s;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int t = __shfl_up_sync(bvp::FULL, incl, o);
             if (lane >= o) incl += t;
         }
-        int run = incl - s;
-        for (int k = 0; k < PER; ++k) {
-            const int hv = hist[lane * PER + k];
-            hist[lane * PER + k] = run;
-            run += hv;
+        __shared__ int wtot[32];
+        if (lane == 31) wtot[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            int w = wtot[lane], wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(bvp::FULL, wi, o);
+                if (lane >= o) wi += t;
+            }
+            wtot[lane] = wi - w;
         }
+        __syncthreads();
+        int run = wtot[warp] + incl - s;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) { hist[tid * PER + k] = run; run += v[k]; }
     }
     __syncthreads();
     for (int q = tid; q < n; q += blockDim.x) {
@@ -2236,10 +2250,14 @@ extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_
 }
 
 // The work-order autotuner's update after a solve that recorded its instances' times: the
-// mean time per initial-size bucket, blended half and half with the table's earlier value
+// longest time per initial-size bucket, blended half and half with the table's earlier value
 // where the table has one; a bucket without instances takes the value of the nearest measured
 // bucket below it (above it, before the first); the largest value goes to
-// tab[BVP_COST_BUCKETS]. One block.
+// tab[BVP_COST_BUCKETS]. The longest, not the mean: a bucket whose instances mostly need one
+// mesh round but a few need two holds those few among the batch's longest solves, and
+// longest-first scheduling must start them early (on the pendulum batch, 7% of the
+// 64-80-interval meshes take a second round; ordered by the mean they started last and
+// ended 60 us after everything else). One block.
 extern "C" __global__ void __launch_bounds__(1024) bvp_learn_costs(int n, const int* n_init, const float* cost,
                                                                    float* tab, int blend) {
     __shared__ float s_sum[BVP_COST_BUCKETS];
@@ -2249,13 +2267,14 @@ extern "C" __global__ void __launch_bounds__(1024) bvp_learn_costs(int n, const 
     __syncthreads();
     for (int q = tid; q < n; q += blockDim.x) {
         const int b = min(n_init[q] >> 3, BVP_COST_BUCKETS - 1);
-        atomicAdd(&s_sum[b], cost[q]);
+        // non-negative floats order as their bit patterns
+        atomicMax(reinterpret_cast<int*>(&s_sum[b]), __float_as_int(fmaxf(cost[q], 0.0f)));
         atomicAdd(&s_cnt[b], 1);
     }
     __syncthreads();
     for (int b = tid; b < BVP_COST_BUCKETS; b += blockDim.x) {
         if (s_cnt[b] > 0) {
-            const float m = s_sum[b] / float(s_cnt[b]);
+            const float m = s_sum[b];
             s_sum[b] = (blend && tab[b] > 0.0f) ? 0.5f * (tab[b] + m) : m;
         } else {
             s_sum[b] = blend ? tab[b] : 0.0f;

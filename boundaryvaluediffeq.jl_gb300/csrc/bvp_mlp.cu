@@ -233,7 +233,9 @@ constexpr int FR = 32;            // rows per CTA
 constexpr int FWMAX = 256;        // widest layer the fused kernel takes
 constexpr int FLD = FWMAX + 8;    // shared row stride (bf16): conflict-free fragment loads
 constexpr int FLMAX = 8;          // layers
-constexpr int FQ = FWMAX / 8 / 4; // 8-column tiles per warp at the widest layer
+constexpr int FW = 8;              // warps per CTA: each takes every FW-th 8-column tile
+constexpr int FT = FW * 32;        // threads per CTA
+constexpr int FQ = FWMAX / 8 / FW; // 8-column tiles per warp at the widest layer
 
 struct FusedNet {
     int L;
@@ -260,7 +262,7 @@ __global__ void k_build_wt(int L, FusedNet fn, const long long* offW, const bf16
 constexpr int FWLD = FWMAX + 8;   // staged weight row stride (bf16)
 constexpr size_t FUSED_SMEM = size_t(2) * FR * FLD * 2 + size_t(FWMAX) * FWLD * 2;
 
-__global__ void __launch_bounds__(128) k_mlp_forward_fused(const FusedNet fn, int B, const float* __restrict__ x,
+__global__ void __launch_bounds__(FT) k_mlp_forward_fused(const FusedNet fn, int B, const float* __restrict__ x,
                                                            const bf16* __restrict__ wt, const float* __restrict__ p,
                                                            const float* __restrict__ nrm, float* __restrict__ y) {
     extern __shared__ __align__(16) unsigned char fsm[];
@@ -272,7 +274,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_fused(const FusedNet fn, in
     const int w0 = fn.w[0], wL = fn.w[fn.L];
     {
         const int kp = fn.kp[0];
-        for (int e = tid; e < FR * kp; e += 128) {
+        for (int e = tid; e < FR * kp; e += FT) {
             const int r = e / kp, c = e % kp;
             float v = 0.f;
             if (c < w0 && r0 + r < B) v = (x[(long long)(r0 + r) * w0 + c] - nrm[c]) / nrm[w0 + c];
@@ -290,7 +292,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_fused(const FusedNet fn, in
             // at once (rows 16-byte aligned: K is a multiple of 16)
             const bf16* src = wt + fn.offWt[l];
             const int per_row = K / 8;
-            for (int e = tid; e < N * per_row; e += 128) {
+            for (int e = tid; e < N * per_row; e += FT) {
                 const int nn = e / per_row, c = e - nn * per_row;
                 const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(wsm + nn * WLD + c * 8));
                 asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src + size_t(e) * 8));
@@ -318,7 +320,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_fused(const FusedNet fn, in
             }
 #pragma unroll
             for (int q = 0; q < FQ; ++q) {
-                const int j = warp + 4 * q;
+                const int j = warp + FW * q;
                 if (j < ntiles) {
                     const bf16* wr = W + (j * 8 + g) * WLD + k0 + 2 * t;
                     uint32_t bfr[2];
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_fused(const FusedNet fn, in
         const float* sd = nrm + 2 * w0 + wL;
 #pragma unroll
         for (int q = 0; q < FQ; ++q) {
-            const int j = warp + 4 * q;
+            const int j = warp + FW * q;
             if (j >= ntiles) continue;
             const int c = j * 8 + 2 * t;
 #pragma unroll
@@ -466,7 +468,7 @@ void refresh_wt(bvp_mlp* n) {
 // inference on device pointers: the fused kernel when the network fits it, else layer by layer
 void infer(bvp_mlp* n, int B, const float* d_x, float* d_y, cudaStream_t s) {
     if (n->fused) {
-        k_mlp_forward_fused<<<(B + FR - 1) / FR, 128, FUSED_SMEM, s>>>(n->fn, B, d_x, n->d_wt, n->d_p, n->d_norm, d_y);
+        k_mlp_forward_fused<<<(B + FR - 1) / FR, FT, FUSED_SMEM, s>>>(n->fn, B, d_x, n->d_wt, n->d_p, n->d_norm, d_y);
     } else {
         cudaStream_t prev = n->stream;
         n->stream = s;

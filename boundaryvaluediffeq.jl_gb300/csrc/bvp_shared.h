@@ -92,8 +92,8 @@ struct BvpArgs {
     int* pause_count;              //   at *pause_count
 };
 
-// Work-order cost table of the fused solve: the mean solve time of the instances whose initial
-// interval count falls in each bucket (n_init >> 3), learned from a handle's first solves.
+// Work-order cost table of the fused solve: the longest solve time of the instances whose
+// initial interval count falls in each bucket (n_init >> 3), learned from a handle's first solves.
 #define BVP_COST_BUCKETS 512
 
 // Launch arguments of the larger-state kernels (M > 8, bvp_large.cuh): one instance per CTA or

@@ -71,6 +71,10 @@ struct bvp_handle_s {
     DevBuf d_gerr, d_K_hi, d_pause;
     HostBuf h_pause;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    // the surrogate's forward of a warm solve runs on a second stream, beside the solve's
+    // per-batch setup; the fused kernel waits for it on ev_side
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_side = nullptr;
     // larger-state path (M > 8, bvp_large.cuh)
     bool large = false;
     cudaKernel_t kl_res = nullptr, kl_jac = nullptr, kl_solve = nullptr, kl_update = nullptr, kl_copy = nullptr,
@@ -351,6 +355,9 @@ bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bv
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaEventCreate(&h->ev[k]);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_in, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_side, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         h->err = std::string("CUDA init: ") + cudaGetErrorString(e);
         *out = h;
@@ -592,7 +599,7 @@ static bvp_status ho_rounds(bvp_handle* h, const BvpArgs& a0, int n) {
 static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode, const double* d_params,
                                const int* d_n_init, const double* d_tspans, const double* d_y0,
                                const long long* d_y0_off, const float* d_grid = nullptr, int n_grid = 0,
-                               long long host_pts = 0) {
+                               long long host_pts = 0, bool wait_side = false) {
     BvpArgs a;
     fill_args(h, a, n, tot, y0_mode, d_params, d_n_init, d_tspans, d_y0, d_y0_off);
     a.y0_grid = d_grid;
@@ -634,6 +641,7 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
         void* args[] = {&nn, &ni, &ms, &cs, &cap, &off, &ord, &ctr, &tab};
         CU(cudaLaunchKernel((const void*)h->k_prep, dim3(1), dim3(1024), args, 0, h->stream));
     }
+    if (wait_side) CU(cudaStreamWaitEvent(h->stream, h->ev_side, 0));   // the guesses on the grid
     CU(cudaEventRecord(h->ev[1], h->stream));
     if (h->ho) CU(cudaMemsetAsync(a.pause_count, 0, 2 * sizeof(int), h->stream));
     {
@@ -1469,6 +1477,40 @@ bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const
     return finish_host(h, out);
 }
 
+// The surrogate's forward into the handle's grid buffer on the side stream, once the work
+// enqueued so far on the handle's stream (the inputs' copies) is done; ev_side marks its end.
+static bvp_status side_forward(bvp_handle* h, bvp_mlp* net, int n, const float* d_features) {
+    CU(cudaEventRecord(h->ev_in, h->stream));
+    CU(cudaStreamWaitEvent(h->side, h->ev_in, 0));
+    if (bvp_mlp_forward_device(net, n, d_features, static_cast<float*>(h->d_grid.p), h->side) != BVP_OK)
+        return fail(h, BVP_ERR_CUDA, "surrogate forward failed");
+    CU(cudaEventRecord(h->ev_side, h->side));
+    return BVP_OK;
+}
+
+bvp_status bvp_solve_batch_device_warm(bvp_handle* h, bvp_mlp* net, int32_t n, const float* d_features,
+                                       int32_t n_grid, const double* d_params, const int32_t* d_n_intervals,
+                                       const double* d_tspans, int32_t max_intervals) {
+    if (!h) return BVP_ERR_INVALID;
+    if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: only bvp_solve_batch is available");
+    if (!net || n < 1 || !d_features || n_grid < 2 || !d_n_intervals || !d_tspans || max_intervals < 1 ||
+        (h->desc.n_params > 0 && !d_params))
+        return fail(h, BVP_ERR_INVALID, "invalid arguments");
+    const long long tot = (long long)n * cap_nodes(h, max_intervals);
+    bvp_status s = ensure_arena(h, tot, n, 1);
+    if (s != BVP_OK) return s;
+    if (!ensure_dev(h->d_grid, size_t(n) * n_grid * h->L.M * 4)) return fail(h, BVP_ERR_NOMEM, "device allocation failed");
+    s = side_forward(h, net, n, d_features);
+    if (s != BVP_OK) return s;
+    s = launch_solve(h, n, tot, 2, d_params, d_n_intervals, d_tspans, static_cast<const double*>(h->d_y0.p),
+                     static_cast<const long long*>(h->d_y0_off.p), static_cast<const float*>(h->d_grid.p), n_grid, 0,
+                     true);
+    if (s != BVP_OK) return s;
+    h->pending_device = true;
+    h->have_results = false;
+    return BVP_OK;
+}
+
 bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t n_features, const float* features,
                                 int32_t n_grid, const double* params, const int32_t* n_intervals,
                                 const double* tspans, const double* y0_plain, bvp_results* out,
@@ -1508,14 +1550,13 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
     CU(cudaMemcpyAsync(h->d_tspans.p, hp + b_params, b_ts, cudaMemcpyHostToDevice, h->stream));
     CU(cudaMemcpyAsync(h->d_n_init.p, hp + b_params + b_ts, b_ni, cudaMemcpyHostToDevice, h->stream));
     CU(cudaMemcpyAsync(h->d_feat.p, hp + b_params + b_ts + b_ni, b_feat, cudaMemcpyHostToDevice, h->stream));
-    if (bvp_mlp_forward_device(net, n, static_cast<const float*>(h->d_feat.p), static_cast<float*>(h->d_grid.p),
-                               h->stream) != BVP_OK)
-        return fail(h, BVP_ERR_CUDA, "surrogate forward failed");
+    s = side_forward(h, net, n, static_cast<const float*>(h->d_feat.p));
+    if (s != BVP_OK) return s;
     // the solve resamples the grid guesses onto the initial meshes itself (y0_mode 2)
     s = launch_solve(h, n, tot, 2, static_cast<const double*>(h->d_params.p), static_cast<const int*>(h->d_n_init.p),
                      static_cast<const double*>(h->d_tspans.p), static_cast<const double*>(h->d_y0.p),
                      static_cast<const long long*>(h->d_y0_off.p), static_cast<const float*>(h->d_grid.p), n_grid,
-                     pts);
+                     pts, true);
     if (s != BVP_OK) return s;
     s = finish_host(h, nullptr);
     if (s != BVP_OK) return s;
@@ -1838,6 +1879,9 @@ void bvp_destroy(bvp_handle* h) {
         if (b->p) cudaFreeHost(b->p);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
+    if (h->ev_in) cudaEventDestroy(h->ev_in);
+    if (h->ev_side) cudaEventDestroy(h->ev_side);
+    if (h->side) cudaStreamDestroy(h->side);
     if (h->lib) cudaLibraryUnload(h->lib);
     if (h->lib_hi) cudaLibraryUnload(h->lib_hi);
     if (h->stream) cudaStreamDestroy(h->stream);

@@ -202,6 +202,20 @@ class BatchSolver:
         self._check(st, "bvp_solve_batch_device")
         self._pending_n = n
 
+    def solve_device_warm(self, net, d_features, n_grid, d_params, d_n_intervals, d_tspans, max_intervals):
+        """Surrogate-warm solve on device inputs (bvp_solve_batch_device_warm): the network's
+        forward on a second stream beside the solve's setup; returns without synchronising and
+        without the plain-guess fallback."""
+        def ptr(x):
+            if x is None:
+                return None
+            return C.c_void_p(x.data_ptr() if hasattr(x, "data_ptr") else int(x))
+        n = int(d_n_intervals.numel() if hasattr(d_n_intervals, "numel") else len(d_n_intervals))
+        st = self.lib.bvp_solve_batch_device_warm(self.h, net.h, n, ptr(d_features), int(n_grid), ptr(d_params),
+                                                  ptr(d_n_intervals), ptr(d_tspans), int(max_intervals))
+        self._check(st, "bvp_solve_batch_device_warm")
+        self._pending_n = n
+
     def solve_device_grid(self, d_params, d_n_intervals, d_tspans, d_grid, n_grid, max_intervals):
         """solve_device with the initial guesses on uniform n_grid-point grids (FP32 device
         array n_inst x n_grid x M), resampled onto the initial meshes inside the solve."""
@@ -241,7 +255,7 @@ class BatchSolver:
 
     def work_order(self):
         """(learned, costs): whether the fused solve's work order comes from the handle's learned
-        cost table, and the table (mean solve time per initial-size bucket of 8 intervals, the
+        cost table, and the table (longest solve time per initial-size bucket of 8 intervals, the
         maximum last)."""
         learned = np.zeros(1, np.int32)
         costs = np.zeros(513, np.float32)

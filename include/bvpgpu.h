@@ -255,6 +255,15 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n_inst, int
                                 const int32_t* n_intervals, const double* tspans,
                                 const double* y0_plain, bvp_results* out, int32_t* n_fallback);
 
+/* bvp_solve_batch_warm's solve on inputs already in device memory (d_features: n_inst x the
+ * network's input width, FP32): the network's forward writes the grid guesses on a second
+ * stream beside the solve's per-batch setup, and the solve waits for it. No plain-guess
+ * fallback (the caller reads the retcodes with bvp_fetch_results and re-solves with
+ * bvp_solve_batch_device); returns without synchronising. */
+bvp_status bvp_solve_batch_device_warm(bvp_handle* h, bvp_mlp* net, int32_t n_inst, const float* d_features,
+                                       int32_t n_grid, const double* d_params, const int32_t* d_n_intervals,
+                                       const double* d_tspans, int32_t max_intervals);
+
 /* Device time of the last solve's kernels in milliseconds (CUDA events on the handle's
  * stream): [0] whole solve, [1] fused solve kernel. */
 bvp_status bvp_last_timing(bvp_handle* h, double* ms2);
@@ -267,7 +276,7 @@ bvp_status bvp_get_tuning(bvp_handle* h, int32_t* threads);
 /* The fused solve's work order (no reference counterpart: the reference solves one problem at
  * a time). One warp carries one instance, so a batch ends when its slowest instances end; the
  * handle's first three solves of at least 256 instances record every instance's solve time
- * and fold it into a table of mean times per initial-size bucket (initial intervals / 8, 512
+ * and fold it into a table of the longest time per initial-size bucket (initial intervals / 8, 512
  * buckets), and later solves start the instances the table predicts to be longest first
  * (before any table: coarsest initial mesh first). The order changes no result. *learned: 1
  * once the table exists; costs (if not NULL): the first n_costs of the 512 bucket costs and,

@@ -103,6 +103,18 @@ def test_surrogate_warm_start_cuts_newton_iterations(pkg, problems):
     assert (dev.newton_iters == warm.result.newton_iters).all()
     for i in range(len(tn)):
         assert np.array_equal(dev.solution(i)[1], warm.result.solution(i)[1])
+    # and on device inputs (bvp_solve_batch_device_warm: the forward on the handle's second
+    # stream beside the solve's setup): the same warm results before any fallback
+    import torch
+    sv2 = pkg.BatchSolver(p, order=4)
+    sv2.solve_device_warm(sur.net, torch.tensor(tp.astype(np.float32), device="cuda"), sur.grid,
+                          torch.tensor(tp, device="cuda"), torch.tensor(tn, device="cuda"),
+                          torch.tensor(tt, device="cuda"), int(tn.max()))
+    dw = sv2.fetch()
+    ok = dw.retcode == RET_SUCCESS
+    assert ok.sum() == len(tn) - nfb
+    for i in np.nonzero(ok)[0][::7]:
+        assert np.array_equal(dw.solution(i)[1], dev.solution(i)[1])
     # both are solutions of the same discretisation to the same tolerance
     o = Oracle(p.source, p.M, p.n_params, bc_t=p.bc_t)
     for i in range(0, 1024, 37):
