@@ -1955,35 +1955,42 @@ constexpr int SM_ISCRW = SCR_SMEM ? ISCRW : 1;
 constexpr int SM_DNS = SMEM_DENSE ? NDENSE * DLD : 1;
 constexpr bool TREC_SMEM = WARPS_PER_BLOCK * TREE_SLOTS * RECW * int(sizeof(JT)) <= 16 * 1024;
 constexpr int SM_TREC = TREC_SMEM ? TREE_SLOTS * RECW : 1;
-}  // namespace bvp
 
-// Persistent fused solve: each warp repeatedly takes the next instance from the work
-// counter and runs its complete adaptive solve.
-extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::Args a) {
-    __shared__ double s_scr[bvp::WARPS_PER_BLOCK][bvp::SM_SCRW];
-    __shared__ int s_iscr[bvp::WARPS_PER_BLOCK][bvp::SM_ISCRW];
-    __shared__ bvp::JT s_dns[bvp::WARPS_PER_BLOCK][bvp::SM_DNS];
-    __shared__ bvp::JT s_trec[bvp::WARPS_PER_BLOCK][bvp::SM_TREC];
-    const int lane = bvp::lane_id();
+BVP_DEV void fused_body(const Args& a) {
+    __shared__ double s_scr[WARPS_PER_BLOCK][SM_SCRW];
+    __shared__ int s_iscr[WARPS_PER_BLOCK][SM_ISCRW];
+    __shared__ JT s_dns[WARPS_PER_BLOCK][SM_DNS];
+    __shared__ JT s_trec[WARPS_PER_BLOCK][SM_TREC];
+    const int lane = lane_id();
     const int w = threadIdx.x >> 5;
     while (true) {
         int k = 0;
         if (lane == 0) k = atomicAdd(a.work_counter, 1);
-        k = __shfl_sync(bvp::FULL, k, 0);
+        k = __shfl_sync(FULL, k, 0);
         if (k >= a.n_inst) break;
-        bvp::Inst I = bvp::make_inst(a, a.order[k]);
-        if (bvp::SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
+        Inst I = make_inst(a, a.order[k]);
+        if (SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
         I.dns = s_dns[w];
-        if (bvp::TREC_SMEM) I.trec = s_trec[w];
-        if (bvp::GLOBAL_CTL && a.phase == 2) {
-            bvp::polish_instance(a, I);
+        if (TREC_SMEM) I.trec = s_trec[w];
+        if (GLOBAL_CTL && a.phase == 2) {
+            polish_instance(a, I);
             continue;
         }
         const long long c0 = a.inst_cost ? clock64() : 0;
-        bvp::solve_instance(a, I);
+        solve_instance(a, I);
         if (a.inst_cost && lane == 0) a.inst_cost[I.q] = float(clock64() - c0) * (1.0f / 2000.0f);
     }
 }
+}  // namespace bvp
+
+// The same kernel for three register budgets: 4, 3 or 2 resident blocks of 4 warps per SM
+// (128, 168 and 255 registers per thread at most). More resident warps hide more latency;
+// fewer leave each warp the registers its solve needs without spilling (the pendulum's MIRK4
+// solve takes 156: 198 bytes of spills per thread at 4 blocks, none at 3). The handle's
+// autotuner picks one by timing them on its own batches.
+extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::Args a) { bvp::fused_body(a); }
+extern "C" __global__ void __launch_bounds__(128, 3) bvp_solve_fused_b3(const bvp::Args a) { bvp::fused_body(a); }
+extern "C" __global__ void __launch_bounds__(128, 2) bvp_solve_fused_b2(const bvp::Args a) { bvp::fused_body(a); }
 
 // Stage kernels on caller-provided (mesh, y) in buffer 0 with N = st[q].N. Used by the
 // per-kernel parity tests; stage: 0 residual (F, K, BC residual), 1 Jacobian blocks,

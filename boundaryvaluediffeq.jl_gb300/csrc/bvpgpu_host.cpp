@@ -61,6 +61,18 @@ struct bvp_handle_s {
     DevBuf d_inst_cost, d_cost_tab;
     int learn_left = 3;
     bool have_tab = false;
+    // launch-shape autotuner of the fused solve: the kernel built for 4, 3 and 2 resident
+    // blocks per SM; once the work order is learned, the next solves of one batch shape rotate
+    // through the three (two timed solves each) and the handle keeps the fastest
+    cudaKernel_t k_fused_v[3] = {nullptr, nullptr, nullptr};
+    int fused_pick = 1;
+    struct {
+        long long key = -1;
+        int pending = -1, next = 0;
+        float sum[3] = {0, 0, 0};
+        int cnt[3] = {0, 0, 0};
+        bool done = false;
+    } tune;
     // error controllers other than DefectControl (fused path): the global estimates per interval,
     // and for HOErrorControl the module compiled for MIRK(p+2), its stage array, the two lists
     // of instances waiting for its solve and their counts (pinned for the host's loop)
@@ -295,6 +307,9 @@ static bvp_status compile_and_load(bvp_handle* h) {
         return BVP_OK;
     }
     CU(cudaLibraryGetKernel(&h->k_fused, h->lib, "bvp_solve_fused"));
+    CU(cudaLibraryGetKernel(&h->k_fused_v[1], h->lib, "bvp_solve_fused_b3"));
+    CU(cudaLibraryGetKernel(&h->k_fused_v[2], h->lib, "bvp_solve_fused_b2"));
+    h->k_fused_v[0] = h->k_fused;
     CU(cudaLibraryGetKernel(&h->k_stage, h->lib, "bvp_stage"));
     CU(cudaLibraryGetKernel(&h->k_pack, h->lib, "bvp_pack"));
     CU(cudaLibraryGetKernel(&h->k_offsets, h->lib, "bvp_out_offsets"));
@@ -549,6 +564,44 @@ static int fused_grid(bvp_handle* h, int n) {
 static bvp_status prepare_host_outputs(bvp_handle* h, int n, long long pts_guess, BvpArgs& a);
 
 static constexpr int kLearnMin = 256;   // smallest batch the work-order autotuner learns from
+static constexpr int kFusedBlocks[3] = {4, 3, 2};   // resident blocks per SM of the fused variants
+
+// The fused variant for the next launch. Folds the previous launch's kernel time into the
+// launch-shape tuner when that launch ran a candidate and has completed; candidates are
+// compared on one batch shape (instance count, guess form) after the work order is learned.
+static int fused_variant(bvp_handle* h, int n, int y0_mode) {
+    auto& t = h->tune;
+    if (t.done || h->ho) return h->fused_pick;
+    if (t.pending >= 0) {
+        float ms = 0.0f;
+        if (cudaEventQuery(h->ev[2]) == cudaSuccess && cudaEventElapsedTime(&ms, h->ev[1], h->ev[2]) == cudaSuccess) {
+            t.sum[t.pending] += ms;
+            ++t.cnt[t.pending];
+        } else {
+            (void)cudaGetLastError();   // not ready: that sample is dropped
+        }
+        t.pending = -1;
+    }
+    if (n < kLearnMin || h->learn_left > 0) return h->fused_pick;
+    const long long key = (long long)n * 4 + y0_mode;
+    if (key != t.key) {
+        t.key = key;
+        t.next = 0;
+        for (int c = 0; c < 3; ++c) { t.sum[c] = 0.0f; t.cnt[c] = 0; }
+    }
+    if (t.cnt[0] >= 2 && t.cnt[1] >= 2 && t.cnt[2] >= 2) {
+        int best = 0;
+        for (int c = 1; c < 3; ++c)
+            if (t.sum[c] / t.cnt[c] < t.sum[best] / t.cnt[best]) best = c;
+        h->fused_pick = best;
+        t.done = true;
+        return best;
+    }
+    const int c = t.next;
+    t.next = (t.next + 1) % 3;
+    t.pending = c;
+    return c;
+}
 
 // HOErrorControl: instances stop after each round's Newton solve (and defect) and wait in a list
 // for their MIRK(p+2) solve on the same mesh, which the module of that order runs (phase 2, its
@@ -589,7 +642,8 @@ static bvp_status ho_rounds(bvp_handle* h, const BvpArgs& a0, int n) {
         CU(cudaMemsetAsync(a1.pause_count, 0, sizeof(int), h->stream));
         {
             void* args[] = {&a1};
-            CU(cudaLaunchKernel((const void*)h->k_fused, dim3(fused_grid(h, c)), dim3(128), args, 0, h->stream));
+            CU(cudaLaunchKernel((const void*)h->k_fused_v[h->fused_pick], dim3(fused_grid(h, c)), dim3(128), args, 0,
+                                h->stream));
         }
         cur ^= 1;
     }
@@ -642,11 +696,12 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
         CU(cudaLaunchKernel((const void*)h->k_prep, dim3(1), dim3(1024), args, 0, h->stream));
     }
     if (wait_side) CU(cudaStreamWaitEvent(h->stream, h->ev_side, 0));   // the guesses on the grid
+    const int var = fused_variant(h, n, y0_mode);
     CU(cudaEventRecord(h->ev[1], h->stream));
     if (h->ho) CU(cudaMemsetAsync(a.pause_count, 0, 2 * sizeof(int), h->stream));
     {
         void* args[] = {&a};
-        CU(cudaLaunchKernel((const void*)h->k_fused, dim3(fused_grid(h, n)), dim3(128), args, 0, h->stream));
+        CU(cudaLaunchKernel((const void*)h->k_fused_v[var], dim3(fused_grid(h, n)), dim3(128), args, 0, h->stream));
     }
     if (h->ho) {
         bvp_status s = ho_rounds(h, a, n);
@@ -1724,6 +1779,15 @@ bvp_status bvp_dense_output(bvp_handle* h, int32_t nq, const double* tq, int32_t
 bvp_status bvp_get_tuning(bvp_handle* h, int32_t* threads) {
     if (!h || !threads) return BVP_ERR_INVALID;
     threads[0] = (h->large && h->l_tuned) ? h->l_threads : 0;
+    return BVP_OK;
+}
+
+bvp_status bvp_get_fused_tuning(bvp_handle* h, int32_t* blocks_per_sm, int32_t* tuned, float* ms) {
+    if (!h || !blocks_per_sm) return BVP_ERR_INVALID;
+    *blocks_per_sm = h->large ? 0 : kFusedBlocks[h->fused_pick];
+    if (tuned) *tuned = h->tune.done ? 1 : 0;
+    if (ms)
+        for (int c = 0; c < 3; ++c) ms[c] = h->tune.cnt[c] > 0 ? h->tune.sum[c] / h->tune.cnt[c] : 0.0f;
     return BVP_OK;
 }
 

@@ -251,7 +251,12 @@ class BatchSolver:
         """Launch shapes the library's autotuner picked for this handle."""
         t = np.zeros(1, np.int32)
         self._check(self.lib.bvp_get_tuning(self.h, i32(t)), "bvp_get_tuning")
-        return {"linsolve_threads": int(t[0])}
+        b, done = np.zeros(1, np.int32), np.zeros(1, np.int32)
+        ms = np.zeros(3, np.float32)
+        self._check(self.lib.bvp_get_fused_tuning(self.h, i32(b), i32(done), ms.ctypes.data_as(C.POINTER(C.c_float))),
+                    "bvp_get_fused_tuning")
+        return {"linsolve_threads": int(t[0]), "fused_blocks_per_sm": int(b[0]), "fused_tuned": bool(done[0]),
+                "fused_ms_by_blocks": {4: float(ms[0]), 3: float(ms[1]), 2: float(ms[2])}}
 
     def work_order(self):
         """(learned, costs): whether the fused solve's work order comes from the handle's learned
