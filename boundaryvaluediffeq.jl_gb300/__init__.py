@@ -12,3 +12,6 @@ from . import sciml  # noqa: F401
 from .sciml import solve, EnsembleProblem, MIRK2, MIRK3, MIRK4, MIRK5, MIRK6, MIRK6I  # noqa: F401
 from .sciml import (DefectControl, GlobalErrorControl, SequentialErrorControl, HybridErrorControl,  # noqa: F401
                     HOErrorControl, REErrorControl)
+from .sciml import (FIRK, RadauIIa1, RadauIIa2, RadauIIa3, RadauIIa5, RadauIIa7, LobattoIIIa2,  # noqa: F401
+                    LobattoIIIa3, LobattoIIIa4, LobattoIIIa5, LobattoIIIb2, LobattoIIIb3, LobattoIIIb4, LobattoIIIb5,
+                    LobattoIIIc2, LobattoIIIc3, LobattoIIIc4, LobattoIIIc5)

@@ -21,7 +21,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD = os.path.join(PKG_DIR, "_build")
 INCLUDE = os.path.join(os.path.dirname(PKG_DIR), "include")
 LIB_PATH = os.path.join(BUILD, "libbvpgpu.so")
-EMBED = ("bvp_prelude.cuh", "bvp_kernels.cuh", "bvp_large.cuh", "bvp_shared.h", "bvp_tableau.cuh")
+EMBED = ("bvp_prelude.cuh", "bvp_kernels.cuh", "bvp_large.cuh", "bvp_shared.h", "bvp_tableau.cuh", "bvp_firk.cuh")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
@@ -86,16 +86,27 @@ def _nvrtc():
     return None
 
 
-def nvrtc_check(problem, order: int, jac_bits: int = 32, mirk6i: int = 0, global_ctl: int = 0) -> None:
+def nvrtc_check(problem, order: int, jac_bits: int = 32, mirk6i: int = 0, global_ctl: int = 0,
+                firk_stages: int = 0) -> None:
     """Compile the problem's kernels with NVRTC exactly as bvp_create does (same source
     assembly and options, no GPU needed; global_ctl: the build with the error controllers other
-    than DefectControl); raises with the NVRTC log on failure."""
+    than DefectControl; firk_stages: the FIRK path's build for that many stages, with
+    placeholder coefficients); raises with the NVRTC log on failure."""
     lib = _nvrtc()
     if lib is None:
         return
     large = problem.M > 8
     nbc = 2 if problem.twopoint else len(problem.bc_t)
-    src = ("#include \"bvp_prelude.cuh\"\n#line 1 \"problem_source\"\n" + problem.source +
+    prefix = ""
+    if firk_stages:
+        s = firk_stages
+        row = "{" + ", ".join(["0.5"] * s) + "}"
+        prefix = ("#define BVP_FIRK 1\nnamespace bvp {\n"
+                  f"constexpr int FS = {s}, FORDER = {2 * s - 1};\nconstexpr double FTAU = 0.0;\n"
+                  f"constexpr double FC[{s}] = {row};\nconstexpr double FB[{s}] = {row};\n"
+                  f"constexpr double FA[{s}][{s}] = {{{', '.join([row] * s)}}};\n"
+                  f"constexpr double FQ[{s}][{s}] = {{{', '.join([row] * s)}}};\n}}\n")
+    src = ("#include \"bvp_prelude.cuh\"\n" + prefix + "#line 1 \"problem_source\"\n" + problem.source +
            ("\n#include \"bvp_large.cuh\"\n" if large else "\n#include \"bvp_kernels.cuh\"\n"))
     opts = ["--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true", f"-DBVP_M={problem.M}",
             f"-DBVP_ORDER={order}", f"-DBVP_TWOPOINT={int(problem.twopoint)}", f"-DBVP_NBC={nbc}",
@@ -198,12 +209,15 @@ class Options(C.Structure):
                 ("fp32_phase", C.c_int32), ("abstol", C.c_double), ("defect_threshold", C.c_double),
                 ("divergence_factor", C.c_double), ("mirk6i", C.c_int32),
                 ("controller", C.c_int32), ("global_method", C.c_int32),
-                ("hybrid_de", C.c_double), ("hybrid_ge", C.c_double)]
+                ("hybrid_de", C.c_double), ("hybrid_ge", C.c_double),
+                ("firk", C.c_int32), ("firk_stages", C.c_int32)]
 
 
 # bvp_controller and bvp_global_method
 CONTROLLERS = {"defect": 0, "global": 1, "sequential": 2, "hybrid": 3}
 GLOBAL_METHODS = {"HO": 0, "RE": 1}
+# bvp_options.firk
+FIRK_FAMILIES = {"RadauIIa": 1, "LobattoIIIa": 2, "LobattoIIIb": 3, "LobattoIIIc": 4}
 
 
 class Results(C.Structure):

@@ -80,6 +80,17 @@ constexpr bool GLOBAL_CTL = BVP_GLOBAL_CTL != 0;
 enum : int { CTL_DEFECT = 0, CTL_GLOBAL = 1, CTL_SEQUENTIAL = 2, CTL_HYBRID = 3 };
 enum : int { GLOBAL_HO = 0, GLOBAL_RE = 1 };
 
+// FIRK (expanded Radau IIA / Lobatto collocation, bvp_firk.cuh): the host prepends the scheme's
+// coefficients (FS stages, order FORDER, c, b, a, q_coeff and τ*) and defines BVP_FIRK
+#ifndef BVP_FIRK
+#define BVP_FIRK 0
+constexpr int FS = 1, FORDER = 1;
+constexpr double FTAU = 0.0, FC[1] = {1.0}, FB[1] = {1.0}, FA[1][1] = {{1.0}}, FQ[1][1] = {{1.0}};
+#endif
+constexpr bool FIRK = BVP_FIRK != 0;
+constexpr int FN = FS * M;          // stage unknowns of an interval
+constexpr int FXW = FN * (M + 1);   // its condensation record: J_K^-1 [J_y | R]
+
 // ---- launch arguments (shared with the host runtime) ------------------------------------
 using InstState = BvpInstState;
 using Args = BvpArgs;
@@ -233,7 +244,7 @@ template <class T, class PT> BVP_DEV void call_stage_f(T* du, const T* u, const 
 // terms): K_1 of interval i is f(y_i, t_i) and K_2 is f(y_{i+1}, t_{i+1}), which is K_1 of
 // interval i+1. The residual evaluates each node once and shares it between neighbours
 // (the reference evaluates it twice, collocation.jl:60-66).
-constexpr bool NODE_SHARE = S >= 2 && ORD >= 4;
+constexpr bool NODE_SHARE = !FIRK && S >= 2 && ORD >= 4;
 
 // ---- Φ for one interval (collocation.jl:44-72) ------------------------------------------
 // With `node` non-null and NODE_SHARE, stage 0 is taken from node[] (f at the left node)
@@ -408,6 +419,55 @@ BVP_DEV void mesh_setup(const Args& a, const Inst& I) {
 // Newton iterations of the mixed-precision path (writes only the FP32 right-hand side).
 // Each lane owns a contiguous block of intervals so node stages pass between neighbours
 // in registers. Lane 0 then evaluates the BCs and caches u at the BC points.
+// The BC rows on lane 0: u at the BC points (interior ones as the interval loop cached them,
+// endpoints from the nodes) cached for the Jacobian, the BC residual into the scratch; returns
+// its largest magnitude and flags a non-finite entry in bad.
+template <class R>
+BVP_DEV double bc_rows_lane0(const Args& a, const Inst& I, const R* pr, bool& bad) {
+    double mx = 0.0;
+    R res[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) res[m] = R(0);
+    double* ua_c = I.scr + SCR_UA;
+    if (TWOPOINT) {
+        R ya[M], yb[M], ra[M], rb[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) { ya[m] = y_at<R>(a, I, m); yb[m] = y_at<R>(a, I, (I.N - 1) * M + m); }
+        bvp_bca<R, R>(ra, ya, pr);
+        bvp_bcb<R, R>(rb, yb, pr);
+        for (int k = 0; k < LA; ++k) res[k] = ra[k];
+        for (int k = LA; k < M; ++k) res[k] = rb[k - LA];
+        for (int m = 0; m < M; ++m) { ua_c[m] = double(ya[m]); ua_c[M + m] = double(yb[m]); }
+    } else {
+        R ua[NBC * M];
+        const R* ptrs[NBC];
+#pragma unroll
+        for (int k = 0; k < NBC; ++k) {
+            if (I.iscr[ISCR_UIN + k]) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) ua[k * M + m] = R(ua_c[k * M + m]);
+            } else {
+                // exact endpoints: EvalSol returns y_1 / y_N
+                const int nd = I.iscr[ISCR_UNODE + k];
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    ua[k * M + m] = y_at<R>(a, I, nd * M + m);
+                    ua_c[k * M + m] = double(ua[k * M + m]);
+                }
+            }
+            ptrs[k] = &ua[k * M];
+        }
+        bvp_bc<R, R>(res, ptrs, pr);
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        I.scr[SCR_BCRES + m] = double(res[m]);
+        bad |= !isfinite(res[m]);
+        mx = fmax(mx, fabs(double(res[m])));
+    }
+    return mx;
+}
+
 template <class R = double>
 BVP_DEV double residual(const Args& a, const Inst& I) {
     const int lane = lane_id();
@@ -479,48 +539,7 @@ BVP_DEV double residual(const Args& a, const Inst& I) {
     }
     mx = double(mxr);
     __syncwarp();
-    if (lane == 0) {
-        R res[M];
-#pragma unroll
-        for (int m = 0; m < M; ++m) res[m] = R(0);
-        double* ua_c = I.scr + SCR_UA;
-        if (TWOPOINT) {
-            R ya[M], yb[M], ra[M], rb[M];
-#pragma unroll
-            for (int m = 0; m < M; ++m) { ya[m] = y_at<R>(a, I, m); yb[m] = y_at<R>(a, I, (I.N - 1) * M + m); }
-            bvp_bca<R, R>(ra, ya, pr);
-            bvp_bcb<R, R>(rb, yb, pr);
-            for (int k = 0; k < LA; ++k) res[k] = ra[k];
-            for (int k = LA; k < M; ++k) res[k] = rb[k - LA];
-            for (int m = 0; m < M; ++m) { ua_c[m] = double(ya[m]); ua_c[M + m] = double(yb[m]); }
-        } else {
-            R ua[NBC * M];
-            const R* ptrs[NBC];
-#pragma unroll
-            for (int k = 0; k < NBC; ++k) {
-                if (I.iscr[ISCR_UIN + k]) {
-#pragma unroll
-                    for (int m = 0; m < M; ++m) ua[k * M + m] = R(ua_c[k * M + m]);
-                } else {
-                    // exact endpoints: EvalSol returns y_1 / y_N
-                    const int nd = I.iscr[ISCR_UNODE + k];
-#pragma unroll
-                    for (int m = 0; m < M; ++m) {
-                        ua[k * M + m] = y_at<R>(a, I, nd * M + m);
-                        ua_c[k * M + m] = double(ua[k * M + m]);
-                    }
-                }
-                ptrs[k] = &ua[k * M];
-            }
-            bvp_bc<R, R>(res, ptrs, pr);
-        }
-#pragma unroll
-        for (int m = 0; m < M; ++m) {
-            I.scr[SCR_BCRES + m] = double(res[m]);
-            bad |= !isfinite(res[m]);
-            mx = fmax(mx, fabs(double(res[m])));
-        }
-    }
+    if (lane == 0) mx = fmax(mx, bc_rows_lane0<R>(a, I, pr, bad));
     __syncwarp();
     mx = warp_max(mx);
     bad = warp_any(bad);
@@ -958,6 +977,103 @@ BVP_DEV void block_jacobian(const JT* yj, const JT* tj, const JT* hj, const JT* 
         }
 }
 
+#if BVP_FIRK
+// FIRK interval c, linearised at the current nodes and stages: the stage equations
+// R_r = f(Y_r, t_r) - K_r with Y_r = y_c + h sum_j a_rj K_j have J_K = h a_rj J_f(Y_r) - δ_rj I
+// and J_y = J_f(Y_r); X = J_K^-1 [J_y | R] (an FN x FN elimination with partial pivoting, kept
+// in a.fx for the stage update) eliminates the stage unknowns from the continuity row
+// C = y_{c+1} - y_c - h sum_j b_j K_j, leaving the node relation of the structured solve:
+// S = h sum_j b_j X_y,j - I, R = I, right-hand side -(C + h sum_j b_j X_r,j).
+BVP_DEV bool firk_block(const Args& a, const Inst& I, int c, double* Sr, double* Rr, double* gr) {
+    using DU = Dual<double, M>;
+    const double* mesh = mesh_of(a, I, I.cur);
+    const double* hv = h_of(a, I, I.cur);
+    const double* y = y_of(a, I, I.cur);
+    const double* Kc = a.K + (I.nb + c) * FN;
+    const double hc = hv[c];
+    double JK[FN * FN];
+    double X[FXW];
+#pragma unroll
+    for (int q = 0; q < FN * FN; ++q) JK[q] = 0.0;
+#pragma unroll 1
+    for (int r = 0; r < FS; ++r) {
+        DU Y[M], fy[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            double acc = y[c * M + m];
+#pragma unroll
+            for (int j = 0; j < FS; ++j) acc += hc * (Kc[j * M + m] * FA[r][j]);
+            Y[m] = DU(acc);
+            Y[m].d[m] = 1.0;
+        }
+        bvp_f<DU, double>(fy, Y, I.p, mesh[c] + FC[r] * hc);
+#pragma unroll
+        for (int q = 0; q < M; ++q) {
+            const int row = r * M + q;
+#pragma unroll
+            for (int cc = 0; cc < M; ++cc) {
+                const double J = fy[q].d[cc];
+                X[row * (M + 1) + cc] = J;
+#pragma unroll
+                for (int j = 0; j < FS; ++j) JK[row * FN + j * M + cc] = hc * FA[r][j] * J;
+            }
+            JK[row * FN + row] -= 1.0;
+            X[row * (M + 1) + M] = fy[q].v - Kc[r * M + q];
+        }
+    }
+    // elimination with partial pivoting on JK, applied to the M + 1 columns of X
+    bool ok = true;
+#pragma unroll 1
+    for (int k = 0; k < FN; ++k) {
+        int p = k;
+        for (int r = k + 1; r < FN; ++r)
+            if (fabs(JK[r * FN + k]) > fabs(JK[p * FN + k])) p = r;
+        if (JK[p * FN + k] == 0.0) { ok = false; break; }
+        if (p != k) {
+            for (int q = 0; q < FN; ++q) { const double t = JK[k * FN + q]; JK[k * FN + q] = JK[p * FN + q]; JK[p * FN + q] = t; }
+            for (int q = 0; q <= M; ++q) { const double t = X[k * (M + 1) + q]; X[k * (M + 1) + q] = X[p * (M + 1) + q]; X[p * (M + 1) + q] = t; }
+        }
+        for (int r = k + 1; r < FN; ++r) {
+            const double mlt = JK[r * FN + k] / JK[k * FN + k];
+            for (int q = k; q < FN; ++q) JK[r * FN + q] -= mlt * JK[k * FN + q];
+            for (int q = 0; q <= M; ++q) X[r * (M + 1) + q] -= mlt * X[k * (M + 1) + q];
+        }
+    }
+    if (ok) {
+#pragma unroll 1
+        for (int k = FN - 1; k >= 0; --k)
+            for (int q = 0; q <= M; ++q) {
+                double v = X[k * (M + 1) + q];
+                for (int j = k + 1; j < FN; ++j) v -= JK[k * FN + j] * X[j * (M + 1) + q];
+                X[k * (M + 1) + q] = v / JK[k * FN + k];
+            }
+    }
+    double* fx = a.fx + (I.nb + c) * FXW;
+#pragma unroll
+    for (int q = 0; q < FXW; ++q) fx[q] = X[q];
+#pragma unroll
+    for (int q = 0; q < M; ++q) {
+#pragma unroll
+        for (int cc = 0; cc < M; ++cc) {
+            double acc = 0.0;
+#pragma unroll
+            for (int j = 0; j < FS; ++j) acc += FB[j] * X[(j * M + q) * (M + 1) + cc];
+            Sr[q * M + cc] = hc * acc - (q == cc ? 1.0 : 0.0);
+            Rr[q * M + cc] = q == cc ? 1.0 : 0.0;
+        }
+        double kb = 0.0, xb = 0.0;
+#pragma unroll
+        for (int j = 0; j < FS; ++j) {
+            kb += Kc[j * M + q] * FB[j];
+            xb += FB[j] * X[(j * M + q) * (M + 1) + M];
+        }
+        const double C = (y[(c + 1) * M + q] - y[c * M + q]) - hc * kb;
+        gr[q] = -(C + hc * xb);
+    }
+    return ok;
+}
+#endif
+
 // Newton direction δ (in a.delta) for J δ = -F. Returns false if singular.
 BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     const int lane = lane_id();
@@ -994,9 +1110,13 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
 #pragma unroll 1
         for (int c = blo; c < bhi; ++c) {
             JT Sr[M * M], Rr[M * M], gr[M];
+#if BVP_FIRK
+            bad |= !firk_block(a, I, c, Sr, Rr, gr);
+#else
             block_jacobian(yj, tj, hj, I.pj, c, node, Sr, Rr);
 #pragma unroll
             for (int m = 0; m < M; ++m) gr[m] = -Fj[c * M + m];
+#endif
             if (c == blo) {
 #pragma unroll
                 for (int q = 0; q < M * M; ++q) { A[q] = Sr[q]; B[q] = Rr[q]; }
@@ -1401,7 +1521,7 @@ BVP_DEV double root_n(double x) {
     }
     return y;
 }
-BVP_DEV double root_p1(double x) { return root_n<ORD + 1>(x); }
+BVP_DEV double root_p1(double x) { return root_n<(FIRK ? FORDER : ORD) + 1>(x); }
 
 // which errors make the selector's ŝ: the defect's (DefectControl, and SequentialErrorControl
 // before its defect passes), the global estimate's to 1/(p+1) (SequentialErrorControl after),
@@ -1779,6 +1899,8 @@ BVP_DEV void polish_instance(const Args& a, Inst& I) {
     second_solve(a, I, false);
 }
 
+BVP_DEV void finish_instance(const Args& a, Inst& I, InstState& s);
+
 BVP_DEV void solve_instance(const Args& a, Inst& I) {
     InstState s;
     // phase 1: the instance stopped after its Newton solve (and defect) of this round for the
@@ -1884,6 +2006,12 @@ BVP_DEV void solve_instance(const Args& a, Inst& I) {
     }
     if (a.adaptive) s.retcode = maxed ? RET_MAXITERS : (info_ok ? RET_SUCCESS : RET_FAILURE);
     if (a.want_stages) finalize_stages(a, I);
+    finish_instance(a, I, s);
+}
+
+// An instance's results: the final mesh and solution to buffer 0, its state record, and with
+// host outputs its mesh, solution (and stages) to the pinned host arrays.
+BVP_DEV void finish_instance(const Args& a, Inst& I, InstState& s) {
     // results live in buffer 0
     if (I.cur == 1) {
         double* m0 = mesh_of(a, I, 0); const double* m1 = mesh_of(a, I, 1);
@@ -1923,6 +2051,12 @@ BVP_DEV void solve_instance(const Args& a, Inst& I) {
     }
     __syncwarp();
 }
+
+#if BVP_FIRK
+}  // namespace bvp
+#include "bvp_firk.cuh"
+namespace bvp {
+#endif
 
 BVP_DEV Inst make_inst(const Args& a, int q) {
     Inst I;
@@ -1977,7 +2111,11 @@ BVP_DEV void fused_body(const Args& a) {
             continue;
         }
         const long long c0 = a.inst_cost ? clock64() : 0;
+#if BVP_FIRK
+        firk_solve_instance(a, I);
+#else
         solve_instance(a, I);
+#endif
         if (a.inst_cost && lane == 0) a.inst_cost[I.q] = float(clock64() - c0) * (1.0f / 2000.0f);
     }
 }

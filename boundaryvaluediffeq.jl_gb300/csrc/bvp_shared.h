@@ -90,6 +90,7 @@ struct BvpArgs {
     int phase;                     // 0 new solves; 1 resume after the MIRK(p+2) solve; 2 that solve
     int* pause_list;               // phase 0/1: instances stopping for the MIRK(p+2) solve, appended
     int* pause_count;              //   at *pause_count
+    double* fx;                    // FIRK: [tot][FS M (M+1)] each interval's condensation record
 };
 
 // Work-order cost table of the fused solve: the longest solve time of the instances whose

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "bvp_shared.h"
+#include "bvp_firk_tableau.h"
 #include "bvp_embedded.inc"  // kEmbedCount, kEmbedNames[], kEmbedSources[], kEmbedHash
 
 namespace {
@@ -77,6 +78,12 @@ struct bvp_handle_s {
     // and for HOErrorControl the module compiled for MIRK(p+2), its stage array, the two lists
     // of instances waiting for its solve and their counts (pinned for the host's loop)
     bool glob = false, ho = false;
+    // a FIRK scheme (options.firk): its coefficients, the stage unknowns and condensation
+    // record per interval, and the records' array
+    bool firk = false;
+    BvpFirkTab ftab{};
+    int firk_fn = 0, firk_fxw = 0;
+    DevBuf d_fx;
     BvpLayout L_hi{};
     cudaLibrary_t lib_hi = nullptr;
     cudaKernel_t k_fused_hi = nullptr, k_probe_hi = nullptr;
@@ -235,7 +242,8 @@ void* bvp_stream(bvp_handle* h) { return h ? static_cast<void*>(h->stream) : nul
 // NVRTC build of the problem's module for one MIRK order (the cubin is cached on disk under a
 // hash of the sources and options). global_ctl compiles in the error controllers other than
 // DefectControl.
-static bvp_status build_cubin(bvp_handle* h, int order, int mirk6i, int global_ctl, std::vector<char>& cubin) {
+static bvp_status build_cubin(bvp_handle* h, int order, int mirk6i, int global_ctl, std::vector<char>& cubin,
+                              const std::string& prefix = std::string()) {
     const bvp_problem_desc& d = h->desc;
     const bvp_options& o = h->opt;
     std::vector<std::string> opts = {
@@ -251,7 +259,7 @@ static bvp_status build_cubin(bvp_handle* h, int order, int mirk6i, int global_c
     };
     if (global_ctl) opts.push_back("-DBVP_GLOBAL_CTL=1");
     const bool large = d.M > 8;
-    const std::string src = std::string("#include \"bvp_prelude.cuh\"\n#line 1 \"problem_source\"\n") +
+    const std::string src = std::string("#include \"bvp_prelude.cuh\"\n") + prefix + "#line 1 \"problem_source\"\n" +
                             h->source + (large ? "\n#include \"bvp_large.cuh\"\n" : "\n#include \"bvp_kernels.cuh\"\n");
     uint64_t key = fnv1a(kEmbedHash, std::strlen(kEmbedHash));
     key = fnv1a(src.data(), src.size(), key);
@@ -288,7 +296,9 @@ static bvp_status build_cubin(bvp_handle* h, int order, int mirk6i, int global_c
 static bvp_status compile_and_load(bvp_handle* h) {
     const bool large = h->desc.M > 8;
     std::vector<char> cubin;
-    bvp_status bs = build_cubin(h, h->opt.order, h->opt.mirk6i, h->glob ? 1 : 0, cubin);
+    // a FIRK handle's module: the MIRK4 build with the FIRK scheme's constants and solve path
+    bvp_status bs = h->firk ? build_cubin(h, 4, 0, 0, cubin, bvp_firk_constants(h->ftab))
+                            : build_cubin(h, h->opt.order, h->opt.mirk6i, h->glob ? 1 : 0, cubin);
     if (bs != BVP_OK) return bs;
     CU(cudaLibraryLoadData(&h->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
     if (large) {
@@ -359,12 +369,30 @@ bvp_status bvp_create(const bvp_problem_desc* desc, const char* source, const bv
     else if (o.controller != BVP_CTL_DEFECT && d.M > 8) why = "error controllers other than DefectControl take M <= 8";
     else if (o.controller != BVP_CTL_DEFECT && o.global_method == BVP_GLOBAL_HO && (o.order + 2 > 6 || o.mirk6i))
         why = "HOErrorControl solves with MIRK(order + 2): orders 2, 3 and 4";
+    else if (o.firk < 0 || o.firk > 4) why = "firk must be 0..4";
+    else if (o.firk && bvp_firk_tableau(o.firk, o.firk_stages).order == 0) why = "no such FIRK scheme";
+    else if (o.firk && (d.M > 8 || o.firk_stages * d.M > 32 || o.controller != BVP_CTL_DEFECT || o.want_stages ||
+                        h->source.find("BVP_SING") != std::string::npos))
+        why = "the FIRK path takes M <= 8, stages x M <= 32, DefectControl, no stage output and no singular term";
+    else if (o.firk && o.adaptive &&
+             ((o.firk == 1 && o.firk_stages == 1) || ((o.firk == 3 || o.firk == 4) && o.firk_stages == 2)))
+        why = "RadauIIa1, LobattoIIIb2 and LobattoIIIc2 have no adaptivity (algorithms.jl:411)";
     if (!why.empty()) { delete h; return BVP_ERR_INVALID; }
-    h->L = bvp_make_layout(d.M, o.order, d.twopoint ? 2 : d.n_bc_pts, d.twopoint, o.mirk6i);
+    if (o.firk) {
+        // FP64 throughout: the stage unknowns and their condensation in the Jacobian precision
+        h->firk = true;
+        h->ftab = bvp_firk_tableau(o.firk, o.firk_stages);
+        h->firk_fn = o.firk_stages * d.M;
+        h->firk_fxw = h->firk_fn * (d.M + 1);
+        h->opt.jac_precision = 64;
+        h->opt.fp32_phase = 0;
+        h->opt.linesearch_fallback = 0;
+    }
+    h->L = bvp_make_layout(d.M, h->firk ? 4 : o.order, d.twopoint ? 2 : d.n_bc_pts, d.twopoint, h->firk ? 0 : o.mirk6i);
     h->glob = o.adaptive && o.controller != BVP_CTL_DEFECT;
     h->ho = h->glob && o.global_method == BVP_GLOBAL_HO;
     if (h->ho) h->L_hi = bvp_make_layout(d.M, o.order + 2, d.twopoint ? 2 : d.n_bc_pts, d.twopoint, 0);
-    h->js = o.jac_precision == 64 ? 8 : 4;
+    h->js = h->opt.jac_precision == 64 ? 8 : 4;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
@@ -453,7 +481,7 @@ static bvp_status ensure_arena(bvp_handle* h, long long tot, int n, long long y0
     const size_t T = size_t(tot);
     bool ok = ensure_dev(h->d_mesh, 2 * T * 8) && ensure_dev(h->d_h, 2 * T * 8) &&
               ensure_dev(h->d_y, 2 * T * M * 8) && ensure_dev(h->d_ybak, T * M * 8) &&
-              ensure_dev(h->d_ybase, T * M * 8) && ensure_dev(h->d_K, T * L.S * M * 8) &&
+              ensure_dev(h->d_ybase, T * M * 8) && ensure_dev(h->d_K, T * std::max(L.S * M, h->firk_fn) * 8) &&
               ensure_dev(h->d_KI, T * L.NSXA * M * 8) && ensure_dev(h->d_F, T * M * 8) &&
               ensure_dev(h->d_err, T * 8) && ensure_dev(h->d_inc, T * M * 8) &&
               ensure_dev(h->d_iold, T * 4) && ensure_dev(h->d_Sb, T * M * M * js) &&
@@ -473,6 +501,7 @@ static bvp_status ensure_arena(bvp_handle* h, long long tot, int n, long long y0
               ensure_dev(h->d_y0_off, size_t(n + 1) * 8) && ensure_dev(h->d_out_off, size_t(n + 1) * 8) &&
               ensure_dev(h->d_norm, size_t(n) * 8);
     if (ok && h->glob) ok = ensure_dev(h->d_gerr, T * 8);
+    if (ok && h->firk) ok = ensure_dev(h->d_fx, T * h->firk_fxw * 8);
     if (ok && h->ho)
         ok = ensure_dev(h->d_K_hi, T * h->L_hi.S * M * 8) && ensure_dev(h->d_pause, (size_t(2) * n + 2) * 4) &&
              ensure_host(h->h_pause, 16);
@@ -539,6 +568,7 @@ static void fill_args(bvp_handle* h, BvpArgs& a, int n, long long tot, int y0_mo
     a.hybrid_de = o.hybrid_de;
     a.hybrid_ge = o.hybrid_ge;
     a.gerr = static_cast<double*>(h->d_gerr.p);
+    a.fx = static_cast<double*>(h->d_fx.p);
     a.phase = 0;
     if (h->ho) {
         a.pause_count = static_cast<int*>(h->d_pause.p);
@@ -1935,7 +1965,7 @@ void bvp_destroy(bvp_handle* h) {
                       &h->d_bcres, &h->d_G, &h->d_lnorm, &h->d_lsq, &h->d_ldnorm, &h->d_lbad,
                       &h->d_active, &h->d_N, &h->d_newN,
                       // work-order tables and the error controllers' arrays
-                      &h->d_inst_cost, &h->d_cost_tab, &h->d_gerr, &h->d_K_hi, &h->d_pause};
+                      &h->d_inst_cost, &h->d_cost_tab, &h->d_gerr, &h->d_K_hi, &h->d_pause, &h->d_fx};
     for (DevBuf* b : devs)
         if (b->p) cudaFree(b->p);
     HostBuf* hosts[] = {&h->h_in, &h->h_st, &h->h_off, &h->h_mesh, &h->h_y, &h->h_K, &h->h_KI, &h->h_pause};

@@ -105,6 +105,42 @@ def _controller_options(c) -> dict:
     raise TypeError(f"unknown error controller {c!r}")
 
 
+@dataclass(frozen=True)
+class FIRK:
+    """A FIRK algorithm in the expanded form (lib/BoundaryValueDiffEqFIRK/src/algorithms.jl):
+    family "RadauIIa", "LobattoIIIa", "LobattoIIIb" or "LobattoIIIc" with `stages` stages,
+    solved in FP64 throughout."""
+    family: str
+    stages: int
+    max_num_subintervals: int = 3000
+    defect_threshold: float = 0.1
+
+    def __post_init__(self):
+        ok = {"RadauIIa": (1, 2, 3, 5, 7), "LobattoIIIa": (2, 3, 4, 5), "LobattoIIIb": (2, 3, 4, 5),
+              "LobattoIIIc": (2, 3, 4, 5)}
+        if self.stages not in ok.get(self.family, ()):
+            raise ValueError(f"no FIRK scheme {self.family}{self.stages}")
+
+
+def RadauIIa1(**kw): return FIRK("RadauIIa", 1, **kw)  # noqa: E704
+def RadauIIa2(**kw): return FIRK("RadauIIa", 2, **kw)  # noqa: E704
+def RadauIIa3(**kw): return FIRK("RadauIIa", 3, **kw)  # noqa: E704
+def RadauIIa5(**kw): return FIRK("RadauIIa", 5, **kw)  # noqa: E704
+def RadauIIa7(**kw): return FIRK("RadauIIa", 7, **kw)  # noqa: E704
+def LobattoIIIa2(**kw): return FIRK("LobattoIIIa", 2, **kw)  # noqa: E704
+def LobattoIIIa3(**kw): return FIRK("LobattoIIIa", 3, **kw)  # noqa: E704
+def LobattoIIIa4(**kw): return FIRK("LobattoIIIa", 4, **kw)  # noqa: E704
+def LobattoIIIa5(**kw): return FIRK("LobattoIIIa", 5, **kw)  # noqa: E704
+def LobattoIIIb2(**kw): return FIRK("LobattoIIIb", 2, **kw)  # noqa: E704
+def LobattoIIIb3(**kw): return FIRK("LobattoIIIb", 3, **kw)  # noqa: E704
+def LobattoIIIb4(**kw): return FIRK("LobattoIIIb", 4, **kw)  # noqa: E704
+def LobattoIIIb5(**kw): return FIRK("LobattoIIIb", 5, **kw)  # noqa: E704
+def LobattoIIIc2(**kw): return FIRK("LobattoIIIc", 2, **kw)  # noqa: E704
+def LobattoIIIc3(**kw): return FIRK("LobattoIIIc", 3, **kw)  # noqa: E704
+def LobattoIIIc4(**kw): return FIRK("LobattoIIIc", 4, **kw)  # noqa: E704
+def LobattoIIIc5(**kw): return FIRK("LobattoIIIc", 5, **kw)  # noqa: E704
+
+
 def MIRK2(**kw): return MIRK(2, **kw)  # noqa: E704
 def MIRK3(**kw): return MIRK(3, **kw)  # noqa: E704
 def MIRK4(**kw): return MIRK(4, **kw)  # noqa: E704
@@ -190,16 +226,22 @@ def _solver(problem, alg: MIRK, abstol, adaptive, dense, solver_cls, controller=
         opts = dict(defect_threshold=alg.defect_threshold)
         if controller is not None:
             opts.update(_controller_options(controller))
-        sv = solver_cls(problem, order=alg.order, abstol=abstol, jac_precision=alg.jac_precision,
-                        adaptive=int(adaptive), want_stages=int(dense),
-                        max_subintervals=alg.max_num_subintervals, mirk6i=int(alg.mirk6i), **opts)
+        if isinstance(alg, FIRK):
+            # no stage output on the FIRK path: sol(t) is not available there
+            sv = solver_cls(problem, order=4, abstol=abstol, jac_precision=64, adaptive=int(adaptive),
+                            max_subintervals=alg.max_num_subintervals, firk=alg.family, firk_stages=alg.stages,
+                            **opts)
+        else:
+            sv = solver_cls(problem, order=alg.order, abstol=abstol, jac_precision=alg.jac_precision,
+                            adaptive=int(adaptive), want_stages=int(dense),
+                            max_subintervals=alg.max_num_subintervals, mirk6i=int(alg.mirk6i), **opts)
         _CACHE[key] = sv
     return sv
 
 
 def _to_solutions(res, solver, dense):
     n = len(res.n_nodes)
-    batch = _Batch(solver, n) if dense else None
+    batch = _Batch(solver, n) if dense and not getattr(getattr(solver, "options", None), "firk", 0) else None
     out = []
     for i in range(n):
         m, y = res.solution(i)
@@ -209,7 +251,7 @@ def _to_solutions(res, solver, dense):
     return out
 
 
-def solve(prob, alg: MIRK, *, dt: float, abstol: float = 1e-6, adaptive: bool = True, p=None, u0=None,
+def solve(prob, alg, *, dt: float, abstol: float = 1e-6, adaptive: bool = True, p=None, u0=None,
           dense: bool = True, controller=None, _solver_cls=BatchSolver):
     """solve(prob, MIRKn(); dt, abstol, controller) for one problem, or for an EnsembleProblem
     (one batched call over its trajectories). ``u0`` is a constant guess (M values) or per-node
@@ -246,5 +288,8 @@ def solve(prob, alg: MIRK, *, dt: float, abstol: float = 1e-6, adaptive: bool = 
 
 
 __all__ = ["solve", "MIRK", "MIRK2", "MIRK3", "MIRK4", "MIRK5", "MIRK6", "MIRK6I", "EnsembleProblem", "BVPSolution",
+           "FIRK", "RadauIIa1", "RadauIIa2", "RadauIIa3", "RadauIIa5", "RadauIIa7", "LobattoIIIa2", "LobattoIIIa3",
+           "LobattoIIIa4", "LobattoIIIa5", "LobattoIIIb2", "LobattoIIIb3", "LobattoIIIb4", "LobattoIIIb5",
+           "LobattoIIIc2", "LobattoIIIc3", "LobattoIIIc4", "LobattoIIIc5",
            "DefectControl", "GlobalErrorControl", "SequentialErrorControl", "HybridErrorControl",
            "HOErrorControl", "REErrorControl", "RET_SUCCESS", "RET_MAXITERS"]

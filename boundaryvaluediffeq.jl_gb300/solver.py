@@ -98,6 +98,9 @@ class BatchSolver:
             opts["controller"] = _lib.CONTROLLERS[opts["controller"]]
         if isinstance(opts.get("global_method"), str):
             opts["global_method"] = _lib.GLOBAL_METHODS[opts["global_method"]]
+        # firk="RadauIIa" | "LobattoIIIa" | "LobattoIIIb" | "LobattoIIIc" with firk_stages=s
+        if isinstance(opts.get("firk"), str):
+            opts["firk"] = _lib.FIRK_FAMILIES[opts["firk"]]
         for k, v in opts.items():
             if not hasattr(o, k):
                 raise KeyError(k)

@@ -78,6 +78,13 @@ typedef struct {
     int32_t global_method;        /* bvp_global_method of the global estimate (the controller's
                                      GlobalErrorControl(method = ...)) */
     double hybrid_de, hybrid_ge;  /* HybridErrorControl(DE, GE) */
+    int32_t firk;                 /* 0: MIRK (order, mirk6i). A FIRK scheme in the expanded form
+                                     (lib/BoundaryValueDiffEqFIRK): 1 RadauIIa, 2 LobattoIIIa,
+                                     3 LobattoIIIb, 4 LobattoIIIc, with firk_stages stages (RadauIIa
+                                     1, 2, 3, 5, 7; Lobatto 2..5). FP64 throughout, DefectControl,
+                                     M <= 8, standard BCs at the tspan's ends or two-point BCs, no
+                                     singular term and no stage output */
+    int32_t firk_stages;
 } bvp_options;
 
 /* Error controllers (lib/BoundaryValueDiffEqCore/src/calc_errors.jl:54-139, the error

@@ -726,16 +726,18 @@ struct InstanceSolver {
     // errors of this round's estimate (the global ones when the defect passed) to 1/(p+1),
     // ρ = 2 (127-177); HybridErrorControl the sum of the defect and global terms, each to
     // 1/(p+1), ρ = 2 (179-243).
+    // `order` overrides the method order (the FIRK solver's, whose tableau is not a MIRK one).
     bool mesh_selector(std::vector<double>& old_mesh, std::vector<double>& old_h,
-                       int ctl = CTL_DEFECT, bool seq_global = false) {
+                       int ctl = CTL_DEFECT, bool seq_global = false, int order = 0) {
         const int n = N - 1;
         const double safety = 1.3, rho = ctl == CTL_DEFECT ? 1.0 : 2.0;
         const int ub = 4 * (N - 1), lb = N / 2;
         std::vector<double> s_hat(n);
-        const double e1 = 1.0 / (tb.order + 1);
+        const int p = order > 0 ? order : tb.order;
+        const double e1 = 1.0 / (p + 1);
         for (int i = 0; i < n; ++i) {
             if (ctl == CTL_DEFECT) s_hat[i] = std::pow(err_max[i] / op.abstol, e1);
-            else if (ctl == CTL_GLOBAL) s_hat[i] = std::pow(gerr[i] / op.abstol, 1.0 / tb.order);
+            else if (ctl == CTL_GLOBAL) s_hat[i] = std::pow(gerr[i] / op.abstol, 1.0 / p);
             else if (ctl == CTL_SEQUENTIAL) s_hat[i] = std::pow((seq_global ? gerr : err_max)[i] / op.abstol, e1);
             else s_hat[i] = std::pow(err_max[i] / op.abstol, e1) + std::pow(gerr[i] / op.abstol, e1);
         }

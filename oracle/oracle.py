@@ -20,7 +20,8 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _BUILD = os.path.join(_HERE, "_build")
-_SOURCES = ("oracle_entry.cpp", "mirk_oracle.hpp", "mirk_tableaus.hpp", "dual.hpp")
+_SOURCES = ("oracle_entry.cpp", "mirk_oracle.hpp", "mirk_tableaus.hpp", "dual.hpp", "firk_oracle.hpp",
+            "firk_tableaus.hpp")
 _lock = threading.Lock()
 
 RET_SUCCESS, RET_FAILURE, RET_MAXITERS, RET_TRUNCATED = 0, 1, 2, 3
@@ -48,6 +49,7 @@ class Options(C.Structure):
 
 
 CONTROLLERS = {"defect": 0, "global": 1, "sequential": 2, "hybrid": 3}
+FIRK_FAMILIES = {"RadauIIa": 0, "LobattoIIIa": 1, "LobattoIIIb": 2, "LobattoIIIc": 3}
 GLOBAL_METHODS = {"HO": 0, "RE": 1}
 
 
@@ -111,6 +113,9 @@ class Oracle:
         L.oracle_defect.restype = C.c_double
         L.oracle_jacobian.restype = C.c_int
         L.oracle_newton_step.restype = C.c_int
+        L.oracle_firk_solve_batch.restype = C.c_int
+        L.oracle_firk_residual.restype = C.c_double
+        L.oracle_firk_tableau.restype = C.c_int
 
     def options(self, **kw) -> Options:
         o = Options()
@@ -164,6 +169,64 @@ class Oracle:
         if want_stages:
             out["K"], out["KI"] = K, KI
         return out
+
+    def firk_solve_batch(self, family, stages, params, n_intervals, tspans, y0, *, y0_mode=0, cap_nodes=None,
+                         want_stages=False, **opts):
+        """Expanded FIRK solve of n instances (family: FIRK_FAMILIES key or index)."""
+        fam = FIRK_FAMILIES[family] if isinstance(family, str) else int(family)
+        o = self.options(**opts)
+        params = np.ascontiguousarray(params, dtype=np.float64).reshape(len(n_intervals), -1)
+        n_int = np.ascontiguousarray(n_intervals, dtype=np.int32)
+        n = len(n_int)
+        tsp = np.ascontiguousarray(tspans, dtype=np.float64).reshape(n, 2)
+        y0a = np.ascontiguousarray(y0, dtype=np.float64).ravel()
+        if cap_nodes is None:
+            cap_nodes = int(max(int(n_int.max()) + 1, 4 * int(n_int.max()) + 1, o.max_subintervals + 1))
+        M = self.M
+        out = dict(retcode=np.zeros(n, np.int32), n_nodes=np.zeros(n, np.int32),
+                   mesh=np.zeros((n, cap_nodes)), y=np.zeros((n, cap_nodes, M)),
+                   newton_iters=np.zeros(n, np.int32), rounds=np.zeros(n, np.int32),
+                   defect=np.zeros(n), resid=np.zeros(n))
+        K = np.zeros((n, cap_nodes - 1, stages, M)) if want_stages else None
+        rc = self.lib.oracle_firk_solve_batch(
+            C.byref(self.info), C.byref(o), C.c_int(fam), C.c_int(stages), C.c_int(n), _p(params, C.c_double),
+            _p(n_int, C.c_int32), _p(tsp, C.c_double), C.c_int(y0_mode), _p(y0a, C.c_double), C.c_int(cap_nodes),
+            _p(out["retcode"], C.c_int32), _p(out["n_nodes"], C.c_int32), _p(out["mesh"], C.c_double),
+            _p(out["y"], C.c_double), _p(out["newton_iters"], C.c_int32), _p(out["rounds"], C.c_int32),
+            _p(out["defect"], C.c_double), _p(out["resid"], C.c_double), _p(K, C.c_double))
+        if rc == -2:
+            raise ValueError(f"no FIRK scheme {family} with {stages} stages")
+        if rc == -3:
+            raise ValueError("the FIRK path evaluates standard BCs at the tspan's ends only")
+        if rc != 0:
+            raise RuntimeError(f"oracle_firk_solve_batch failed: {rc}")
+        if want_stages:
+            out["K"] = K
+        return out
+
+    def firk_tableau(self, family, stages):
+        """(order, s, tau*, c, b, a, q) of a FIRK scheme as the oracle computes them."""
+        fam = FIRK_FAMILIES[family] if isinstance(family, str) else int(family)
+        buf = np.zeros(115)
+        if self.lib.oracle_firk_tableau(C.c_int(fam), C.c_int(stages), _p(buf, C.c_double)) != 0:
+            raise ValueError("no such scheme")
+        s = int(buf[1])
+        return (int(buf[0]), s, float(buf[2]), buf[3:3 + s].copy(), buf[10:10 + s].copy(),
+                buf[17:66].reshape(7, 7)[:s, :s].copy(), buf[66:115].reshape(7, 7)[:s, :s].copy())
+
+    def firk_residual(self, family, stages, params, mesh, y, K):
+        fam = FIRK_FAMILIES[family] if isinstance(family, str) else int(family)
+        params, mesh, y = self._prep(params, mesh, y)
+        N, M = len(mesh), self.M
+        K = np.ascontiguousarray(K, dtype=np.float64).reshape(N - 1, stages, M)
+        F = np.zeros(N * M)
+        Fs = np.zeros((N - 1, stages, M))
+        o = self.options()
+        nrm = self.lib.oracle_firk_residual(C.byref(self.info), C.byref(o), C.c_int(fam), C.c_int(stages),
+                                            _p(params, C.c_double), C.c_int(N), _p(mesh, C.c_double),
+                                            _p(y, C.c_double), _p(K, C.c_double), _p(F, C.c_double),
+                                            _p(Fs, C.c_double))
+        return F, Fs, nrm
 
     def _prep(self, params, mesh, y):
         params = np.ascontiguousarray(params, dtype=np.float64).ravel()

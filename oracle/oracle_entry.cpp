@@ -42,6 +42,7 @@ template <class T, class P> inline void bvp_bcb(T*, const T*, const P*) {}
 #endif
 
 #include "mirk_oracle.hpp"
+#include "firk_oracle.hpp"
 
 using namespace oracle;
 static constexpr int MM = BVP_M;
@@ -225,6 +226,96 @@ void oracle_interpolate(int order, int N, const double* mesh, const double* y, c
             out[size_t(k) * MM + m] = deriv ? acc : acc * dt + y[size_t(i) * MM + m];
         }
     }
+}
+
+
+// FIRK coefficients of one scheme (family: 0 Radau IIA, 1 Lobatto IIIA, 2 IIIB, 3 IIIC):
+// out = [order, s, tau*, c(7), b(7), a(7x7), q(7x7)]; returns 0, or -1 for no such scheme.
+int oracle_firk_tableau(int family, int stages, double* out) {
+    const FirkTableau t = make_firk_tableau(family, stages);
+    if (t.order == 0) return -1;
+    out[0] = t.order; out[1] = t.s; out[2] = t.tau_star;
+    for (int i = 0; i < 7; ++i) { out[3 + i] = t.c[i]; out[10 + i] = t.b[i]; }
+    for (int i = 0; i < 7; ++i)
+        for (int j = 0; j < 7; ++j) { out[17 + i * 7 + j] = t.a[i][j]; out[66 + i * 7 + j] = t.q[i][j]; }
+    return 0;
+}
+
+// Expanded FIRK solve of a batch (firk.jl:290-622); arguments as oracle_solve_batch, with
+// the scheme given by family and stages (opt->order is not used). K_out (may be null):
+// the final stage derivatives, (cap_nodes - 1) x stages x M per instance.
+int oracle_firk_solve_batch(const ProblemInfo* info, const Options* opt, int family, int stages, int n_inst,
+                            const double* params, const int32_t* n_intervals, const double* tspans, int y0_mode,
+                            const double* y0, int cap_nodes, int32_t* retcode, int32_t* n_nodes, double* mesh_out,
+                            double* y_out, int32_t* newton_iters, int32_t* rounds, double* defect, double* resid,
+                            double* K_out) {
+    if (info->M != MM) return -1;
+    const FirkTableau ft = make_firk_tableau(family, stages);
+    if (ft.order == 0) return -2;
+    if (!info->twopoint)
+        for (int k = 0; k < info->n_bc_pts; ++k)
+            for (int q = 0; q < n_inst; ++q)
+                if (info->bc_t[k] != tspans[2 * q] && info->bc_t[k] != tspans[2 * q + 1]) return -3;
+    const Tableau dummy = make_tableau(4);
+    std::vector<int64_t> y0_off(n_inst + 1, 0);
+    for (int i = 0; i < n_inst; ++i)
+        y0_off[i + 1] = y0_off[i] + (y0_mode == 1 ? int64_t(n_intervals[i] + 1) * MM : MM);
+    int nt = opt->nthreads;
+#ifdef _OPENMP
+    if (nt <= 0) nt = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+#endif
+    for (int q = 0; q < n_inst; ++q) {
+        FirkSolver<MM> sv(dummy, ft, *opt, *info, params + size_t(q) * info->n_params);
+        const int n = n_intervals[q];
+        sv.N = n + 1;
+        sv.mesh.resize(n + 1);
+        uniform_mesh(tspans[2 * q], tspans[2 * q + 1], n, sv.mesh.data());
+        sv.h.resize(n);
+        for (int i = 0; i < n; ++i) sv.h[i] = sv.mesh[i + 1] - sv.mesh[i];
+        sv.y.resize(size_t(n + 1) * MM);
+        const double* src = y0 + y0_off[q];
+        for (int i = 0; i <= n; ++i)
+            for (int m = 0; m < MM; ++m) sv.y[size_t(i) * MM + m] = (y0_mode == 1) ? src[size_t(i) * MM + m] : src[m];
+        sv.extend();
+        sv.solve();
+        retcode[q] = sv.retcode;
+        n_nodes[q] = sv.N;
+        newton_iters[q] = sv.newton_total;
+        rounds[q] = sv.rounds;
+        defect[q] = sv.last_defect;
+        resid[q] = sv.last_resid;
+        const int nc = std::min(sv.N, cap_nodes);
+        if (sv.N > cap_nodes) retcode[q] = 3;
+        for (int i = 0; i < nc; ++i) {
+            mesh_out[size_t(q) * cap_nodes + i] = sv.mesh[i];
+            for (int m = 0; m < MM; ++m) y_out[(size_t(q) * cap_nodes + i) * MM + m] = sv.y[size_t(i) * MM + m];
+        }
+        if (K_out)
+            std::memcpy(K_out + size_t(q) * (cap_nodes - 1) * stages * MM, sv.K.data(),
+                        sizeof(double) * size_t(std::max(nc - 1, 0)) * stages * MM);
+    }
+    return 0;
+}
+
+// The FIRK residual (stage and continuity rows, BC rows) and its norm on a given mesh, nodes
+// and stages: F as oracle_residual lays it out, Fs (N-1) x stages x M.
+double oracle_firk_residual(const ProblemInfo* info, const Options* opt, int family, int stages,
+                            const double* params, int N, const double* mesh, const double* y, const double* K,
+                            double* F_out, double* Fs_out) {
+    const FirkTableau ft = make_firk_tableau(family, stages);
+    const Tableau dummy = make_tableau(4);
+    FirkSolver<MM> sv(dummy, ft, *opt, *info, params);
+    sv.N = N;
+    sv.mesh.assign(mesh, mesh + N);
+    sv.h.resize(N - 1);
+    for (int i = 0; i + 1 < N; ++i) sv.h[i] = mesh[i + 1] - mesh[i];
+    sv.y.assign(y, y + size_t(N) * MM);
+    sv.K.assign(K, K + size_t(N - 1) * stages * MM);
+    const double nrm = sv.residual();
+    if (F_out) std::memcpy(F_out, sv.F.data(), sizeof(double) * sv.F.size());
+    if (Fs_out) std::memcpy(Fs_out, sv.Fs.data(), sizeof(double) * sv.Fs.size());
+    return nrm;
 }
 
 }  // extern "C"

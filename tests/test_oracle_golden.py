@@ -292,3 +292,82 @@ def test_ho_error_control_needs_mirk_p_plus_2(problems):
     p = problems.LINEAR
     with pytest.raises(ValueError, match="order"):
         _solve1(p, n=10, order=5, controller="global", global_method="HO")
+
+
+# ---- FIRK, expanded form (lib/BoundaryValueDiffEqFIRK/test/expanded) ----------------------
+FIRK_SCHEMES = [("LobattoIIIa", s) for s in (2, 3, 4, 5)] + [("LobattoIIIb", s) for s in (2, 3, 4, 5)] + \
+               [("LobattoIIIc", s) for s in (2, 3, 4, 5)] + [("RadauIIa", s) for s in (2, 3, 5, 7)]
+
+
+@pytest.mark.parametrize("family,stages", FIRK_SCHEMES)
+@pytest.mark.parametrize("name", ["affine", "affine_twopoint"])
+def test_firk_affineness(problems, name, family, stages):
+    # firk_affineness_tests.jl:6-29: u1 = 5 - t exactly, dt = 0.2, non-adaptive, affineTol 1e-2
+    p = problems.ALL[name]
+    o = _oracle(p)
+    r = o.firk_solve_batch(family, stages, np.zeros((1, 1)), [25], [p.tspan], [p.u0], adaptive=0)
+    assert r["retcode"][0] == RET_SUCCESS
+    u1 = r["y"][0, :26, 0]
+    assert np.abs(np.diff(u1) + 0.2).max() + abs(u1[0] - 5) < 1e-2
+
+
+@pytest.mark.parametrize("family,stages", FIRK_SCHEMES)
+@pytest.mark.parametrize("name", ["linear", "linear_twopoint"])
+def test_firk_convergence_order(problems, name, family, stages):
+    # firk_convergence_tests.jl:6-57: the error at the nodes falls at order 2s - 2 (Lobatto) or
+    # 2s - 1 (Radau IIA), testTol 0.3, on dt = 1/8, 1/16, 1/32 (1/4 .. 1/16 for four stages);
+    # estimates where the error is already at roundoff are not judged (the reference marks them
+    # broken)
+    p = problems.ALL[name]
+    o = _oracle(p)
+    dts = (1 / 4, 1 / 8, 1 / 16) if stages == 4 else (1 / 8, 1 / 16, 1 / 32)
+    errs = []
+    for dt in dts:
+        n = int(round(5.0 / dt))
+        r = o.firk_solve_batch(family, stages, np.zeros((1, 1)), [n], [p.tspan], [p.u0], adaptive=0, abstol=1e-8)
+        assert r["retcode"][0] == RET_SUCCESS
+        m, y = r["mesh"][0, :n + 1], r["y"][0, :n + 1]
+        errs.append(np.abs(y - problems.linear_analytic(m)).max())
+    order = 2 * stages - 1 if family == "RadauIIa" else 2 * stages - 2
+    if errs[-1] < 1e-12:
+        return
+    est = np.log2(errs[-2] / errs[-1])
+    assert abs(est - order) < 0.3, (errs, est)
+
+
+def test_firk_tableaus_match_the_reference_tables(problems):
+    # the coefficients, computed from their defining conditions, against entries the reference
+    # tabulates (radau_tableaus.jl:47-69, lobatto_tableaus.jl:136-160, 244-266)
+    o = _oracle(problems.LINEAR)
+    order, s, tau, c, b, a, q = o.firk_tableau("RadauIIa", 3)
+    assert order == 5 and tau == 0.0
+    assert np.allclose(q, [[1.5580782047249224, -0.8914115380582555, 0.33333333333333315],
+                           [-1.9869472213484427, 3.320280554681775, -1.3333333333333326],
+                           [0.8052720793239877, -1.9163831904350983, 1.1111111111111107]], rtol=0, atol=1e-13)
+    assert np.allclose(b, [4 / 9 - math.sqrt(6) / 36, 4 / 9 + math.sqrt(6) / 36, 1 / 9], atol=1e-15)
+    assert np.allclose(a[0], [11 / 45 - 7 * math.sqrt(6) / 360, 37 / 225 - 169 * math.sqrt(6) / 1800,
+                              -2 / 225 + math.sqrt(6) / 75], atol=1e-15)
+    _, _, tau_b, _, _, ab, _ = o.firk_tableau("LobattoIIIb", 3)
+    assert np.allclose(ab, [[1 / 6, -1 / 6, 0], [1 / 6, 1 / 3, 0], [1 / 6, 5 / 6, 0]], atol=1e-15)
+    _, _, tau_c, _, _, ac, _ = o.firk_tableau("LobattoIIIc", 3)
+    assert np.allclose(ac, [[1 / 6, -1 / 3, 1 / 6], [1 / 6, 5 / 12, -1 / 12], [1 / 6, 2 / 3, 1 / 6]], atol=1e-15)
+    assert tau_b == 0.21132486540518713 and tau_c == 0.7886751345948129
+    _, _, _, _, _, _, q5 = o.firk_tableau("RadauIIa", 5)
+    assert np.allclose(q5[0], [1.5864079001863276, -1.0081178814983707, 0.7309748661597844,
+                               -0.5092648848477398, 0.19999999999999882], atol=1e-10)
+
+
+@pytest.mark.parametrize("family,stages", [("RadauIIa", 2), ("RadauIIa", 3), ("RadauIIa", 5), ("RadauIIa", 7),
+                                           ("LobattoIIIa", 3), ("LobattoIIIb", 4), ("LobattoIIIc", 5)])
+def test_firk_ensemble_converges(problems, family, stages):
+    # ensemble_tests.jl:4-95: u'' = -p u on (0, pi/2) over random p, every trajectory converges
+    # (adaptive); the second BC at the tspan's end (the FIRK path evaluates BCs at the ends, the
+    # reference's test at t = 1)
+    import dataclasses
+    p = dataclasses.replace(problems.ENSEMBLE, bc_t=(0.0, math.pi / 2))
+    o = _oracle(p)
+    rng = np.random.default_rng(3)
+    params = rng.uniform(0.5, 1.5, (16, 1))
+    n = int(math.ceil((math.pi / 2) / 0.1 - 1e-12))
+    r = o.firk_solve_batch(family, stages, params, [n] * 16, [p.tspan] * 16, [p.u0] * 16)
+    assert (r["retcode"] == RET_SUCCESS).all()
