@@ -2126,9 +2126,20 @@ BVP_DEV void fused_body(const Args& a) {
 // fewer leave each warp the registers its solve needs without spilling (the pendulum's MIRK4
 // solve takes 156: 198 bytes of spills per thread at 4 blocks, none at 3). The handle's
 // autotuner picks one by timing them on its own batches.
+// The builds with the error controllers and the FIRK schemes are not tuned: one kernel each, at
+// 3 blocks per SM (which keeps the MIRK4 pendulum solve's registers without spills), and the
+// module that only runs HOErrorControl's MIRK(p+2) solves (BVP_POLISH_ONLY) has nothing else.
+#if BVP_GLOBAL_CTL || BVP_FIRK
+extern "C" __global__ void __launch_bounds__(128, 3) bvp_solve_fused(const bvp::Args a) { bvp::fused_body(a); }
+#else
 extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::Args a) { bvp::fused_body(a); }
 extern "C" __global__ void __launch_bounds__(128, 3) bvp_solve_fused_b3(const bvp::Args a) { bvp::fused_body(a); }
 extern "C" __global__ void __launch_bounds__(128, 2) bvp_solve_fused_b2(const bvp::Args a) { bvp::fused_body(a); }
+#endif
+#ifndef BVP_POLISH_ONLY
+#define BVP_POLISH_ONLY 0
+#endif
+#if !BVP_POLISH_ONLY && !BVP_FIRK
 
 // Stage kernels on caller-provided (mesh, y) in buffer 0 with N = st[q].N. Used by the
 // per-kernel parity tests; stage: 0 residual (F, K, BC residual), 1 Jacobian blocks,
@@ -2169,6 +2180,7 @@ extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, i
         __syncwarp();
     }
 }
+#endif  // !BVP_POLISH_ONLY && !BVP_FIRK
 
 // Copy the results of every instance (buffer 0) into packed host-bound arrays.
 // out_off has n_inst + 1 entries (bvp_out_offsets); the outputs hold cap points: a batch
@@ -2238,6 +2250,8 @@ extern "C" __global__ void __launch_bounds__(1024) bvp_out_offsets(int n, const 
     if (tid == 0) { d_off[n] = carry; h_off[n] = carry; }
 }
 
+#if !BVP_POLISH_ONLY && !BVP_FIRK
+
 // Dense output of the last solve (needs want_stages): u(t) or u'(t) at nq query times per
 // instance through the MIRK interpolant (interpolation.jl:17-204: interval(mesh, t),
 // τ = (t - t_i)/h_i, u = y_i + h Σ w_r(τ) K_r, u' = Σ w'_r(τ) K_r). One warp per instance,
@@ -2275,6 +2289,8 @@ extern "C" __global__ void bvp_dense(const bvp::Args a, int nq, const double* tq
 }
 
 // Device-side layout constants, checked against the host's at handle creation.
+#endif  // !BVP_POLISH_ONLY && !BVP_FIRK
+
 extern "C" __global__ void bvp_layout_probe(int* out) {
     out[0] = bvp::SCRW;
     out[1] = bvp::ISCRW;

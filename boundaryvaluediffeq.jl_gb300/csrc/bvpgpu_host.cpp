@@ -317,21 +317,28 @@ static bvp_status compile_and_load(bvp_handle* h) {
         return BVP_OK;
     }
     CU(cudaLibraryGetKernel(&h->k_fused, h->lib, "bvp_solve_fused"));
-    CU(cudaLibraryGetKernel(&h->k_fused_v[1], h->lib, "bvp_solve_fused_b3"));
-    CU(cudaLibraryGetKernel(&h->k_fused_v[2], h->lib, "bvp_solve_fused_b2"));
     h->k_fused_v[0] = h->k_fused;
-    CU(cudaLibraryGetKernel(&h->k_stage, h->lib, "bvp_stage"));
+    if (h->glob || h->firk) {
+        // one fused kernel in these builds: nothing to tune
+        h->k_fused_v[1] = h->k_fused_v[2] = h->k_fused;
+        h->fused_pick = 1;
+        h->tune.done = true;
+    } else {
+        CU(cudaLibraryGetKernel(&h->k_fused_v[1], h->lib, "bvp_solve_fused_b3"));
+        CU(cudaLibraryGetKernel(&h->k_fused_v[2], h->lib, "bvp_solve_fused_b2"));
+    }
+    if (!h->firk) CU(cudaLibraryGetKernel(&h->k_stage, h->lib, "bvp_stage"));
     CU(cudaLibraryGetKernel(&h->k_pack, h->lib, "bvp_pack"));
     CU(cudaLibraryGetKernel(&h->k_offsets, h->lib, "bvp_out_offsets"));
     CU(cudaLibraryGetKernel(&h->k_probe, h->lib, "bvp_layout_probe"));
     CU(cudaLibraryGetKernel(&h->k_convert, h->lib, "bvp_convert_params"));
     CU(cudaLibraryGetKernel(&h->k_prep, h->lib, "bvp_prep"));
-    CU(cudaLibraryGetKernel(&h->k_dense, h->lib, "bvp_dense"));
+    if (!h->firk) CU(cudaLibraryGetKernel(&h->k_dense, h->lib, "bvp_dense"));
     CU(cudaLibraryGetKernel(&h->k_learn, h->lib, "bvp_learn_costs"));
     if (h->ho) {
         // HOErrorControl's second solve: the same problem with MIRK(p+2) (adaptivity.jl:552-555)
         std::vector<char> cubin_hi;
-        bs = build_cubin(h, h->opt.order + 2, 0, 1, cubin_hi);
+        bs = build_cubin(h, h->opt.order + 2, 0, 1, cubin_hi, "#define BVP_POLISH_ONLY 1\n");
         if (bs != BVP_OK) return bs;
         CU(cudaLibraryLoadData(&h->lib_hi, cubin_hi.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
         CU(cudaLibraryGetKernel(&h->k_fused_hi, h->lib_hi, "bvp_solve_fused"));
@@ -1882,6 +1889,7 @@ bvp_status bvp_eval_stage(bvp_handle* h, int32_t stage, int32_t n, const double*
                           double* K, double* S, double* R, double* delta, double* err) {
     if (!h) return BVP_ERR_INVALID;
     if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: only bvp_solve_batch is available");
+    if (h->firk) return fail(h, BVP_ERR_INVALID, "the stage kernels are MIRK's: not available on the FIRK path");
     if (stage < 0 || stage > 3 || n < 1 || !n_nodes || !mesh || !y || (h->desc.n_params > 0 && !params))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
     const BvpLayout& L = h->L;
