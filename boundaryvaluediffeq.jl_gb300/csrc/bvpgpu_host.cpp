@@ -619,13 +619,6 @@ static int fused_variant(bvp_handle* h, int n, int y0_mode) {
         }
         t.pending = -1;
     }
-    if (n < kLearnMin || h->learn_left > 0) return h->fused_pick;
-    const long long key = (long long)n * 4 + y0_mode;
-    if (key != t.key) {
-        t.key = key;
-        t.next = 0;
-        for (int c = 0; c < 3; ++c) { t.sum[c] = 0.0f; t.cnt[c] = 0; }
-    }
     if (t.cnt[0] >= 2 && t.cnt[1] >= 2 && t.cnt[2] >= 2) {
         int best = 0;
         for (int c = 1; c < 3; ++c)
@@ -633,6 +626,13 @@ static int fused_variant(bvp_handle* h, int n, int y0_mode) {
         h->fused_pick = best;
         t.done = true;
         return best;
+    }
+    if (n < kLearnMin || h->learn_left > 0) return h->fused_pick;
+    const long long key = (long long)n * 4 + y0_mode;
+    if (key != t.key) {
+        t.key = key;
+        t.next = 0;
+        for (int c = 0; c < 3; ++c) { t.sum[c] = 0.0f; t.cnt[c] = 0; }
     }
     const int c = t.next;
     t.next = (t.next + 1) % 3;
