@@ -249,11 +249,11 @@ def run_reference(args):
     return 0
 
 
-# DRAM bytes (read + write) of one bvp_solve_fused launch per instance, from an ncu capture
+# DRAM bytes (read + write) of one fused-solve launch per instance, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the surrogate-warm solve of the
-# 2048-instance pendulum batch: 54.56 MB / 2048. Traffic grows with the instance count, so
-# the roofline's traffic is this figure times the batch size.
-FUSED_DRAM_BYTES_PER_INSTANCE = 54.56e6 / 2048
+# 2048-instance pendulum batch with the tuned 2-blocks-per-SM build: 38.18 MB / 2048. Traffic
+# grows with the instance count, so the roofline's traffic is this figure times the batch size.
+FUSED_DRAM_BYTES_PER_INSTANCE = 38.18e6 / 2048
 N_TRAIN = 50000
 TRAIN_SEED = SEED + 10_000      # training instances are disjoint from the timed batch
 GRID = 64
@@ -425,8 +425,8 @@ def main():
         sv.solve_device_warm(net, dfeat, GRID, dp, dn, dts, nmax)
 
     # handle setup, untimed: its first solves teach the handle its work order (three solves)
-    # and then its launch shape (two solves per candidate); both stay fixed afterwards
-    for _ in range(9):
+    # and then its launch shape (three solves per candidate); both stay fixed afterwards
+    for _ in range(12):
         timed(warm_kernels)
     # warm-up; the warm attempt's failures are deterministic for a given batch, and their
     # plain-guess re-solve is part of every timed warm step
@@ -564,7 +564,7 @@ def main():
                   "failures": int((res_plain.retcode != 0).sum()),
                   "fused_ms_mean": statistics.mean(plain_fused)},
         "gpu_launches": launches_warm * args.steps,
-        "handle_setup": {"note": "9 untimed solves before warm-up: work order learned, then launch shape tuned",
+        "handle_setup": {"note": "12 untimed solves before warm-up: work order learned, then launch shape tuned",
                          "work_order_learned": bool(sv.work_order()[0]), "tuning": sv.tuning()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                      "frac": achieved / peaks.get("hbm_gbs", 1.0),

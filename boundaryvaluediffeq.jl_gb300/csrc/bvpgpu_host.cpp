@@ -64,7 +64,8 @@ struct bvp_handle_s {
     bool have_tab = false;
     // launch-shape autotuner of the fused solve: the kernel built for 4, 3 and 2 resident
     // blocks per SM; once the work order is learned, the next solves of one batch shape rotate
-    // through the three (two timed solves each) and the handle keeps the fastest
+    // through the three (an untimed first launch, then two timed solves each) and the handle
+    // keeps the fastest
     cudaKernel_t k_fused_v[3] = {nullptr, nullptr, nullptr};
     int fused_pick = 1;
     struct {
@@ -72,6 +73,7 @@ struct bvp_handle_s {
         int pending = -1, next = 0;
         float sum[3] = {0, 0, 0};
         int cnt[3] = {0, 0, 0};
+        bool seen[3] = {false, false, false};   // a candidate's first launch (module load) is not timed
         bool done = false;
     } tune;
     // error controllers other than DefectControl (fused path): the global estimates per interval,
@@ -636,7 +638,8 @@ static int fused_variant(bvp_handle* h, int n, int y0_mode) {
     }
     const int c = t.next;
     t.next = (t.next + 1) % 3;
-    t.pending = c;
+    if (t.seen[c]) t.pending = c;
+    t.seen[c] = true;
     return c;
 }
 

@@ -283,8 +283,8 @@ bvp_status bvp_get_tuning(bvp_handle* h, int32_t* threads);
 /* The fused solve's launch shape (no reference counterpart): bvp_solve_fused is built for 4, 3
  * and 2 resident blocks of 4 warps per SM (register budgets of 128, 168 and 255 per thread).
  * The handle starts with 3; once its work order is learned, its next solves of one batch
- * shape (instance count, guess form; at least 256 instances) rotate through the three, two
- * timed solves each, and it keeps the fastest. *blocks_per_sm: the current choice (0 for
+ * shape (instance count, guess form; at least 256 instances) rotate through the three (a first,
+ * untimed launch of each, then two timed solves each), and it keeps the fastest. *blocks_per_sm: the current choice (0 for
  * state dimensions above 8); *tuned (if not NULL): 1 once chosen; ms (if not NULL, 3 entries):
  * the candidates' mean kernel times so far. */
 bvp_status bvp_get_fused_tuning(bvp_handle* h, int32_t* blocks_per_sm, int32_t* tuned, float* ms);
