@@ -359,6 +359,163 @@ __global__ void __launch_bounds__(FT) k_mlp_forward_fused(const FusedNet fn, int
     }
 }
 
+// ---- fused forward on the 5th-generation tensor cores (tcgen05, accumulators in TMEM) ---------
+// A CTA takes TR = 128 rows through all layers. Shared memory holds the layer input (A, BF16,
+// 128 x K) and the layer's weights (B, BF16, N x K, k contiguous) in the no-swizzle K-major
+// core-matrix layout: 8 rows x 16 bytes per core matrix, the core matrices of an 8-row group
+// consecutive along K (leading byte offset 128), the 8-row groups K * 16 bytes apart (stride
+// byte offset). One thread issues K / 16 tcgen05.mma (M = 128, N = layer width, K = 16, BF16 x
+// BF16 -> FP32) into a TMEM accumulator of N columns and commits them to an mbarrier; the 16
+// warps then read the accumulator back (tcgen05.ld, warp w the TMEM lanes of its subpartition
+// w % 4 and a quarter of the columns), add the bias, apply GELU and write the BF16 result as the next
+// layer's A, while the next layer's weights stream into B with cp.async. The last layer writes
+// the de-normalised output. Every wait is bounded: a timeout sets g_mlp_tc_timeout and the CTA
+// still frees its TMEM.
+constexpr int TR = 128;                       // rows per CTA (the MMA's M)
+constexpr int TC_THREADS = 512;               // 16 warps: four per TMEM subpartition
+constexpr int TC_KMAX = 256;                  // widest layer input
+constexpr int TC_NMAX = 256;                  // widest layer output (TMEM columns)
+constexpr size_t TC_A_BYTES = size_t(TR) * TC_KMAX * 2;
+constexpr size_t TC_B_BYTES = size_t(TC_NMAX) * TC_KMAX * 2;
+constexpr size_t TC_SMEM = TC_A_BYTES + TC_B_BYTES + 64;
+__device__ int g_mlp_tc_timeout = 0;
+
+// byte offset of element (row r, k) in the no-swizzle K-major core-matrix layout with K columns
+__device__ __forceinline__ unsigned tc_off(int r, int k, int K) {
+    return unsigned((r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+// shared memory descriptor: start >> 4 (bits 0-13), leading byte offset >> 4 (16-29), stride
+// byte offset >> 4 (32-45), descriptor version 1 (bit 46), no swizzle (bits 61-63 zero)
+__device__ __forceinline__ unsigned long long tc_desc(unsigned saddr, unsigned lbo, unsigned sbo) {
+    return (unsigned long long)((saddr & 0x3FFFF) >> 4) | ((unsigned long long)(lbo >> 4) << 16) |
+           ((unsigned long long)(sbo >> 4) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B (bits 7-9
+// and 10-12 = 1), both K-major, N >> 3 (bits 17-22), M >> 4 (bits 24-28)
+__device__ __forceinline__ unsigned tc_idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (unsigned(n >> 3) << 17) | (unsigned(TR >> 4) << 24);
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_forward_tc(const FusedNet fn, int B, const float* __restrict__ x,
+                                                                  const bf16* __restrict__ wt, const float* __restrict__ p,
+                                                                  const float* __restrict__ nrm, float* __restrict__ y) {
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    unsigned char* As = tsm;
+    unsigned char* Bs = tsm + TC_A_BYTES;
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(tsm + TC_A_BYTES + TC_B_BYTES);
+    unsigned* tslot = reinterpret_cast<unsigned*>(tsm + TC_A_BYTES + TC_B_BYTES + 16);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int r0 = blockIdx.x * TR;
+    const int w0 = fn.w[0], wL = fn.w[fn.L];
+    const unsigned a_s = static_cast<unsigned>(__cvta_generic_to_shared(As));
+    const unsigned b_s = static_cast<unsigned>(__cvta_generic_to_shared(Bs));
+    const unsigned mb_s = static_cast<unsigned>(__cvta_generic_to_shared(mbar));
+    if (warp == 0) {
+        const unsigned slot = static_cast<unsigned>(__cvta_generic_to_shared(tslot));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(TC_NMAX));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb_s));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // the input rows, normalised, as the first A (columns up to kp[0] zero-padded)
+    {
+        const int kp = fn.kp[0];
+        for (int e = tid; e < TR * kp; e += TC_THREADS) {
+            const int r = e / kp, c = e % kp;
+            float v = 0.f;
+            if (c < w0 && r0 + r < B) v = (x[(long long)(r0 + r) * w0 + c] - nrm[c]) / nrm[w0 + c];
+            *reinterpret_cast<bf16*>(As + tc_off(r, c, kp)) = __float2bfloat16(v);
+        }
+    }
+    auto stage_weights = [&](int l) {
+        const int K = fn.kp[l], N = fn.w[l + 1];
+        const bf16* src = wt + fn.offWt[l];
+        const int per_row = K / 8;
+        for (int e = tid; e < N * per_row; e += TC_THREADS) {
+            const int n = e / per_row, c = e - n * per_row;
+            const unsigned dst = b_s + tc_off(n, c * 8, K);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src + size_t(e) * 8));
+        }
+    };
+    stage_weights(0);
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = *tslot;
+    unsigned phase = 0;
+    bool timed_out = false;
+    const float* mu = nrm + 2 * w0;
+    const float* sd = nrm + 2 * w0 + wL;
+    for (int l = 0; l < fn.L; ++l) {
+        const int K = fn.kp[l], N = fn.w[l + 1];
+        const bool last = l == fn.L - 1;
+        if (tid == 0) {
+            const unsigned idesc = tc_idesc(N);
+            for (int ks = 0; ks < K / 16; ++ks) {
+                const unsigned long long ad = tc_desc(a_s + ks * 256, 128, unsigned(K * 16));
+                const unsigned long long bd = tc_desc(b_s + ks * 256, 128, unsigned(K * 16));
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(ks));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb_s)
+                         : "memory");
+        }
+        // wait for the layer's products (bounded)
+        {
+            unsigned done = 0;
+            for (long long it = 0; it < (1LL << 26) && !done; ++it)
+                asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                             : "=r"(done) : "r"(mb_s), "r"(phase) : "memory");
+            if (!done) { timed_out = true; atomicExch(&g_mlp_tc_timeout, 1); }
+            phase ^= 1u;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (timed_out) break;
+        if (!last) stage_weights(l + 1);   // B is free: the products are done
+        // epilogue: warp w reads rows 32 (w % 4) .. + 31 of the accumulator, a quarter of the
+        // columns (N / 4 is a multiple of 8 when N is a multiple of 32; otherwise the last
+        // quarter is empty and the others take 8-column steps up to N)
+        const int sub = warp & 3;
+        const int r = sub * 32 + lane;
+        const int quarter = (N / 4 + 7) / 8 * 8;
+        const int cbeg = min((warp >> 2) * quarter, N), cend = min(cbeg + quarter, N);
+        const float* bias = p + fn.offb[l];
+        for (int c = cbeg; c < cend; c += 8) {
+            unsigned v[8];
+            const unsigned taddr = tmem + (unsigned(sub * 32) << 16) + unsigned(c);
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (!last) {
+                __align__(16) bf16 o[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) o[q] = __float2bfloat16(gelu(__uint_as_float(v[q]) + bias[c + q]));
+                *reinterpret_cast<uint4*>(As + tc_off(r, c, N)) = *reinterpret_cast<const uint4*>(o);
+            } else if (r0 + r < B) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const float z = __uint_as_float(v[q]) + bias[c + q];
+                    y[(long long)(r0 + r) * wL + c + q] = z * sd[c + q] + mu[c + q];
+                }
+            }
+        }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_NMAX));
+}
+
 }  // namespace
 
 struct bvp_mlp_s {
@@ -378,8 +535,10 @@ struct bvp_mlp_s {
     cudaStream_t stream = nullptr;
     long long step = 0;
     std::string err;
-    // fused inference (k_mlp_forward_fused) when every width fits it
+    // fused inference (k_mlp_forward_fused) when every width fits it; on request the tcgen05
+    // kernel (k_mlp_forward_tc) when, in addition, every layer width is a multiple of 16
     bool fused = false;
+    bool tc = false;
     FusedNet fn{};
     bf16* d_wt = nullptr;         // transposed BF16 weights, [N][Kp] per layer
     long long* d_offW = nullptr;
@@ -467,7 +626,9 @@ void refresh_wt(bvp_mlp* n) {
 
 // inference on device pointers: the fused kernel when the network fits it, else layer by layer
 void infer(bvp_mlp* n, int B, const float* d_x, float* d_y, cudaStream_t s) {
-    if (n->fused) {
+    if (n->tc) {
+        k_mlp_forward_tc<<<(B + TR - 1) / TR, TC_THREADS, TC_SMEM, s>>>(n->fn, B, d_x, n->d_wt, n->d_p, n->d_norm, d_y);
+    } else if (n->fused) {
         k_mlp_forward_fused<<<(B + FR - 1) / FR, FT, FUSED_SMEM, s>>>(n->fn, B, d_x, n->d_wt, n->d_p, n->d_norm, d_y);
     } else {
         cudaStream_t prev = n->stream;
@@ -518,7 +679,18 @@ bvp_status bvp_mlp_create(int32_t n_layers, const int32_t* widths, bvp_mlp** out
             ot += (long long)n->w[l + 1] * f.kp[l];
             f.offb[l] = n->offb[l];
         }
-        ok = cudaFuncSetAttribute(k_mlp_forward_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FUSED_SMEM)) ==
+        // the tcgen05 kernel on request (BVPGPU_MLP_TC=1): on the 3-256-256-256-128 surrogate
+        // it takes 52 us for 4096 rows against the mma.sync kernel's 30 us (32 CTAs of 128 rows
+        // against 128 CTAs of 32, each layer a dependent chain of weight staging, products and
+        // epilogue), so the mma.sync kernel stays the default
+        const char* env = std::getenv("BVPGPU_MLP_TC");
+        n->tc = env && env[0] == '1';
+        for (int l = 1; l <= n_layers; ++l) n->tc = n->tc && n->w[l] % 16 == 0 && n->w[l] >= 16;
+        if (n->tc)
+            ok = cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)) ==
+                 cudaSuccess;
+        ok = ok &&
+             cudaFuncSetAttribute(k_mlp_forward_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FUSED_SMEM)) ==
                  cudaSuccess &&
              cudaMalloc(&n->d_wt, ot * 2) == cudaSuccess && cudaMalloc(&n->d_offW, n_layers * 8) == cudaSuccess &&
              cudaMemcpy(n->d_offW, n->offW.data(), n_layers * 8, cudaMemcpyHostToDevice) == cudaSuccess;

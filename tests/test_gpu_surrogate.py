@@ -123,3 +123,38 @@ def test_surrogate_warm_start_cuts_newton_iterations(pkg, problems):
         assert nrm <= 1e-6 * (1 + 1e-6)
         err, dn = o.defect(tp[i], m, y)
         assert dn <= 1e-6 * (1 + 1e-3)
+
+
+@pytest.mark.parametrize("batch", [37, 4096, 9000])
+def test_tcgen05_forward_matches_the_mma_forward(pkg, batch, monkeypatch):
+    # the inference kernel on the 5th-generation tensor cores (tcgen05.mma into TMEM; widths
+    # multiples of 16; selected with BVPGPU_MLP_TC=1) against the default mma.sync kernel on the
+    # same network and inputs: the same BF16 operands, FP32 sums in another order (a hidden
+    # activation may round to the neighbouring BF16 value), and against the CPU restatement as
+    # the other forward tests are
+    import torch
+    widths = [3, 256, 256, 256, 128]
+    rng = np.random.default_rng(8)
+    net_mma = pkg.MLP(widths, seed=9)
+    monkeypatch.setenv("BVPGPU_MLP_TC", "1")
+    net_tc = pkg.MLP(widths, seed=9)
+    monkeypatch.delenv("BVPGPU_MLP_TC")
+    p = net_tc.get_params()
+    p += rng.normal(0, 0.05, p.size).astype(np.float32)
+    norm = _norm(widths, rng)
+    for net in (net_tc, net_mma):
+        net.set_params(p)
+        net.set_normalization(*norm)
+    x = rng.normal(0, 1, (batch, 3)).astype(np.float32)
+    dx = torch.tensor(x, device="cuda")
+    outs = []
+    for net in (net_tc, net_mma):
+        dy = torch.full((batch, 128), float("nan"), device="cuda")
+        net.forward_device(dx, dy, batch)
+        torch.cuda.synchronize()
+        outs.append(dy.cpu().numpy())
+    y_tc, y_mma = outs
+    assert np.isfinite(y_tc).all()
+    assert np.linalg.norm(y_tc - y_mma) <= 1e-2 * np.linalg.norm(y_mma)
+    y_ref, _, _ = mlp_ref.forward(p, widths, x, norm)
+    assert np.linalg.norm(y_tc - y_ref) <= 2e-2 * np.linalg.norm(y_ref)
