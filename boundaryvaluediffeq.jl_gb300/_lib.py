@@ -210,7 +210,7 @@ class Options(C.Structure):
                 ("divergence_factor", C.c_double), ("mirk6i", C.c_int32),
                 ("controller", C.c_int32), ("global_method", C.c_int32),
                 ("hybrid_de", C.c_double), ("hybrid_ge", C.c_double),
-                ("firk", C.c_int32), ("firk_stages", C.c_int32)]
+                ("firk", C.c_int32), ("firk_stages", C.c_int32), ("block_min", C.c_int32)]
 
 
 # bvp_controller and bvp_global_method

@@ -88,6 +88,12 @@ constexpr int FS = 1, FORDER = 1;
 constexpr double FTAU = 0.0, FC[1] = {1.0}, FB[1] = {1.0}, FA[1][1] = {{1.0}}, FQ[1][1] = {{1.0}};
 #endif
 constexpr bool FIRK = BVP_FIRK != 0;
+#ifndef BVP_POLISH_ONLY
+#define BVP_POLISH_ONLY 0
+#endif
+constexpr int GROUP_WARPS = 4;   // warps of a fused block (block mode: all of them on one instance)
+// block mode in the builds with the defect controller only
+constexpr bool GROUP_OK = !GLOBAL_CTL && !FIRK && !BVP_POLISH_ONLY;
 constexpr int FN = FS * M;          // stage unknowns of an interval
 constexpr int FXW = FN * (M + 1);   // its condensation record: J_K^-1 [J_y | R]
 
@@ -152,6 +158,7 @@ BVP_DEV int interval_of(const double* mesh, int N, double t) {
 }
 
 // ---- per-instance view -----------------------------------------------------------------
+struct GroupShared;
 struct Inst {
     int q, cap, N, cur;
     long long nb;          // node offset
@@ -161,6 +168,7 @@ struct Inst {
     int* iscr;
     JT* dns;               // per-warp shared memory for the separator system
     JT* trec;              // per-warp shared memory for the shuffle tree's elimination records (or null)
+    GroupShared* grp;      // block mode: the block's command area (null: the warp solves alone)
 };
 
 BVP_DEV double* mesh_of(const Args& a, const Inst& I, int b) { return a.mesh + b * a.tot + I.nb; }
@@ -468,18 +476,17 @@ BVP_DEV double bc_rows_lane0(const Args& a, const Inst& I, const R* pr, bool& ba
     return mx;
 }
 
-template <class R = double>
-BVP_DEV double residual(const Args& a, const Inst& I) {
-    const int lane = lane_id();
+// The intervals of group lane gl of GL (a warp's lanes, or a block's in block mode): its
+// largest |F| entry; a non-finite entry sets bad.
+template <class R, int GL>
+BVP_DEV double residual_part(const Args& a, const Inst& I, int gl, bool& bad) {
     const double* mesh = mesh_of(a, I, I.cur);
     const double* h = h_of(a, I, I.cur);
     const R* pr = params_as<R>(I);
-    double mx = 0.0;
     R mxr = R(0);
-    bool bad = false;
     const int nI = I.N - 1;
-    const int per = (nI + 31) >> 5;
-    const int i0 = lane * per;
+    const int per = (nI + GL - 1) / GL;
+    const int i0 = gl * per;
     const int i1 = min(i0 + per, nI);
     R node[M];
     if (NODE_SHARE && i0 < i1) {
@@ -537,9 +544,21 @@ BVP_DEV double residual(const Args& a, const Inst& I) {
             mxr = fmax(mxr, fabs(ri[m]));
         }
     }
-    mx = double(mxr);
+    return double(mxr);
+}
+
+BVP_DEV double group_phase(const Args& a, const Inst& I, int cmd, bool& bad);
+constexpr int CMD_EXIT = 0, CMD_RES32 = 1, CMD_RES64 = 2, CMD_DEFECT = 3;
+
+template <class R = double>
+BVP_DEV double residual(const Args& a, const Inst& I) {
+    const int lane = lane_id();
+    bool bad = false;
+    double mx;
+    if (GROUP_OK && I.grp) mx = group_phase(a, I, sizeof(R) == 8 ? CMD_RES64 : CMD_RES32, bad);
+    else mx = residual_part<R, 32>(a, I, lane, bad);
     __syncwarp();
-    if (lane == 0) mx = fmax(mx, bc_rows_lane0<R>(a, I, pr, bad));
+    if (lane == 0) mx = fmax(mx, bc_rows_lane0<R>(a, I, params_as<R>(I), bad));
     __syncwarp();
     mx = warp_max(mx);
     bad = warp_any(bad);
@@ -1422,8 +1441,8 @@ BVP_DEV bool newton(const Args& a, Inst& I, InstState& s) {
 }
 
 // ---- K4: defect estimate (adaptivity.jl:416-461) -------------------------------------------
-BVP_DEV double defect(const Args& a, const Inst& I) {
-    const int lane = lane_id();
+template <int GL>
+BVP_DEV double defect_part(const Args& a, const Inst& I, int gl, bool& bad) {
     const double* mesh = mesh_of(a, I, I.cur);
     const double* h = h_of(a, I, I.cur);
     const double* y = y_of(a, I, I.cur);
@@ -1431,8 +1450,7 @@ BVP_DEV double defect(const Args& a, const Inst& I) {
     interp_weights<double>(tau_star(), w1, w1p);
     interp_weights<double>(1.0 - tau_star(), w2, w2p);
     double dn = 0.0;
-    bool bad = false;
-    for (int i = lane; i < I.N - 1; i += 32) {
+    for (int i = gl; i < I.N - 1; i += GL) {
         double yi[M], yi1[M], Ki[S * M], KIi[NSXA * M];
 #pragma unroll
         for (int m = 0; m < M; ++m) { yi[m] = y[i * M + m]; yi1[m] = y[(i + 1) * M + m]; }
@@ -1470,9 +1488,81 @@ BVP_DEV double defect(const Args& a, const Inst& I) {
         bad |= isnan(ei);
         dn = fmax(dn, ei);
     }
+    return dn;
+}
+
+BVP_DEV double defect(const Args& a, const Inst& I) {
+    bool bad = false;
+    double dn;
+    if (GROUP_OK && I.grp) dn = group_phase(a, I, CMD_DEFECT, bad);
+    else dn = defect_part<32>(a, I, lane_id(), bad);
     __syncwarp();
     dn = warp_max(dn);
     return warp_any(bad) ? dinf() : dn;
+}
+
+// ---- block mode ------------------------------------------------------------------------------
+// A long mesh is solved by a whole block: its first warp runs the solve and the other warps
+// join it for the phases that are independent per interval (the residuals and the defect,
+// most of a long mesh's time), each lane of the block taking its share of the intervals. The
+// warps meet at a named barrier of the block's 128 threads; the leader posts a command and
+// the instance, every warp runs its part and leaves its largest value, and the leader
+// combines them. The parts are the warp code's with 128 lanes instead of 32, and each
+// interval's values do not depend on which lane computes them, so the results are the same
+// as the warp's.
+struct GroupShared {
+    Inst inst;
+    int cmd;
+    int bad[GROUP_WARPS];
+    double red[GROUP_WARPS];
+};
+BVP_DEV void group_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+__device__ __noinline__ double group_part(const Args& a, const Inst& I, int cmd, int gl, int* bad_out) {
+    bool bad = false;
+    double v = 0.0;
+    if (cmd == CMD_RES64) {
+        v = residual_part<double, 32 * GROUP_WARPS>(a, I, gl, bad);
+    } else if (cmd == CMD_RES32) {
+        if constexpr (F32_PHASE_OK) v = residual_part<float, 32 * GROUP_WARPS>(a, I, gl, bad);
+    } else {
+        v = defect_part<32 * GROUP_WARPS>(a, I, gl, bad);
+    }
+    *bad_out = bad ? 1 : 0;
+    return v;
+}
+
+// the leader's side: post, run its own part, collect (every lane gets the block's result)
+BVP_DEV double group_phase(const Args& a, const Inst& I, int cmd, bool& bad) {
+    GroupShared* g = I.grp;
+    const int lane = lane_id();
+    if (lane == 0) { g->inst = I; g->cmd = cmd; }
+    group_bar();
+    int b = 0;
+    double v = warp_max(group_part(a, I, cmd, lane, &b));
+    const bool wb = warp_any(b != 0);
+    if (lane == 0) { g->red[0] = v; g->bad[0] = wb ? 1 : 0; }
+    group_bar();
+#pragma unroll
+    for (int w = 1; w < GROUP_WARPS; ++w) { v = fmax(v, g->red[w]); bad |= g->bad[w] != 0; }
+    bad |= wb;
+    return v;
+}
+
+// the other warps' side, until the leader posts CMD_EXIT
+BVP_DEV void group_helper(const Args& a, GroupShared* g, int w) {
+    const int lane = lane_id();
+    while (true) {
+        group_bar();
+        const int cmd = g->cmd;
+        if (cmd == CMD_EXIT) break;
+        const Inst I = g->inst;
+        int b = 0;
+        const double v = warp_max(group_part(a, I, cmd, w * 32 + lane, &b));
+        const bool wb = warp_any(b != 0);
+        if (lane == 0) { g->red[w] = v; g->bad[w] = wb ? 1 : 0; }
+        group_bar();
+    }
 }
 
 // ---- mesh selection (adaptivity.jl:23-75, 250-304) -------------------------------------------
@@ -2069,6 +2159,7 @@ BVP_DEV Inst make_inst(const Args& a, int q) {
     I.iscr = a.iscr + (long long)q * ISCRW;
     I.dns = nullptr;
     I.trec = nullptr;
+    I.grp = nullptr;
     I.N = 0;
     I.cur = 0;
     return I;
@@ -2082,7 +2173,7 @@ BVP_DEV Inst make_inst(const Args& a, int q) {
 // Per-warp scratch in shared memory when it fits (it is read back right after being
 // written, by other lanes of the warp); otherwise the global scratch arrays.
 namespace bvp {
-constexpr int WARPS_PER_BLOCK = 4;
+constexpr int WARPS_PER_BLOCK = GROUP_WARPS;
 constexpr bool SCR_SMEM = WARPS_PER_BLOCK * (SCRW * 8 + ISCRW * 4) <= 40 * 1024;
 constexpr int SM_SCRW = SCR_SMEM ? SCRW : 1;
 constexpr int SM_ISCRW = SCR_SMEM ? ISCRW : 1;
@@ -2095,17 +2186,53 @@ BVP_DEV void fused_body(const Args& a) {
     __shared__ int s_iscr[WARPS_PER_BLOCK][SM_ISCRW];
     __shared__ JT s_dns[WARPS_PER_BLOCK][SM_DNS];
     __shared__ JT s_trec[WARPS_PER_BLOCK][SM_TREC];
+    __shared__ GroupShared s_grp;
+    __shared__ int s_item;
     const int lane = lane_id();
     const int w = threadIdx.x >> 5;
+    // block mode first: the first n_group positions of the order (the long meshes, as bvp_prep
+    // placed them), one per block at a time from the second counter
+    const int n_group = GROUP_OK ? a.work_counter[5] : 0;
+    bool block_mode = GROUP_OK && n_group > 0;
+    // warp mode. The static deal (blocks b and b + S share an SM when the grid fills S SMs a
+    // block at a time) only when every warp starts together, without block-mode work
+    const bool deal = a.deal_sms > 0 && n_group == 0;
+    int k_first = -1;
+    if (deal) {
+        const int S = a.deal_sms, sm = int(blockIdx.x) % S, j = (int(blockIdx.x) / S) * WARPS_PER_BLOCK + w;
+        k_first = j * S + ((j & 1) ? S - 1 - sm : sm);
+    }
     while (true) {
-        int k = 0;
-        if (lane == 0) k = atomicAdd(a.work_counter, 1);
-        k = __shfl_sync(FULL, k, 0);
-        if (k >= a.n_inst) break;
+        int k = -1;
+        if (GROUP_OK && block_mode) {
+            if (threadIdx.x == 0) s_item = atomicAdd(a.work_counter + 4, 1);
+            group_bar();
+            const int gi = s_item;
+            if (gi >= n_group) {
+                block_mode = false;
+            } else if (w != 0) {
+                group_helper(a, &s_grp, w);
+                continue;
+            } else {
+                k = gi;
+            }
+        }
+        const bool grp = k >= 0;
+        if (!grp) {
+            k = k_first;
+            k_first = -1;
+            if (k < 0) {
+                if (lane == 0)
+                    k = n_group + atomicAdd(a.work_counter, 1) + (deal ? WARPS_PER_BLOCK * int(gridDim.x) : 0);
+                k = __shfl_sync(FULL, k, 0);
+            }
+            if (k >= a.n_inst) break;
+        }
         Inst I = make_inst(a, a.order[k]);
         if (SCR_SMEM) { I.scr = s_scr[w]; I.iscr = s_iscr[w]; }
         I.dns = s_dns[w];
         if (TREC_SMEM) I.trec = s_trec[w];
+        if (GROUP_OK && grp) I.grp = &s_grp;
         if (GLOBAL_CTL && a.phase == 2) {
             polish_instance(a, I);
             continue;
@@ -2117,6 +2244,11 @@ BVP_DEV void fused_body(const Args& a) {
         solve_instance(a, I);
 #endif
         if (a.inst_cost && lane == 0) a.inst_cost[I.q] = float(clock64() - c0) * (1.0f / 2000.0f);
+        if (GROUP_OK && grp) {
+            // release the helpers
+            if (lane == 0) s_grp.cmd = CMD_EXIT;
+            group_bar();
+        }
     }
 }
 }  // namespace bvp
@@ -2317,14 +2449,16 @@ extern "C" __global__ void bvp_convert_params(const double* p, bvp::JT* pj, long
 // batch: about 11% less time than largest-first).
 extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_init, int max_sub, int cap_scale,
                                                             int* cap, long long* node_off, int* order, int* counter,
-                                                            const float* cost_tab) {
-    constexpr int NB = 4096;
-    __shared__ int hist[NB];
+                                                            const float* cost_tab, int group_min) {
+    constexpr int NB = 4096;            // sort keys of one class
+    constexpr int NB2 = 2 * NB;         // block-mode instances' keys first, then the others'
+    __shared__ int hist[NB2];
     __shared__ long long wsum[32];
     __shared__ long long carry;
+    __shared__ int n_group;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int k = tid; k < NB; k += blockDim.x) hist[k] = 0;
-    if (tid == 0) { carry = 0; *counter = 0; }
+    for (int k = tid; k < NB2; k += blockDim.x) hist[k] = 0;
+    if (tid == 0) { carry = 0; n_group = 0; counter[0] = 0; counter[4] = 0; }
     __syncthreads();
     for (int base = 0; base < n; base += blockDim.x) {
         const int q = base + tid;
@@ -2370,12 +2504,23 @@ extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_
         }
         return ni < NB - 1 ? ni : NB - 1;
     };
-    for (int q = tid; q < n; q += blockDim.x) atomicAdd(&hist[key_of(q)], 1);
+    // block mode (group_min > 0): meshes of at least group_min intervals, sorted among
+    // themselves the same way, ahead of the others; their count goes to counter[5]
+    auto key2_of = [&](int q) {
+        const bool grp = group_min > 0 && n_init[q] >= group_min;
+        return (grp ? 0 : NB) + key_of(q);
+    };
+    for (int q = tid; q < n; q += blockDim.x) {
+        const int k2 = key2_of(q);
+        atomicAdd(&hist[k2], 1);
+        if (k2 < NB) atomicAdd(&n_group, 1);
+    }
     __syncthreads();
+    if (tid == 0) counter[5] = n_group;
     {
-        // exclusive scan of the histogram by the whole block: each thread a run of NB / 1024
+        // exclusive scan of the histogram by the whole block: each thread a run of NB2 / 1024
         // bins, a warp scan of the run sums, then the warps' totals
-        constexpr int PER = NB / 1024;
+        constexpr int PER = NB2 / 1024;
         int v[PER];
         int s = 0;
 #pragma unroll
@@ -2405,7 +2550,7 @@ extern "C" __global__ void __launch_bounds__(1024) bvp_prep(int n, const int* n_
     }
     __syncthreads();
     for (int q = tid; q < n; q += blockDim.x) {
-        const int pos = atomicAdd(&hist[key_of(q)], 1);
+        const int pos = atomicAdd(&hist[key2_of(q)], 1);
         order[pos] = q;
     }
 }

@@ -36,6 +36,13 @@ struct BvpArgs {
     bvp_i64 tot;                   // total node capacity (sum over instances)
     const int* order;              // work order (instance ids, coarsest initial mesh first)
     int* work_counter;
+    int deal_sms;                  // > 0: the grid is that many SMs times the resident blocks per
+                                   // SM, and each warp's first position of the order is dealt
+                                   // statically, round j (the warp's index among its SM's warps)
+                                   // taking positions j S .. j S + S - 1 over the SMs in a snake,
+                                   // so the longest solves start spread over the SMs; the counter
+                                   // deals the positions from 4 * gridDim.x on. 0: every position
+                                   // comes from the counter
     const double* params;          // n_inst x n_params
     const BVP_JT_PTR* params_j;    // same, in the Jacobian precision
     const int* n_init;             // initial interval counts

@@ -67,6 +67,8 @@ struct bvp_handle_s {
     // through the three (an untimed first launch, then two timed solves each) and the handle
     // keeps the fastest
     cudaKernel_t k_fused_v[3] = {nullptr, nullptr, nullptr};
+    int occ_v[3] = {4, 3, 2}, occ_hi = 3;   // resident blocks per SM of each fused kernel
+    int group_min = 0;   // meshes of at least this many intervals are solved in block mode (0: none)
     int fused_pick = 1;
     struct {
         long long key = -1;
@@ -295,6 +297,21 @@ static bvp_status build_cubin(bvp_handle* h, int order, int mirk6i, int global_c
     return BVP_OK;
 }
 
+// Meshes of at least this many initial intervals are solved by a whole block (block mode:
+// the residuals and defects over 128 lanes) unless bvp_options.block_min says otherwise.
+static constexpr int kGroupMinDefault = 1024;
+
+// Resident 128-thread blocks per SM of a loaded kernel (registers and shared memory), or the
+// fallback when the runtime cannot say.
+static int kernel_occupancy(cudaKernel_t k, int fallback) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k, 128, 0) != cudaSuccess || nb <= 0) {
+        (void)cudaGetLastError();
+        return fallback;
+    }
+    return nb;
+}
+
 static bvp_status compile_and_load(bvp_handle* h) {
     const bool large = h->desc.M > 8;
     std::vector<char> cubin;
@@ -329,6 +346,10 @@ static bvp_status compile_and_load(bvp_handle* h) {
         CU(cudaLibraryGetKernel(&h->k_fused_v[1], h->lib, "bvp_solve_fused_b3"));
         CU(cudaLibraryGetKernel(&h->k_fused_v[2], h->lib, "bvp_solve_fused_b2"));
     }
+    for (int v = 0; v < 3; ++v) h->occ_v[v] = kernel_occupancy(h->k_fused_v[v], h->occ_v[v]);
+    // block mode for long meshes, in the defect-controlled MIRK build
+    if (!h->glob && !h->firk)
+        h->group_min = h->opt.block_min == 0 ? kGroupMinDefault : std::max(0, h->opt.block_min);
     if (!h->firk) CU(cudaLibraryGetKernel(&h->k_stage, h->lib, "bvp_stage"));
     CU(cudaLibraryGetKernel(&h->k_pack, h->lib, "bvp_pack"));
     CU(cudaLibraryGetKernel(&h->k_offsets, h->lib, "bvp_out_offsets"));
@@ -345,6 +366,7 @@ static bvp_status compile_and_load(bvp_handle* h) {
         CU(cudaLibraryLoadData(&h->lib_hi, cubin_hi.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
         CU(cudaLibraryGetKernel(&h->k_fused_hi, h->lib_hi, "bvp_solve_fused"));
         CU(cudaLibraryGetKernel(&h->k_probe_hi, h->lib_hi, "bvp_layout_probe"));
+        h->occ_hi = kernel_occupancy(h->k_fused_hi, h->occ_hi);
     }
     return BVP_OK;
 }
@@ -502,7 +524,7 @@ static bvp_status ensure_arena(bvp_handle* h, long long tot, int n, long long y0
               ensure_dev(h->d_iscr, size_t(n) * L.ISCRW * 4) &&
               ensure_dev(h->d_st, size_t(n) * sizeof(BvpInstState)) && ensure_dev(h->d_order, size_t(n) * 4) &&
               ensure_dev(h->d_cap, size_t(n) * 4) && ensure_dev(h->d_node_off, size_t(n) * 8) &&
-              ensure_dev(h->d_counter, 16) &&
+              ensure_dev(h->d_counter, 32) &&
               ensure_dev(h->d_params, size_t(n) * std::max(1, h->desc.n_params) * 8) &&
               ensure_dev(h->d_params_j, size_t(n) * std::max(1, h->desc.n_params) * js) &&
               ensure_dev(h->d_n_init, size_t(n) * 4) && ensure_dev(h->d_tspans, size_t(n) * 16) &&
@@ -542,6 +564,7 @@ static void fill_args(bvp_handle* h, BvpArgs& a, int n, long long tot, int y0_mo
     a.tot = tot;
     a.order = static_cast<const int*>(h->d_order.p);
     a.work_counter = static_cast<int*>(h->d_counter.p);
+    a.deal_sms = 0;
     a.params = d_params;
     a.params_j = h->d_params_j.p;
     a.n_init = d_n_init;
@@ -590,6 +613,15 @@ static void fill_args(bvp_handle* h, BvpArgs& a, int n, long long tot, int y0_mo
 static int cap_scale(const bvp_handle* h) { return (h->glob && h->opt.global_method == BVP_GLOBAL_RE) ? 2 : 1; }
 static long long cap_nodes(const bvp_handle* h, long long ni) {
     return cap_scale(h) * std::max<long long>(ni, h->opt.max_subintervals) + 1;
+}
+
+// A fused kernel's grid for the static deal (BvpArgs::deal_sms): a whole number of blocks per
+// SM, no more than the SMs hold at once (so every block starts together), and no more rounds
+// of blocks than the batch fills.
+static int resident_grid(bvp_handle* h, int n, int occ) {
+    const int sms = std::max(1, h->sm_count);
+    const int rounds = std::max(1, std::min(std::max(1, occ), (n + 4 * sms - 1) / (4 * sms)));
+    return rounds * sms;
 }
 
 static int fused_grid(bvp_handle* h, int n) {
@@ -669,7 +701,8 @@ static bvp_status ho_rounds(bvp_handle* h, const BvpArgs& a0, int n) {
         CU(cudaMemsetAsync(a0.work_counter, 0, sizeof(int), h->stream));
         {
             void* args[] = {&a2};
-            CU(cudaLaunchKernel((const void*)h->k_fused_hi, dim3(fused_grid(h, c)), dim3(128), args, 0, h->stream));
+            CU(cudaLaunchKernel((const void*)h->k_fused_hi, dim3(resident_grid(h, c, h->occ_hi)), dim3(128), args, 0,
+                                h->stream));
         }
         BvpArgs a1 = a0;
         a1.phase = 1;
@@ -682,8 +715,8 @@ static bvp_status ho_rounds(bvp_handle* h, const BvpArgs& a0, int n) {
         CU(cudaMemsetAsync(a1.pause_count, 0, sizeof(int), h->stream));
         {
             void* args[] = {&a1};
-            CU(cudaLaunchKernel((const void*)h->k_fused_v[h->fused_pick], dim3(fused_grid(h, c)), dim3(128), args, 0,
-                                h->stream));
+            CU(cudaLaunchKernel((const void*)h->k_fused_v[h->fused_pick],
+                                dim3(resident_grid(h, c, h->occ_v[h->fused_pick])), dim3(128), args, 0, h->stream));
         }
         cur ^= 1;
     }
@@ -732,16 +765,19 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
         int* ord = static_cast<int*>(h->d_order.p);
         int* ctr = static_cast<int*>(h->d_counter.p);
         const float* tab = h->have_tab ? static_cast<const float*>(h->d_cost_tab.p) : nullptr;
-        void* args[] = {&nn, &ni, &ms, &cs, &cap, &off, &ord, &ctr, &tab};
+        int gm = h->group_min;
+        void* args[] = {&nn, &ni, &ms, &cs, &cap, &off, &ord, &ctr, &tab, &gm};
         CU(cudaLaunchKernel((const void*)h->k_prep, dim3(1), dim3(1024), args, 0, h->stream));
     }
     if (wait_side) CU(cudaStreamWaitEvent(h->stream, h->ev_side, 0));   // the guesses on the grid
     const int var = fused_variant(h, n, y0_mode);
     CU(cudaEventRecord(h->ev[1], h->stream));
     if (h->ho) CU(cudaMemsetAsync(a.pause_count, 0, 2 * sizeof(int), h->stream));
+    a.deal_sms = std::max(1, h->sm_count);
     {
         void* args[] = {&a};
-        CU(cudaLaunchKernel((const void*)h->k_fused_v[var], dim3(fused_grid(h, n)), dim3(128), args, 0, h->stream));
+        CU(cudaLaunchKernel((const void*)h->k_fused_v[var], dim3(resident_grid(h, n, h->occ_v[var])), dim3(128), args,
+                            0, h->stream));
     }
     if (h->ho) {
         bvp_status s = ho_rounds(h, a, n);

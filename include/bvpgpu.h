@@ -85,6 +85,12 @@ typedef struct {
                                      M <= 8, standard BCs at the tspan's ends or two-point BCs, no
                                      singular term and no stage output */
     int32_t firk_stages;
+    int32_t block_min;            /* meshes of at least this many initial intervals are solved by a
+                                     whole 128-thread block instead of one warp: the residuals and
+                                     the defect spread over 128 lanes, the rest of the solve on the
+                                     block's first warp; the results are the same. 0: the library's
+                                     threshold (1024 intervals); -1: never. The defect-controlled
+                                     MIRK path only (M <= 8) */
 } bvp_options;
 
 /* Error controllers (lib/BoundaryValueDiffEqCore/src/calc_errors.jl:54-139, the error
