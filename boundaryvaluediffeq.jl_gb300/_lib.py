@@ -87,11 +87,12 @@ def _nvrtc():
 
 
 def nvrtc_check(problem, order: int, jac_bits: int = 32, mirk6i: int = 0, global_ctl: int = 0,
-                firk_stages: int = 0) -> None:
+                firk_stages: int = 0, block_mode: int = 0) -> None:
     """Compile the problem's kernels with NVRTC exactly as bvp_create does (same source
     assembly and options, no GPU needed; global_ctl: the build with the error controllers other
     than DefectControl; firk_stages: the FIRK path's build for that many stages, with
-    placeholder coefficients); raises with the NVRTC log on failure."""
+    placeholder coefficients; block_mode: the block-mode module for long meshes); raises with the
+    NVRTC log on failure."""
     lib = _nvrtc()
     if lib is None:
         return
@@ -106,6 +107,8 @@ def nvrtc_check(problem, order: int, jac_bits: int = 32, mirk6i: int = 0, global
                   f"constexpr double FC[{s}] = {row};\nconstexpr double FB[{s}] = {row};\n"
                   f"constexpr double FA[{s}][{s}] = {{{', '.join([row] * s)}}};\n"
                   f"constexpr double FQ[{s}][{s}] = {{{', '.join([row] * s)}}};\n}}\n")
+    if block_mode:
+        prefix += "#define BVP_BLOCK_MODE 1\n"
     src = ("#include \"bvp_prelude.cuh\"\n" + prefix + "#line 1 \"problem_source\"\n" + problem.source +
            ("\n#include \"bvp_large.cuh\"\n" if large else "\n#include \"bvp_kernels.cuh\"\n"))
     opts = ["--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true", f"-DBVP_M={problem.M}",

@@ -91,9 +91,13 @@ constexpr bool FIRK = BVP_FIRK != 0;
 #ifndef BVP_POLISH_ONLY
 #define BVP_POLISH_ONLY 0
 #endif
+#ifndef BVP_BLOCK_MODE
+#define BVP_BLOCK_MODE 0
+#endif
 constexpr int GROUP_WARPS = 4;   // warps of a fused block (block mode: all of them on one instance)
-// block mode in the builds with the defect controller only
-constexpr bool GROUP_OK = !GLOBAL_CTL && !FIRK && !BVP_POLISH_ONLY;
+// block mode: compiled into a module of its own (BVP_BLOCK_MODE), which the host loads for
+// batches with long meshes, so that the warp-only kernels keep their code; defect control only
+constexpr bool GROUP_OK = BVP_BLOCK_MODE && !GLOBAL_CTL && !FIRK && !BVP_POLISH_ONLY;
 constexpr int FN = FS * M;          // stage unknowns of an interval
 constexpr int FXW = FN * (M + 1);   // its condensation record: J_K^-1 [J_y | R]
 
@@ -956,6 +960,96 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
     return true;
 }
 
+// The same elimination with each lane's row in registers (separator systems of at most 16
+// unknowns). Rows are not moved: each lane tracks its row's position, and the pivot search, the
+// row swap, the update order and every operation are those of separator_solve_warp, so the
+// results are the same; a column is broadcast from the pivot lane by a shuffle, and entries at a
+// run-time column are picked by unrolled selects instead of indexed loads.
+constexpr bool SEP_REG = NDENSE <= 16;
+template <class T> BVP_DEV T pick(const T (&r)[NDENSE], int c) {
+    T v = T(0);
+#pragma unroll
+    for (int cc = 0; cc < NDENSE; ++cc) v = cc == c ? r[cc] : v;
+    return v;
+}
+BVP_DEV bool separator_solve_reg(const Args& a, const Inst& I, int nk) {
+    const int lane = lane_id();
+    const int n = nk * M;
+    const int row0 = (nk - 1) * M;
+    JT ar[NDENSE], b = JT(0);
+#pragma unroll
+    for (int cc = 0; cc < NDENSE; ++cc) ar[cc] = JT(0);
+    if (lane < row0) {
+        // segment relation j: A δ_{kept j} + B δ_{kept j+1} = g
+        const int j = lane / M, r = lane - j * M;
+        const JT* seg = seg_of(I, j);
+#pragma unroll
+        for (int cc = 0; cc < NDENSE; ++cc) {
+            const int cA = cc - j * M, cB = cc - (j + 1) * M;
+            if (cA >= 0 && cA < M) ar[cc] = seg[r * M + cA];
+            else if (cB >= 0 && cB < M) ar[cc] = seg[M * M + r * M + cB];
+        }
+        b = seg[2 * M * M + r];
+    } else if (lane < n) {
+        // BC row r: every BC contribution's block, added at its separator's columns
+        const int r = lane - row0;
+        const int nb = I.iscr[ISCR_NB];
+#pragma unroll 1
+        for (int k = 0; k < nb; ++k) {
+            const int node = I.iscr[ISCR_BNODE + k];
+            int kj = 0;
+            while (kj < nk - 1 && I.iscr[ISCR_KEPT + kj] != node) ++kj;
+            const double* G = I.scr + SCR_BCBLK + k * M * M + r * M;
+#pragma unroll
+            for (int cc = 0; cc < NDENSE; ++cc) {
+                const int c = cc - kj * M;
+                if (c >= 0 && c < M) ar[cc] += JT(G[c]);
+            }
+        }
+        b = JT(-I.scr[SCR_BCRES + r]);
+    }
+    int pos = lane;   // the position of this lane's row
+#pragma unroll 1
+    for (int k = 0; k < n; ++k) {
+        // pivot: the largest |A[p][k]| over positions p >= k, the lowest position on a tie
+        JT v = (lane < n && pos >= k) ? fabs(pick(ar, k)) : JT(-1);
+        int pp = pos;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const JT v2 = __shfl_xor_sync(FULL, v, o);
+            const int p2 = __shfl_xor_sync(FULL, pp, o);
+            if (v2 > v || (v2 == v && p2 < pp)) { v = v2; pp = p2; }
+        }
+        if (!(v > JT(0)) || !isfinite(v)) return false;   // uniform across the warp
+        const int pl = __ffs(__ballot_sync(FULL, lane < n && pos == pp)) - 1;   // the pivot row's lane
+        if (pp != k && pos == k) pos = pp;   // the row at position k moves to the pivot's place
+        if (lane == pl) pos = k;
+        const JT pk = __shfl_sync(FULL, pick(ar, k), pl);
+        const bool upd = lane < n && pos > k;
+        const JT mlt = pick(ar, k) * (JT(1) / pk);
+#pragma unroll
+        for (int cc = 0; cc < NDENSE; ++cc) {
+            const JT pv = __shfl_sync(FULL, ar[cc], pl);
+            if (upd && cc > k && cc < n) ar[cc] -= mlt * pv;
+        }
+        const JT pb = __shfl_sync(FULL, b, pl);
+        if (upd) b -= mlt * pb;
+    }
+#pragma unroll 1
+    for (int k = n - 1; k >= 0; --k) {
+        const int pl = __ffs(__ballot_sync(FULL, lane < n && pos == k)) - 1;
+        if (lane == pl) b = b / pick(ar, k);
+        const JT xk = __shfl_sync(FULL, b, pl);
+        if (lane < n && pos < k) b -= pick(ar, k) * xk;
+    }
+    if (lane < n) {
+        I.dns[pos * DLD + n] = b;
+        a.delta[(I.nb + I.iscr[ISCR_KEPT + pos / M]) * M + pos % M] = b;
+    }
+    __syncwarp();
+    return true;
+}
+
 #ifndef BVP_TREE_UNROLL
 #define BVP_TREE_UNROLL 1
 #endif
@@ -1172,7 +1266,9 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     __syncwarp();
     // 3. separator system
     int dense_ok = 1;
-    if constexpr (SMEM_DENSE) {
+    if constexpr (SEP_REG) {
+        dense_ok = separator_solve_reg(a, I, nk) ? 1 : 0;
+    } else if constexpr (SMEM_DENSE) {
         dense_ok = separator_solve_warp(a, I, nk) ? 1 : 0;
     } else if (lane == 0) {
         // in thread-local storage (L1-resident), not the global scratch: the elimination
@@ -1516,7 +1612,12 @@ struct GroupShared {
     int bad[GROUP_WARPS];
     double red[GROUP_WARPS];
 };
-BVP_DEV void group_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+// bar.sync is warp-aligned: a warp that reached it in pieces (after a lane-0 store) could
+// count twice, so the warp reconverges first
+BVP_DEV void group_bar() {
+    __syncwarp();
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+}
 
 __device__ __noinline__ double group_part(const Args& a, const Inst& I, int cmd, int gl, int* bad_out) {
     bool bad = false;
@@ -2263,6 +2364,10 @@ BVP_DEV void fused_body(const Args& a) {
 // module that only runs HOErrorControl's MIRK(p+2) solves (BVP_POLISH_ONLY) has nothing else.
 #if BVP_GLOBAL_CTL || BVP_FIRK
 extern "C" __global__ void __launch_bounds__(128, 3) bvp_solve_fused(const bvp::Args a) { bvp::fused_body(a); }
+#elif BVP_BLOCK_MODE
+// the block-mode module: one launch shape, 2 blocks per SM (the fastest of the three on the
+// long meshes it is for)
+extern "C" __global__ void __launch_bounds__(128, 2) bvp_solve_fused(const bvp::Args a) { bvp::fused_body(a); }
 #else
 extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::Args a) { bvp::fused_body(a); }
 extern "C" __global__ void __launch_bounds__(128, 3) bvp_solve_fused_b3(const bvp::Args a) { bvp::fused_body(a); }
@@ -2271,7 +2376,7 @@ extern "C" __global__ void __launch_bounds__(128, 2) bvp_solve_fused_b2(const bv
 #ifndef BVP_POLISH_ONLY
 #define BVP_POLISH_ONLY 0
 #endif
-#if !BVP_POLISH_ONLY && !BVP_FIRK
+#if !BVP_POLISH_ONLY && !BVP_FIRK && !BVP_BLOCK_MODE
 
 // Stage kernels on caller-provided (mesh, y) in buffer 0 with N = st[q].N. Used by the
 // per-kernel parity tests; stage: 0 residual (F, K, BC residual), 1 Jacobian blocks,
@@ -2312,7 +2417,7 @@ extern "C" __global__ void __launch_bounds__(128) bvp_stage(const bvp::Args a, i
         __syncwarp();
     }
 }
-#endif  // !BVP_POLISH_ONLY && !BVP_FIRK
+#endif  // !BVP_POLISH_ONLY && !BVP_FIRK && !BVP_BLOCK_MODE
 
 // Copy the results of every instance (buffer 0) into packed host-bound arrays.
 // out_off has n_inst + 1 entries (bvp_out_offsets); the outputs hold cap points: a batch
@@ -2382,7 +2487,7 @@ extern "C" __global__ void __launch_bounds__(1024) bvp_out_offsets(int n, const 
     if (tid == 0) { d_off[n] = carry; h_off[n] = carry; }
 }
 
-#if !BVP_POLISH_ONLY && !BVP_FIRK
+#if !BVP_POLISH_ONLY && !BVP_FIRK && !BVP_BLOCK_MODE
 
 // Dense output of the last solve (needs want_stages): u(t) or u'(t) at nq query times per
 // instance through the MIRK interpolant (interpolation.jl:17-204: interval(mesh, t),
@@ -2421,7 +2526,7 @@ extern "C" __global__ void bvp_dense(const bvp::Args a, int nq, const double* tq
 }
 
 // Device-side layout constants, checked against the host's at handle creation.
-#endif  // !BVP_POLISH_ONLY && !BVP_FIRK
+#endif  // !BVP_POLISH_ONLY && !BVP_FIRK && !BVP_BLOCK_MODE
 
 extern "C" __global__ void bvp_layout_probe(int* out) {
     out[0] = bvp::SCRW;

@@ -69,6 +69,10 @@ struct bvp_handle_s {
     cudaKernel_t k_fused_v[3] = {nullptr, nullptr, nullptr};
     int occ_v[3] = {4, 3, 2}, occ_hi = 3;   // resident blocks per SM of each fused kernel
     int group_min = 0;   // meshes of at least this many intervals are solved in block mode (0: none)
+    // the block-mode module (BVP_BLOCK_MODE), built on the first batch that has a long mesh
+    cudaLibrary_t lib_blk = nullptr;
+    cudaKernel_t k_fused_blk = nullptr;
+    int occ_blk = 2;
     int fused_pick = 1;
     struct {
         long long key = -1;
@@ -299,7 +303,7 @@ static bvp_status build_cubin(bvp_handle* h, int order, int mirk6i, int global_c
 
 // Meshes of at least this many initial intervals are solved by a whole block (block mode:
 // the residuals and defects over 128 lanes) unless bvp_options.block_min says otherwise.
-static constexpr int kGroupMinDefault = 1024;
+static constexpr int kGroupMinDefault = 512;
 
 // Resident 128-thread blocks per SM of a loaded kernel (registers and shared memory), or the
 // fallback when the runtime cannot say.
@@ -723,10 +727,29 @@ static bvp_status ho_rounds(bvp_handle* h, const BvpArgs& a0, int n) {
     return fail(h, BVP_ERR_STATE, "HOErrorControl rounds did not end");
 }
 
+// The block-mode module: the same sources with BVP_BLOCK_MODE, one fused kernel. Built (or read
+// from the cubin cache) when a batch first has a mesh of group_min intervals or more.
+static bvp_status ensure_block_module(bvp_handle* h) {
+    if (h->k_fused_blk) return BVP_OK;
+    std::vector<char> cubin;
+    bvp_status bs = build_cubin(h, h->opt.order, h->opt.mirk6i, 0, cubin, "#define BVP_BLOCK_MODE 1\n");
+    if (bs != BVP_OK) return bs;
+    CU(cudaLibraryLoadData(&h->lib_blk, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+    CU(cudaLibraryGetKernel(&h->k_fused_blk, h->lib_blk, "bvp_solve_fused"));
+    h->occ_blk = kernel_occupancy(h->k_fused_blk, 2);
+    return BVP_OK;
+}
+
 static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode, const double* d_params,
                                const int* d_n_init, const double* d_tspans, const double* d_y0,
-                               const long long* d_y0_off, const float* d_grid = nullptr, int n_grid = 0,
-                               long long host_pts = 0, bool wait_side = false) {
+                               const long long* d_y0_off, int max_init, const float* d_grid = nullptr,
+                               int n_grid = 0, long long host_pts = 0, bool wait_side = false) {
+    // block mode when the batch has a long mesh (max_init: its largest initial interval count)
+    const bool blk = h->group_min > 0 && max_init >= h->group_min;
+    if (blk) {
+        bvp_status s = ensure_block_module(h);
+        if (s != BVP_OK) return s;
+    }
     BvpArgs a;
     fill_args(h, a, n, tot, y0_mode, d_params, d_n_init, d_tspans, d_y0, d_y0_off);
     a.y0_grid = d_grid;
@@ -765,19 +788,23 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
         int* ord = static_cast<int*>(h->d_order.p);
         int* ctr = static_cast<int*>(h->d_counter.p);
         const float* tab = h->have_tab ? static_cast<const float*>(h->d_cost_tab.p) : nullptr;
-        int gm = h->group_min;
+        int gm = blk ? h->group_min : 0;
         void* args[] = {&nn, &ni, &ms, &cs, &cap, &off, &ord, &ctr, &tab, &gm};
         CU(cudaLaunchKernel((const void*)h->k_prep, dim3(1), dim3(1024), args, 0, h->stream));
     }
     if (wait_side) CU(cudaStreamWaitEvent(h->stream, h->ev_side, 0));   // the guesses on the grid
-    const int var = fused_variant(h, n, y0_mode);
+    // the launch-shape tuner times the warp-only kernels; a block-mode launch drops its pending sample
+    int var = 0;
+    if (blk) h->tune.pending = -1;
+    else var = fused_variant(h, n, y0_mode);
     CU(cudaEventRecord(h->ev[1], h->stream));
     if (h->ho) CU(cudaMemsetAsync(a.pause_count, 0, 2 * sizeof(int), h->stream));
     a.deal_sms = std::max(1, h->sm_count);
     {
         void* args[] = {&a};
-        CU(cudaLaunchKernel((const void*)h->k_fused_v[var], dim3(resident_grid(h, n, h->occ_v[var])), dim3(128), args,
-                            0, h->stream));
+        const cudaKernel_t k = blk ? h->k_fused_blk : h->k_fused_v[var];
+        const int occ = blk ? h->occ_blk : h->occ_v[var];
+        CU(cudaLaunchKernel((const void*)k, dim3(resident_grid(h, n, occ)), dim3(128), args, 0, h->stream));
     }
     if (h->ho) {
         bvp_status s = ho_rounds(h, a, n);
@@ -1569,6 +1596,7 @@ bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const
     if (h->large) return solve_large(h, n, params, n_intervals, tspans, y0_mode, y0, out);
     const int M = h->L.M;
     long long tot = 0, y0_vals = 0, pts = 0;
+    int max_init = 0;
     for (int q = 0; q < n; ++q) {
         const int ni = n_intervals[q];
         if (ni < 1) return fail(h, BVP_ERR_INVALID, "n_intervals must be >= 1");
@@ -1576,6 +1604,7 @@ bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const
         pts += ni + 1;
         tot += cap_nodes(h, ni);
         y0_vals += (y0_mode == 1) ? (long long)(ni + 1) * M : M;
+        max_init = std::max(max_init, ni);
     }
     bvp_status s = ensure_arena(h, tot, n, y0_vals);
     if (s != BVP_OK) return s;
@@ -1602,8 +1631,8 @@ bvp_status bvp_solve_batch(bvp_handle* h, int32_t n, const double* params, const
     if (y0_mode == 1) CU(cudaMemcpyAsync(h->d_y0_off.p, yoff, b_off, cudaMemcpyHostToDevice, h->stream));
     s = launch_solve(h, n, tot, y0_mode, static_cast<const double*>(h->d_params.p),
                      static_cast<const int*>(h->d_n_init.p), static_cast<const double*>(h->d_tspans.p),
-                     static_cast<const double*>(h->d_y0.p), static_cast<const long long*>(h->d_y0_off.p), nullptr,
-                     0, pts);
+                     static_cast<const double*>(h->d_y0.p), static_cast<const long long*>(h->d_y0_off.p), max_init,
+                     nullptr, 0, pts);
     if (s != BVP_OK) return s;
     return finish_host(h, out);
 }
@@ -1634,8 +1663,8 @@ bvp_status bvp_solve_batch_device_warm(bvp_handle* h, bvp_mlp* net, int32_t n, c
     s = side_forward(h, net, n, d_features);
     if (s != BVP_OK) return s;
     s = launch_solve(h, n, tot, 2, d_params, d_n_intervals, d_tspans, static_cast<const double*>(h->d_y0.p),
-                     static_cast<const long long*>(h->d_y0_off.p), static_cast<const float*>(h->d_grid.p), n_grid, 0,
-                     true);
+                     static_cast<const long long*>(h->d_y0_off.p), max_intervals,
+                     static_cast<const float*>(h->d_grid.p), n_grid, 0, true);
     if (s != BVP_OK) return s;
     h->pending_device = true;
     h->have_results = false;
@@ -1653,6 +1682,7 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
         (h->desc.n_params > 0 && !params))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
     long long tot = 0, y0_vals = 0, pts = 0;
+    int max_init = 0;
     for (int q = 0; q < n; ++q) {
         const int ni = n_intervals[q];
         if (ni < 1) return fail(h, BVP_ERR_INVALID, "n_intervals must be >= 1");
@@ -1660,6 +1690,7 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
         pts += ni + 1;
         tot += cap_nodes(h, ni);
         y0_vals += (long long)(ni + 1) * M;
+        max_init = std::max(max_init, ni);
     }
     (void)y0_vals;
     bvp_status s = ensure_arena(h, tot, n, 1);
@@ -1686,8 +1717,8 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
     // the solve resamples the grid guesses onto the initial meshes itself (y0_mode 2)
     s = launch_solve(h, n, tot, 2, static_cast<const double*>(h->d_params.p), static_cast<const int*>(h->d_n_init.p),
                      static_cast<const double*>(h->d_tspans.p), static_cast<const double*>(h->d_y0.p),
-                     static_cast<const long long*>(h->d_y0_off.p), static_cast<const float*>(h->d_grid.p), n_grid,
-                     pts, true);
+                     static_cast<const long long*>(h->d_y0_off.p), max_init, static_cast<const float*>(h->d_grid.p),
+                     n_grid, pts, true);
     if (s != BVP_OK) return s;
     s = finish_host(h, nullptr);
     if (s != BVP_OK) return s;
@@ -1768,7 +1799,7 @@ bvp_status bvp_solve_batch_device(bvp_handle* h, int32_t n, const double* d_para
     if (s != BVP_OK) return s;
     const double* dp = d_params ? d_params : static_cast<const double*>(h->d_params.p);
     s = launch_solve(h, n, tot, y0_mode, dp, d_n_intervals, d_tspans, d_y0,
-                     reinterpret_cast<const long long*>(d_y0_off));
+                     reinterpret_cast<const long long*>(d_y0_off), max_intervals);
     if (s != BVP_OK) return s;
     h->pending_device = true;
     h->have_results = false;
@@ -1787,7 +1818,7 @@ bvp_status bvp_solve_batch_device_grid(bvp_handle* h, int32_t n, const double* d
     bvp_status s = ensure_arena(h, tot, n, 1);
     if (s != BVP_OK) return s;
     s = launch_solve(h, n, tot, 2, d_params, d_n_intervals, d_tspans, static_cast<const double*>(h->d_y0.p),
-                     static_cast<const long long*>(h->d_y0_off.p), d_grid, n_grid);
+                     static_cast<const long long*>(h->d_y0_off.p), max_intervals, d_grid, n_grid);
     if (s != BVP_OK) return s;
     h->pending_device = true;
     h->have_results = false;
@@ -2025,6 +2056,7 @@ void bvp_destroy(bvp_handle* h) {
     if (h->side) cudaStreamDestroy(h->side);
     if (h->lib) cudaLibraryUnload(h->lib);
     if (h->lib_hi) cudaLibraryUnload(h->lib_hi);
+    if (h->lib_blk) cudaLibraryUnload(h->lib_blk);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }

@@ -89,7 +89,7 @@ typedef struct {
                                      whole 128-thread block instead of one warp: the residuals and
                                      the defect spread over 128 lanes, the rest of the solve on the
                                      block's first warp; the results are the same. 0: the library's
-                                     threshold (1024 intervals); -1: never. The defect-controlled
+                                     threshold (512 intervals); -1: never. The defect-controlled
                                      MIRK path only (M <= 8) */
 } bvp_options;
 

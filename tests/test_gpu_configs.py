@@ -96,7 +96,9 @@ def test_singular_perturbation_mesh_cap(pkg, problems):
     ref = o.solve_batch(params, nint, tsp, y0, order=6, max_subintervals=600)
     res = pkg.BatchSolver(p, order=6, jac_precision=64, max_subintervals=600).solve(params, nint, tsp, y0)
     assert (ref["retcode"] == RET_FAILURE).any() and (ref["retcode"] == RET_SUCCESS).any()
-    assert (res.retcode == ref["retcode"]).all()
+    bad = np.nonzero(res.retcode != ref["retcode"])[0]
+    assert len(bad) == 0, [(int(i), int(nint[i]), int(res.retcode[i]), int(ref["retcode"][i]), int(res.n_nodes[i]),
+                            int(ref["n_nodes"][i]), float(res.defect[i]), float(ref["defect"][i])) for i in bad[:5]]
     # a failed redistribution leaves the instance on its last mesh
     fail = res.retcode == RET_FAILURE
     assert (res.n_nodes[fail] == ref["n_nodes"][fail]).all()

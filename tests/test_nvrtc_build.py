@@ -1,7 +1,7 @@
 """The kernels compile through NVRTC for sm_103a exactly as bvp_create compiles them (same
 source assembly and options), for every MIRK order and MIRK6I, both Jacobian precisions, standard and
-two-point problems, the larger-state family, a problem with a singular term, and the build
-with the global-error controllers. NVRTC runs on
+two-point problems, the larger-state family, a problem with a singular term, the build
+with the global-error controllers and the block-mode module. NVRTC runs on
 the CPU, so this catches JIT-only compile errors without a GPU."""
 import pytest
 
@@ -17,6 +17,8 @@ CASES = [
     ("pendulum", 6, 32, 1), ("singular_perturbation", 6, 64, 1), ("nonlinear32", 6, 32, 1),
     # the build with the global-error controllers (BVP_GLOBAL_CTL), and the MIRK(p+2) module of HO
     ("torus", 4, 64, 0, 1), ("pendulum", 6, 32, 0, 1),
+    # the block-mode module for long meshes (BVP_BLOCK_MODE), interior BCs and two-point
+    ("singular_perturbation", 6, 32, 0, 0, 0, 1), ("pendulum", 4, 64, 0, 0, 0, 1),
 ]
 
 
