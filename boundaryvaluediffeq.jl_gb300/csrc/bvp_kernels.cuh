@@ -960,96 +960,6 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
     return true;
 }
 
-// The same elimination with each lane's row in registers (separator systems of at most 16
-// unknowns). Rows are not moved: each lane tracks its row's position, and the pivot search, the
-// row swap, the update order and every operation are those of separator_solve_warp, so the
-// results are the same; a column is broadcast from the pivot lane by a shuffle, and entries at a
-// run-time column are picked by unrolled selects instead of indexed loads.
-constexpr bool SEP_REG = NDENSE <= 16;
-template <class T> BVP_DEV T pick(const T (&r)[NDENSE], int c) {
-    T v = T(0);
-#pragma unroll
-    for (int cc = 0; cc < NDENSE; ++cc) v = cc == c ? r[cc] : v;
-    return v;
-}
-BVP_DEV bool separator_solve_reg(const Args& a, const Inst& I, int nk) {
-    const int lane = lane_id();
-    const int n = nk * M;
-    const int row0 = (nk - 1) * M;
-    JT ar[NDENSE], b = JT(0);
-#pragma unroll
-    for (int cc = 0; cc < NDENSE; ++cc) ar[cc] = JT(0);
-    if (lane < row0) {
-        // segment relation j: A δ_{kept j} + B δ_{kept j+1} = g
-        const int j = lane / M, r = lane - j * M;
-        const JT* seg = seg_of(I, j);
-#pragma unroll
-        for (int cc = 0; cc < NDENSE; ++cc) {
-            const int cA = cc - j * M, cB = cc - (j + 1) * M;
-            if (cA >= 0 && cA < M) ar[cc] = seg[r * M + cA];
-            else if (cB >= 0 && cB < M) ar[cc] = seg[M * M + r * M + cB];
-        }
-        b = seg[2 * M * M + r];
-    } else if (lane < n) {
-        // BC row r: every BC contribution's block, added at its separator's columns
-        const int r = lane - row0;
-        const int nb = I.iscr[ISCR_NB];
-#pragma unroll 1
-        for (int k = 0; k < nb; ++k) {
-            const int node = I.iscr[ISCR_BNODE + k];
-            int kj = 0;
-            while (kj < nk - 1 && I.iscr[ISCR_KEPT + kj] != node) ++kj;
-            const double* G = I.scr + SCR_BCBLK + k * M * M + r * M;
-#pragma unroll
-            for (int cc = 0; cc < NDENSE; ++cc) {
-                const int c = cc - kj * M;
-                if (c >= 0 && c < M) ar[cc] += JT(G[c]);
-            }
-        }
-        b = JT(-I.scr[SCR_BCRES + r]);
-    }
-    int pos = lane;   // the position of this lane's row
-#pragma unroll 1
-    for (int k = 0; k < n; ++k) {
-        // pivot: the largest |A[p][k]| over positions p >= k, the lowest position on a tie
-        JT v = (lane < n && pos >= k) ? fabs(pick(ar, k)) : JT(-1);
-        int pp = pos;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const JT v2 = __shfl_xor_sync(FULL, v, o);
-            const int p2 = __shfl_xor_sync(FULL, pp, o);
-            if (v2 > v || (v2 == v && p2 < pp)) { v = v2; pp = p2; }
-        }
-        if (!(v > JT(0)) || !isfinite(v)) return false;   // uniform across the warp
-        const int pl = __ffs(__ballot_sync(FULL, lane < n && pos == pp)) - 1;   // the pivot row's lane
-        if (pp != k && pos == k) pos = pp;   // the row at position k moves to the pivot's place
-        if (lane == pl) pos = k;
-        const JT pk = __shfl_sync(FULL, pick(ar, k), pl);
-        const bool upd = lane < n && pos > k;
-        const JT mlt = pick(ar, k) * (JT(1) / pk);
-#pragma unroll
-        for (int cc = 0; cc < NDENSE; ++cc) {
-            const JT pv = __shfl_sync(FULL, ar[cc], pl);
-            if (upd && cc > k && cc < n) ar[cc] -= mlt * pv;
-        }
-        const JT pb = __shfl_sync(FULL, b, pl);
-        if (upd) b -= mlt * pb;
-    }
-#pragma unroll 1
-    for (int k = n - 1; k >= 0; --k) {
-        const int pl = __ffs(__ballot_sync(FULL, lane < n && pos == k)) - 1;
-        if (lane == pl) b = b / pick(ar, k);
-        const JT xk = __shfl_sync(FULL, b, pl);
-        if (lane < n && pos < k) b -= pick(ar, k) * xk;
-    }
-    if (lane < n) {
-        I.dns[pos * DLD + n] = b;
-        a.delta[(I.nb + I.iscr[ISCR_KEPT + pos / M]) * M + pos % M] = b;
-    }
-    __syncwarp();
-    return true;
-}
-
 #ifndef BVP_TREE_UNROLL
 #define BVP_TREE_UNROLL 1
 #endif
@@ -1266,9 +1176,7 @@ BVP_DEV bool linear_solve(const Args& a, const Inst& I) {
     __syncwarp();
     // 3. separator system
     int dense_ok = 1;
-    if constexpr (SEP_REG) {
-        dense_ok = separator_solve_reg(a, I, nk) ? 1 : 0;
-    } else if constexpr (SMEM_DENSE) {
+    if constexpr (SMEM_DENSE) {
         dense_ok = separator_solve_warp(a, I, nk) ? 1 : 0;
     } else if (lane == 0) {
         // in thread-local storage (L1-resident), not the global scratch: the elimination
@@ -1754,6 +1662,7 @@ BVP_DEV int mesh_selector(const Args& a, Inst& I, int& newN, int sel = SEL_DEFEC
         r1 = fmax(r1, sh);
         r2p += sh;
     }
+    __syncwarp();   // the block sums below read other lanes' ŝ
     r1 = warp_max(r1);
     const double r2 = warp_sum(r2p);
     const double r3 = r2 / (I.N - 1);
