@@ -237,7 +237,7 @@ EXPORTS = ("bvp_default_options", "bvp_create", "bvp_solve_batch", "bvp_solve_ba
            "bvp_mlp_get_params", "bvp_mlp_set_normalization", "bvp_mlp_forward", "bvp_mlp_loss_grad",
            "bvp_mlp_train", "bvp_mlp_forward_device", "bvp_mlp_forward_noalloc", "bvp_resample_guess_device",
            "bvp_mlp_destroy",
-           "bvp_solve_batch_warm", "bvp_solve_batch_device_warm", "bvp_get_fused_tuning",
+           "bvp_solve_batch_warm", "bvp_solve_batch_device_warm", "bvp_get_fused_tuning", "bvp_get_block_mode",
            "bvp_last_timing", "bvp_get_tuning", "bvp_get_work_order", "bvp_stream", "bvp_last_error",
            "bvp_destroy")
 
@@ -307,6 +307,8 @@ def load_library(path: str | None = None):
     lib.bvp_get_tuning.restype = C.c_int
     lib.bvp_get_fused_tuning.argtypes = [vp, i32p, i32p, C.POINTER(C.c_float)]
     lib.bvp_get_fused_tuning.restype = C.c_int
+    lib.bvp_get_block_mode.argtypes = [vp, i32p, i32p]
+    lib.bvp_get_block_mode.restype = C.c_int
     lib.bvp_get_work_order.argtypes = [vp, i32p, C.POINTER(C.c_float), i32]
     lib.bvp_get_work_order.restype = C.c_int
     lib.bvp_stream.argtypes = [vp]

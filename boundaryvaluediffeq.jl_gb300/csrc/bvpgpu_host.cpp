@@ -73,6 +73,7 @@ struct bvp_handle_s {
     cudaLibrary_t lib_blk = nullptr;
     cudaKernel_t k_fused_blk = nullptr;
     int occ_blk = 2;
+    bool last_blk = false;   // the last solve ran the block-mode module
     int fused_pick = 1;
     struct {
         long long key = -1;
@@ -746,6 +747,7 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
                                int n_grid = 0, long long host_pts = 0, bool wait_side = false) {
     // block mode when the batch has a long mesh (max_init: its largest initial interval count)
     const bool blk = h->group_min > 0 && max_init >= h->group_min;
+    h->last_blk = blk;
     if (blk) {
         bvp_status s = ensure_block_module(h);
         if (s != BVP_OK) return s;
@@ -1895,6 +1897,13 @@ bvp_status bvp_get_fused_tuning(bvp_handle* h, int32_t* blocks_per_sm, int32_t* 
     if (tuned) *tuned = h->tune.done ? 1 : 0;
     if (ms)
         for (int c = 0; c < 3; ++c) ms[c] = h->tune.cnt[c] > 0 ? h->tune.sum[c] / h->tune.cnt[c] : 0.0f;
+    return BVP_OK;
+}
+
+bvp_status bvp_get_block_mode(bvp_handle* h, int32_t* block_min, int32_t* last) {
+    if (!h || !block_min) return BVP_ERR_INVALID;
+    *block_min = h->group_min;
+    if (last) *last = h->last_blk ? 1 : 0;
     return BVP_OK;
 }
 

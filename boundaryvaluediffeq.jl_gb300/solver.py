@@ -258,8 +258,11 @@ class BatchSolver:
         ms = np.zeros(3, np.float32)
         self._check(self.lib.bvp_get_fused_tuning(self.h, i32(b), i32(done), ms.ctypes.data_as(C.POINTER(C.c_float))),
                     "bvp_get_fused_tuning")
+        bm, last = np.zeros(1, np.int32), np.zeros(1, np.int32)
+        self._check(self.lib.bvp_get_block_mode(self.h, i32(bm), i32(last)), "bvp_get_block_mode")
         return {"linsolve_threads": int(t[0]), "fused_blocks_per_sm": int(b[0]), "fused_tuned": bool(done[0]),
-                "fused_ms_by_blocks": {4: float(ms[0]), 3: float(ms[1]), 2: float(ms[2])}}
+                "fused_ms_by_blocks": {4: float(ms[0]), 3: float(ms[1]), 2: float(ms[2])},
+                "block_min": int(bm[0]), "last_solve_block_mode": bool(last[0])}
 
     def work_order(self):
         """(learned, costs): whether the fused solve's work order comes from the handle's learned

@@ -295,6 +295,12 @@ bvp_status bvp_get_tuning(bvp_handle* h, int32_t* threads);
  * the candidates' mean kernel times so far. */
 bvp_status bvp_get_fused_tuning(bvp_handle* h, int32_t* blocks_per_sm, int32_t* tuned, float* ms);
 
+/* Block mode (bvp_options.block_min): *block_min the threshold in effect (0: block mode off),
+ * *last (if not NULL) 1 when the last solve ran the block-mode module (its largest initial mesh
+ * reached the threshold; 2 resident blocks per SM, not tuned), else 0. No reference
+ * counterpart: a performance report of this library, like bvp_get_fused_tuning. */
+bvp_status bvp_get_block_mode(bvp_handle* h, int32_t* block_min, int32_t* last);
+
 /* The fused solve's work order (no reference counterpart: the reference solves one problem at
  * a time). One warp carries one instance, so a batch ends when its slowest instances end; the
  * handle's first three solves of at least 256 instances record every instance's solve time

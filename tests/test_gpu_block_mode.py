@@ -63,3 +63,21 @@ def test_block_mode_failures_and_line_search(pkg, problems):
     ref = _solve(pkg, p, 6, batch, -1, max_subintervals=600)
     assert (ref.retcode != RET_SUCCESS).any()
     _same(_solve(pkg, p, 6, batch, 1, max_subintervals=600), ref)
+
+
+def test_block_mode_selection(pkg, problems):
+    # the library's threshold (512 initial intervals): a batch whose largest mesh reaches it runs
+    # the block-mode module, others the warp kernels; block_min -1 turns it off
+    sp = problems.SINGULAR_PERTURBATION
+    batch = problems.singular_perturbation_family(8, seed=9)
+    sv = pkg.BatchSolver(sp, order=6)
+    sv.solve(*batch)
+    t = sv.tuning()
+    assert t["block_min"] == 512 and t["last_solve_block_mode"]
+    short = problems.singular_perturbation_family(8, seed=9, n_min=64, n_max=256)
+    sv.solve(*short)
+    assert not sv.tuning()["last_solve_block_mode"]
+    off = pkg.BatchSolver(sp, order=6, block_min=-1)
+    off.solve(*batch)
+    t = off.tuning()
+    assert t["block_min"] == 0 and not t["last_solve_block_mode"]
