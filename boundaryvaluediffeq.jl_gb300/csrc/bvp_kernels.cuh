@@ -921,13 +921,25 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
     __syncwarp();
 #pragma unroll 1
     for (int k = 0; k < n; ++k) {
-        JT v = (lane >= k && lane < n) ? fabs(A[lane * DLD + k]) : JT(-1);
-        int pr = lane;
+        const bool cand = lane >= k && lane < n;
+        JT v;
+        int pr;
+        if constexpr (sizeof(JT) == 4) {
+            // largest |a| by one warp reduction on the bit patterns (non-negative floats order as
+            // their bits), the lowest such row by a ballot
+            const unsigned key = cand ? __float_as_uint(fabsf(float(A[lane * DLD + k]))) : 0u;
+            const unsigned mk = __reduce_max_sync(FULL, key);
+            pr = __ffs(__ballot_sync(FULL, cand && key == mk)) - 1;
+            v = JT(__uint_as_float(mk));
+        } else {
+            v = cand ? fabs(A[lane * DLD + k]) : JT(-1);
+            pr = lane;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const JT v2 = __shfl_xor_sync(FULL, v, o);
-            const int p2 = __shfl_xor_sync(FULL, pr, o);
-            if (v2 > v || (v2 == v && p2 < pr)) { v = v2; pr = p2; }
+            for (int o = 16; o > 0; o >>= 1) {
+                const JT v2 = __shfl_xor_sync(FULL, v, o);
+                const int p2 = __shfl_xor_sync(FULL, pr, o);
+                if (v2 > v || (v2 == v && p2 < pr)) { v = v2; pr = p2; }
+            }
         }
         if (!(v > JT(0)) || !isfinite(v)) return false;   // uniform across the warp
         if (pr != k) {
@@ -943,7 +955,8 @@ BVP_DEV bool separator_solve_warp(const Args& a, const Inst& I, int nk) {
             JT* ar = A + lane * DLD;
             const JT* ak = A + k * DLD;
             const JT mlt = ar[k] * (JT(1) / ak[k]);
-#pragma unroll 1
+            // four columns' loads in flight at a time
+#pragma unroll 4
             for (int c = k + 1; c <= n; ++c) ar[c] -= mlt * ak[c];
         }
         __syncwarp();
