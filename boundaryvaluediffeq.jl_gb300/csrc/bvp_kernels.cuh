@@ -2295,9 +2295,6 @@ extern "C" __global__ void __launch_bounds__(128, 4) bvp_solve_fused(const bvp::
 extern "C" __global__ void __launch_bounds__(128, 3) bvp_solve_fused_b3(const bvp::Args a) { bvp::fused_body(a); }
 extern "C" __global__ void __launch_bounds__(128, 2) bvp_solve_fused_b2(const bvp::Args a) { bvp::fused_body(a); }
 #endif
-#ifndef BVP_POLISH_ONLY
-#define BVP_POLISH_ONLY 0
-#endif
 #if !BVP_POLISH_ONLY && !BVP_FIRK && !BVP_BLOCK_MODE
 
 // Stage kernels on caller-provided (mesh, y) in buffer 0 with N = st[q].N. Used by the
