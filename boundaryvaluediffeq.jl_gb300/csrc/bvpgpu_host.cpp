@@ -746,12 +746,15 @@ static bvp_status launch_solve(bvp_handle* h, int n, long long tot, int y0_mode,
                                const long long* d_y0_off, int max_init, const float* d_grid = nullptr,
                                int n_grid = 0, long long host_pts = 0, bool wait_side = false) {
     // block mode when the batch has a long mesh (max_init: its largest initial interval count)
-    const bool blk = h->group_min > 0 && max_init >= h->group_min;
-    h->last_blk = blk;
-    if (blk) {
-        bvp_status s = ensure_block_module(h);
-        if (s != BVP_OK) return s;
+    bool blk = h->group_min > 0 && max_init >= h->group_min;
+    if (blk && ensure_block_module(h) != BVP_OK) {
+        // block mode only changes speed: without its module the handle solves by warps (the
+        // reason stays in bvp_last_error)
+        (void)cudaGetLastError();
+        h->group_min = 0;
+        blk = false;
     }
+    h->last_blk = blk;
     BvpArgs a;
     fill_args(h, a, n, tot, y0_mode, d_params, d_n_init, d_tspans, d_y0, d_y0_off);
     a.y0_grid = d_grid;

@@ -295,7 +295,8 @@ bvp_status bvp_get_tuning(bvp_handle* h, int32_t* threads);
  * the candidates' mean kernel times so far. */
 bvp_status bvp_get_fused_tuning(bvp_handle* h, int32_t* blocks_per_sm, int32_t* tuned, float* ms);
 
-/* Block mode (bvp_options.block_min): *block_min the threshold in effect (0: block mode off),
+/* Block mode (bvp_options.block_min): *block_min the threshold in effect (0: block mode off,
+ * also after its module failed to build, the reason then in bvp_last_error),
  * *last (if not NULL) 1 when the last solve ran the block-mode module (its largest initial mesh
  * reached the threshold; 2 resident blocks per SM, not tuned), else 0. No reference
  * counterpart: a performance report of this library, like bvp_get_fused_tuning. */
