@@ -767,11 +767,6 @@ struct InstanceSolver {
         const int S = tb.s, NS = std::max(1, ns());
         std::vector<double> old_y = y;           // clean copy
         std::vector<double> ny(size_t(N) * M);
-        std::vector<double>& src = op.transfer_inplace ? ny : old_y;
-        if (op.transfer_inplace) {
-            // the reference overwrites y0 in place while reading y0[old interval]
-            for (size_t q = 0; q < std::min(ny.size(), old_y.size()); ++q) ny[q] = old_y[q];
-        }
         for (int j = 0; j < N; ++j) {
             const double m_t = mesh[j];
             const int i = interval_of(old_mesh.data(), On, m_t);
@@ -779,6 +774,11 @@ struct InstanceSolver {
             const double tau = (m_t - old_mesh[i]) / dt;
             double w[9], wp[9];
             interp_weights(tb.scheme, tau, w, wp);
+            // The reference overwrites y0 in place while reading y0[old interval]
+            // (mirk.jl:366-371): node j's base is the new value of node i when i < j, else the
+            // old one (y0 keeps its old length when the mesh shrinks, so an old interval past
+            // the new node count still holds its old value).
+            const std::vector<double>& src = (op.transfer_inplace && i < j) ? ny : old_y;
             double z[M];
             for (int m = 0; m < M; ++m) {
                 double acc = 0;

@@ -91,10 +91,9 @@ def test_singular_perturbation_full_size(pkg, problems, jac_precision):
 
 def test_singular_perturbation_mesh_cap(pkg, problems):
     # Instances whose mesh path (rounds, node counts) is the oracle's must end as the oracle's
-    # does; an instance whose path diverged (the ill-conditioned boundary-layer systems leave
-    # defects near abstol, where the last digits of two FP64 solvers decide the next mesh; the
-    # oracle's own outcome for such an instance was seen to change between hosts) must pass the
-    # reference's acceptance tests when it succeeds.
+    # does; an instance whose path diverged (in the ill-conditioned boundary-layer systems the
+    # last digits of two FP64 solvers pick different next meshes) must pass the reference's
+    # acceptance tests when it succeeds.
     p = problems.SINGULAR_PERTURBATION
     params, nint, tsp, y0 = _sp_batch(problems)
     o = _oracle(p)
