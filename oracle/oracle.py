@@ -71,8 +71,10 @@ def _compile(source: str, M: int, twopoint: bool) -> str:
             h.update(f.read())
     h.update(source.encode())
     trace = bool(os.environ.get("BVP_ORACLE_TRACE"))
+    # BVP_ORACLE_CHECKED: bounds-checked containers (an out-of-range index aborts)
+    checked = bool(os.environ.get("BVP_ORACLE_CHECKED"))
     sing = "BVP_SING" in source
-    h.update(f"M={M};tp={int(twopoint)};trace={int(trace)};sing={int(sing)}".encode())
+    h.update(f"M={M};tp={int(twopoint)};trace={int(trace)};sing={int(sing)};checked={int(checked)}".encode())
     key = h.hexdigest()[:20]
     os.makedirs(_BUILD, exist_ok=True)
     so = os.path.join(_BUILD, f"oracle_{key}.so")
@@ -85,7 +87,8 @@ def _compile(source: str, M: int, twopoint: bool) -> str:
     cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
            f"-DBVP_M={M}", f"-DBVP_TWOPOINT={int(twopoint)}",
            f"-DBVP_SINGULAR={int(sing)}", f'-DBVP_PROBLEM_HEADER="{hdr}"', "-I", _HERE,
-           os.path.join(_HERE, "oracle_entry.cpp"), "-o", tmp] + (["-DBVP_TRACE"] if trace else [])
+           os.path.join(_HERE, "oracle_entry.cpp"), "-o", tmp] + (["-DBVP_TRACE"] if trace else []) + \
+        (["-D_GLIBCXX_ASSERTIONS"] if checked else [])
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     os.replace(tmp, so)
     return so
