@@ -1792,11 +1792,58 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
     return BVP_OK;
 }
 
+// The larger-state path (M > 8) drives its Newton steps from the host, so a solve on device
+// inputs reads them back (on the handle's stream) and runs the host-buffer solve; it returns
+// with the results in the handle, which bvp_fetch_results then reads.
+static bvp_status solve_large_from_device(bvp_handle* h, int n, const double* d_params, const int32_t* d_n_intervals,
+                                          const double* d_tspans, int y0_mode, const double* d_y0,
+                                          const int64_t* d_y0_off, int max_intervals) {
+    const int M = h->L.M, P = h->desc.n_params;
+    if (n < 1 || !d_n_intervals || !d_tspans || !d_y0 || max_intervals < 1 || (y0_mode != 0 && y0_mode != 1) ||
+        (y0_mode == 1 && !d_y0_off) || (P > 0 && !d_params))
+        return fail(h, BVP_ERR_INVALID, "invalid arguments");
+    std::vector<int32_t> ni(n);
+    std::vector<double> ts(size_t(n) * 2), pr(size_t(n) * std::max(P, 1));
+    CU(cudaMemcpyAsync(ni.data(), d_n_intervals, size_t(n) * 4, cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaMemcpyAsync(ts.data(), d_tspans, size_t(n) * 16, cudaMemcpyDeviceToHost, h->stream));
+    if (P > 0) CU(cudaMemcpyAsync(pr.data(), d_params, size_t(n) * P * 8, cudaMemcpyDeviceToHost, h->stream));
+    std::vector<int64_t> off;
+    if (y0_mode == 1) {
+        off.resize(n);
+        CU(cudaMemcpyAsync(off.data(), d_y0_off, size_t(n) * 8, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CU(cudaStreamSynchronize(h->stream));
+    for (int q = 0; q < n; ++q)
+        if (ni[q] < 1 || ni[q] > max_intervals) return fail(h, BVP_ERR_INVALID, "n_intervals outside 1..max_intervals");
+    std::vector<double> y0;
+    if (y0_mode == 0) {
+        y0.resize(size_t(n) * M);
+        CU(cudaMemcpyAsync(y0.data(), d_y0, y0.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaStreamSynchronize(h->stream));
+    } else {
+        // the per-instance blocks of the device array, packed in instance order
+        long long need = 0, packed = 0;
+        for (int q = 0; q < n; ++q) {
+            if (off[q] < 0) return fail(h, BVP_ERR_INVALID, "negative y0 offset");
+            need = std::max<long long>(need, off[q] + ni[q] + 1);
+            packed += ni[q] + 1;
+        }
+        std::vector<double> all(size_t(need) * M);
+        CU(cudaMemcpyAsync(all.data(), d_y0, all.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaStreamSynchronize(h->stream));
+        y0.reserve(size_t(packed) * M);
+        for (int q = 0; q < n; ++q)
+            y0.insert(y0.end(), all.begin() + off[q] * M, all.begin() + (off[q] + ni[q] + 1) * M);
+    }
+    return solve_large(h, n, P > 0 ? pr.data() : nullptr, ni.data(), ts.data(), y0_mode, y0.data(), nullptr);
+}
+
 bvp_status bvp_solve_batch_device(bvp_handle* h, int32_t n, const double* d_params, const int32_t* d_n_intervals,
                                   const double* d_tspans, int32_t y0_mode, const double* d_y0,
                                   const int64_t* d_y0_off, int32_t max_intervals) {
     if (!h) return BVP_ERR_INVALID;
-    if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: only bvp_solve_batch is available");
+    if (h->large)
+        return solve_large_from_device(h, n, d_params, d_n_intervals, d_tspans, y0_mode, d_y0, d_y0_off, max_intervals);
     if (n < 1 || !d_n_intervals || !d_tspans || !d_y0 || max_intervals < 1 || (y0_mode == 1 && !d_y0_off))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
     const long long tot = (long long)n * cap_nodes(h, max_intervals);

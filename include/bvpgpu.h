@@ -148,7 +148,9 @@ bvp_status bvp_solve_batch(bvp_handle* h, int32_t n_inst, const double* params,
 /* Same solve with inputs already in device memory (device pointers; y0_off is the
  * per-instance offset, in M-vectors, for y0_mode 1, else NULL). max_intervals bounds
  * n_intervals. Runs on the handle's stream and returns without synchronising; results
- * stay on the device (read them with bvp_fetch_results). */
+ * stay on the device (read them with bvp_fetch_results). For state dimensions above 8 (the
+ * host-driven path) the inputs are read back on the handle's stream and the call returns
+ * after the solve; bvp_fetch_results reads the results the same way. */
 bvp_status bvp_solve_batch_device(bvp_handle* h, int32_t n_inst, const double* d_params,
                                   const int32_t* d_n_intervals, const double* d_tspans,
                                   int32_t y0_mode, const double* d_y0, const int64_t* d_y0_off,

@@ -117,3 +117,32 @@ def test_nonlinear32_dense_output(pkg, problems):
         assert np.abs(u[i][0] - y[0]).max() == 0.0
         assert np.abs(u[i][-1] - y[-1]).max() <= 1e-6 * (1 + 1e-6)
     assert checked_ki >= 1
+
+
+@pytest.mark.parametrize("y0_mode", [0, 1])
+def test_nonlinear32_device_inputs(pkg, problems, y0_mode):
+    # the device-input entry point on the host-driven path: inputs read back on the handle's
+    # stream, the same solve as from host buffers (same handle, so the same tuned block size)
+    import torch
+    p = problems.NONLINEAR32
+    params, nint, tsp, y0 = problems.nonlinear32_family(4, seed=5, n_intervals=64)
+    if y0_mode == 1:
+        y0 = np.concatenate([np.tile(y0[q], (int(nint[q]) + 1, 1)) for q in range(len(nint))])
+    sv = pkg.BatchSolver(p, order=4, jac_precision=64)
+    sv.solve(params, nint, tsp, y0, y0_mode=y0_mode)          # tunes the linear solve
+    ref = sv.solve(params, nint, tsp, y0, y0_mode=y0_mode)
+
+    def dev(x, dt):
+        return torch.tensor(np.ascontiguousarray(x), dtype=dt, device="cuda")
+
+    off = None
+    if y0_mode == 1:
+        off = dev(np.concatenate([[0], np.cumsum(nint[:-1] + 1)]), torch.int64)
+    sv.solve_device(dev(params, torch.float64), dev(nint, torch.int32), dev(tsp, torch.float64),
+                    dev(y0, torch.float64), int(nint.max()), y0_mode=y0_mode, d_y0_off=off)
+    res = sv.fetch()
+    for f in ("retcode", "n_nodes", "newton_iters", "rounds"):
+        assert np.array_equal(getattr(res, f), getattr(ref, f)), f
+    for i in range(len(nint)):
+        for a, b in zip(res.solution(i), ref.solution(i)):
+            assert np.array_equal(a, b), i
