@@ -1657,7 +1657,7 @@ bvp_status bvp_solve_batch_device_warm(bvp_handle* h, bvp_mlp* net, int32_t n, c
                                        int32_t n_grid, const double* d_params, const int32_t* d_n_intervals,
                                        const double* d_tspans, int32_t max_intervals) {
     if (!h) return BVP_ERR_INVALID;
-    if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: only bvp_solve_batch is available");
+    if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: bvp_solve_batch and bvp_solve_batch_device only");
     if (!net || n < 1 || !d_features || n_grid < 2 || !d_n_intervals || !d_tspans || max_intervals < 1 ||
         (h->desc.n_params > 0 && !d_params))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
@@ -1681,7 +1681,7 @@ bvp_status bvp_solve_batch_warm(bvp_handle* h, bvp_mlp* net, int32_t n, int32_t 
                                 const double* tspans, const double* y0_plain, bvp_results* out,
                                 int32_t* n_fallback) {
     if (!h) return BVP_ERR_INVALID;
-    if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: only bvp_solve_batch is available");
+    if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: bvp_solve_batch and bvp_solve_batch_device only");
     const int M = h->L.M;
     if (!net || n < 1 || n_features < 1 || !features || n_grid < 2 || !n_intervals || !tspans || !y0_plain ||
         (h->desc.n_params > 0 && !params))
@@ -1862,7 +1862,7 @@ bvp_status bvp_solve_batch_device_grid(bvp_handle* h, int32_t n, const double* d
                                        const int32_t* d_n_intervals, const double* d_tspans, const float* d_grid,
                                        int32_t n_grid, int32_t max_intervals) {
     if (!h) return BVP_ERR_INVALID;
-    if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: only bvp_solve_batch is available");
+    if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: bvp_solve_batch and bvp_solve_batch_device only");
     if (n < 1 || !d_n_intervals || !d_tspans || !d_grid || n_grid < 2 || max_intervals < 1 ||
         (h->desc.n_params > 0 && !d_params))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
@@ -2017,7 +2017,7 @@ bvp_status bvp_eval_stage(bvp_handle* h, int32_t stage, int32_t n, const double*
                           const double* mesh, const double* y, double* norm, double* F, double* bc_res,
                           double* K, double* S, double* R, double* delta, double* err) {
     if (!h) return BVP_ERR_INVALID;
-    if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: only bvp_solve_batch is available");
+    if (h->large) return fail(h, BVP_ERR_INVALID, "state dimension above 8: bvp_solve_batch and bvp_solve_batch_device only");
     if (h->firk) return fail(h, BVP_ERR_INVALID, "the stage kernels are MIRK's: not available on the FIRK path");
     if (stage < 0 || stage > 3 || n < 1 || !n_nodes || !mesh || !y || (h->desc.n_params > 0 && !params))
         return fail(h, BVP_ERR_INVALID, "invalid arguments");
